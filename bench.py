@@ -1,0 +1,444 @@
+"""Benchmark: vertex-updates/s of the GPE stepper on one GB300 (or N replicas).
+
+Default workload (the batched configuration the headline metric is quoted on):
+64 independent condensates on the BCC2 lattice, grid edge per instance uniform
+over {24, 32, 48, 64, 96} cells (seed 2), g log-uniform in [100, 5000], trap
+frequencies per axis uniform in [0.5, 2], Gaussian initial state with 1e-3
+noise, dt = 1e-4; FP32 storage and arithmetic, trap potential evaluated in the
+kernel, one fused launch per half-step for the whole batch, CUDA graphs of 100
+steps.  One bench step = one leapfrog step (two half-steps) of every instance.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  Multi-GPU: replicas only (the batch is
+independent condensates; each rank advances its own copy; no collective on the
+data path), value = all ranks' vertex-updates / max-over-ranks time.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "vertex-updates/s"
+BYTES_PER_VERTEX_STEP = 48  # FP32, trap potential in-kernel: 2 half-steps x (read prev 8 B + RMW next 16 B)
+L2_BYTES = 129e6
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _profile_traffic():
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "fused_bcc2_batch64.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch_full_batch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _init_pg(ws, backend):
+    if ws > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group(backend=backend)
+        return dist
+    return None
+
+
+def _max_over_ranks(dist, v, device=None):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_batch():
+    from vaikkari_gb300 import workloads
+    return workloads.config4()
+
+
+def prepare_fields(stepper, conds, precision_dtype):
+    """Uploads the batch; odd = even * exp(i mu dt / 2) with mu from the library's
+    observables of the initial field (GPUGrossPitaevskii_BCC.cu:325,342)."""
+    from vaikkari_gb300.workloads import odd_from_even
+    for i, c in enumerate(conds):
+        stepper.upload(i, c.psi, c.psi, c.V)
+    obs = stepper.observables(0)
+    evens, odds = [], []
+    for i, c in enumerate(conds):
+        odd = odd_from_even(c.psi, obs[i]["mu"], c.inst.dt)
+        evens.append(np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1).astype(precision_dtype)))
+        odds.append(np.ascontiguousarray(np.stack([odd.real, odd.imag], -1).astype(precision_dtype)))
+        stepper.upload(i, evens[-1], odds[-1], c.V)
+    return evens, odds
+
+
+def cpu_sample(conds, evens64, odds64, budget_s, threads):
+    """Oracle FP64 leapfrog (the reference's update restated in C, all threads)
+    over the batch, as many whole steps as fit the time budget (>= 1)."""
+    import oracle.oracle as orc
+    from vaikkari_gb300.gpe import Lattice, lattice_info
+    info = lattice_info(Lattice.BCC2)
+    orc.set_threads(threads)
+    grids, vdts, es, os_ = [], [], [], []
+    for c, e, o in zip(conds, evens64, odds64):
+        inst = c.inst
+        g = orc.Grid(inst.nx, inst.ny, inst.nz, info["entry"], info["class_weight"], inst.block_scale, inst.dt,
+                     inst.g)
+        from vaikkari_gb300.gpe import value_positions
+        from vaikkari_gb300.workloads import harmonic
+        vdt = np.ascontiguousarray(harmonic(value_positions(inst, info), inst.trap) * inst.dt)
+        grids.append(g)
+        vdts.append(vdt)
+        es.append(e.copy())
+        os_.append(o.copy())
+    verts = sum(c.inst.nx * c.inst.ny * c.inst.nz * 2 for c in conds)
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        for g, e, o, v in zip(grids, es, os_, vdts):
+            g.leapfrog(e, o, v, 1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 1000:
+            break
+    return verts * steps / el, steps, el, verts
+
+
+def run_reference(args):
+    """--impl reference: the reference's update loop on the host cores.  The
+    reference's stepping exists only as a CUDA kernel, so this runs the oracle
+    port (its update and leapfrog restated in C, FP64, OpenMP over all host
+    threads); each step is one leapfrog step over a bounded sample of the batch."""
+    ws, rank, local = _dist()
+    if rank != 0:
+        return 0
+    import oracle.oracle as orc
+    from vaikkari_gb300.gpe import Lattice, lattice_info, value_positions
+    from vaikkari_gb300.workloads import harmonic
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    conds = build_batch()
+    info = lattice_info(Lattice.BCC2)
+    items = []
+    for c in conds:
+        inst = c.inst
+        g = orc.Grid(inst.nx, inst.ny, inst.nz, info["entry"], info["class_weight"], inst.block_scale, inst.dt,
+                     inst.g)
+        e = np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1))
+        vdt = np.ascontiguousarray(harmonic(value_positions(inst, info), inst.trap) * inst.dt)
+        items.append((g, e, e.copy(), vdt, inst.nx * inst.ny * inst.nz * 2))
+    # calibrate on one step of the whole batch, then bound the per-step sample so
+    # that warmup + steps fit in about two minutes
+    t0 = time.perf_counter()
+    for g, e, o, v, n in items:
+        g.leapfrog(e, o, v, 1)
+    full = time.perf_counter() - t0
+    per_step_budget = 120.0 / max(args.steps + args.warmup, 1)
+    frac = min(1.0, per_step_budget / max(full, 1e-9))
+    total = sum(it[4] for it in items)
+    sample, acc = [], 0
+    for it in items:
+        if sample and acc + it[4] > frac * total:
+            break
+        sample.append(it)
+        acc += it[4]
+    for _ in range(args.warmup):
+        for g, e, o, v, n in sample:
+            g.leapfrog(e, o, v, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for g, e, o, v, n in sample:
+            g.leapfrog(e, o, v, 1)
+    el = time.perf_counter() - t0
+    value = acc * args.steps / el
+    desc = (f"{len(sample)} of {len(items)} instances ({acc} of {total} vertices) per step, FP64 oracle port of "
+            f"GPUGrossPitaevskii_BCC.cu:176-216,475-481, {threads} threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "batch64_bcc2_realtime", "instances": len(items), "sample_instances": len(sample),
+                   "vertices_per_step": acc, "dt": 1e-4, "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    ws, rank, local = _dist()
+    import torch
+    torch.cuda.set_device(local)
+    dist = _init_pg(ws, "nccl")
+    from vaikkari_gb300.gpe import Kernel, Lattice, Mode, Potential, Precision, Stepper
+    conds = build_batch()
+    insts = [c.inst for c in conds]
+    verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
+    st = Stepper(insts, lattice=Lattice.BCC2, precision=Precision.FP32, kernel=Kernel.FUSED,
+                 potential=Potential.TRAP, graph_steps=100, tile=args.tile, zchunk=args.zchunk, device=local)
+    evens, odds = prepare_fields(st, conds, np.float32)
+
+    # Warm-up: W steps, plus one replay of the 100-step graph so that the
+    # graph is instantiated before the timed region.
+    st.step(args.warmup)
+    st.step(100)
+    st.synchronize()
+    stream = torch.cuda.ExternalStream(st.stream_handle(), device=local)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    n0 = st.launch_count()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        st.step(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = st.launch_count() - n0
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        dist.barrier()
+    ms_max = _max_over_ranks(dist, ms, device=torch.device("cuda", local))
+    value = verts * ws * args.steps / (ms_max * 1e-3)
+
+    # Roofline of the fused kernel: it is the only kernel in the timed region
+    # (two launches per step), so the average launch lasts ms / launches.
+    peak, peak_kind = _peaks()
+    per_launch_s = (ms * 1e-3) / max(launches, 1)
+    achieved = verts * (BYTES_PER_VERTEX_STEP / 2) / per_launch_s / 1e9
+    traffic = _profile_traffic()
+
+    # End to end through the public API with pinned host buffers: upload every
+    # instance, run the steps, read the observables, download every field.
+    pinned_e, pinned_o = [], []
+    for e, o in zip(evens, odds):
+        pe = torch.empty(e.shape, dtype=torch.float32, pin_memory=True).numpy()
+        po = torch.empty(o.shape, dtype=torch.float32, pin_memory=True).numpy()
+        pe[...] = e
+        po[...] = o
+        pinned_e.append(pe)
+        pinned_o.append(po)
+    h2d = sum(a.nbytes for a in pinned_e) + sum(a.nbytes for a in pinned_o)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(len(insts)):
+        st.upload(i, pinned_e[i], pinned_o[i], None)
+    st.step(args.steps)
+    obs = st.observables(0)
+    for i in range(len(insts)):
+        st.lib.gpe_download(st.h, i, pinned_e[i].ctypes.data, pinned_o[i].ctypes.data)
+    st.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_s = _max_over_ranks(dist, e2e_s, device=torch.device("cuda", local))
+    e2e_value = verts * ws * args.steps / e2e_s
+    finite = all(o["finite"] for o in obs)
+    st.close()
+
+    # Accuracy at this workload: FP32 vs FP64 (same scheme) after 1000 steps.
+    acc = None
+    if rank == 0 and not args.skip_accuracy:
+        acc = accuracy_block(conds, insts, local)
+
+    # The FP64 plain path, one instance at a time (the drop-in denominator).
+    fp64 = None
+    if rank == 0 and not args.skip_fp64:
+        fp64 = fp64_plain_rate(conds, insts, local, args.fp64_steps)
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        e64 = [np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1)) for c in conds]
+        o64 = [a.copy() for a in e64]
+        threads = os.cpu_count() or 1
+        v, steps, el, nv = cpu_sample(conds, e64, o64, args.cpu_budget, threads)
+        cpu = {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+               "sample": f"{steps} leapfrog step(s) of the whole batch ({nv} vertices), FP64 oracle port, "
+                         f"{el:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch64_bcc2_fp32_trap_realtime", "instances": len(insts),
+                       "vertices": verts, "sizes": sorted({i.nx for i in insts}), "dt": 1e-4,
+                       "graph_steps": 100, "kernel": "fused", "tile": args.tile,
+                       "parallelism": f"replicas{ws}" if ws > 1 else "single",
+                       "l2": f"inputs larger than L2 (fields {2 * 8 * verts / 1e6:.0f} MB vs {L2_BYTES / 1e6:.0f} MB)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "algorithmic_bytes_per_vertex_step": BYTES_PER_VERTEX_STEP,
+                         "peak_source": f"{peak_kind} hbm_gbs", "kernel": "fused_bcc2_kernel"},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+                    "steps_per_call": args.steps, "seconds": e2e_s, "finite": finite},
+            "cpu_baseline": cpu,
+            "accuracy": acc,
+            "fp64_plain": fp64,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def accuracy_block(conds, insts, device):
+    from vaikkari_gb300.gpe import Kernel, Lattice, Potential, Precision, Stepper
+    steps = 1000
+    res = {}
+    outs = {}
+    for prec, dt_ in ((Precision.FP32, np.float32), (Precision.FP64, np.float64)):
+        st = Stepper(insts, lattice=Lattice.BCC2, precision=prec, kernel=Kernel.FUSED, potential=Potential.TRAP,
+                     graph_steps=100, device=device)
+        prepare_fields(st, conds, dt_)
+        o0 = st.observables(0)
+        st.step(steps)
+        o1 = st.observables(0)
+        fields = [st.download(i, odd=False)[0].astype(np.float64) for i in range(len(insts))]
+        st.close()
+        outs[prec] = (o0, o1, fields)
+    num = sum(float(np.sum((a - b) ** 2)) for a, b in zip(outs[Precision.FP32][2], outs[Precision.FP64][2]))
+    den = sum(float(np.sum(b ** 2)) for b in outs[Precision.FP64][2])
+    n32 = [o["norm"] for o in outs[Precision.FP32][1]]
+    n64 = [o["norm"] for o in outs[Precision.FP64][1]]
+    e32 = [o["energy"] for o in outs[Precision.FP32][1]]
+    e64 = [o["energy"] for o in outs[Precision.FP64][1]]
+    n0 = [o["norm"] for o in outs[Precision.FP64][0]]
+    res["steps"] = steps
+    res["rel_l2_fp32_vs_fp64"] = math.sqrt(num / den)
+    res["max_norm_drift_fp32_vs_fp64"] = max(abs(a - b) / b for a, b in zip(n32, n64))
+    res["max_energy_drift_fp32_vs_fp64"] = max(abs(a - b) / abs(b) for a, b in zip(e32, e64))
+    res["max_norm_drift_fp64_scheme"] = max(abs(a - b) / b for a, b in zip(n64, n0))
+    return res
+
+
+def fp64_plain_rate(conds, insts, device, steps):
+    """The plain FP64 path, one instance at a time, same inputs and trap form."""
+    import torch
+    from vaikkari_gb300.gpe import Kernel, Lattice, Potential, Precision, Stepper
+    total_ms = 0.0
+    verts_total = 0
+    for c in conds:
+        st = Stepper([c.inst], lattice=Lattice.BCC2, precision=Precision.FP64, kernel=Kernel.PLAIN,
+                     potential=Potential.TRAP, graph_steps=100, device=device)
+        prepare_fields(st, [c], np.float64)
+        st.step(3)
+        st.step(100)
+        st.synchronize()
+        stream = torch.cuda.ExternalStream(st.stream_handle(), device=device)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        st.step(steps)
+        b.record(stream)
+        torch.cuda.synchronize()
+        total_ms += a.elapsed_time(b)
+        verts_total += c.inst.nx * c.inst.ny * c.inst.nz * 2
+        st.close()
+    value = verts_total * steps / (total_ms * 1e-3)
+    return {"value": value, "unit": METRIC, "steps": steps, "dtype": "f64", "kernel": "plain",
+            "note": "each instance advanced alone (one launch per instance per half-step)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--zchunk", type=int, default=0)
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--fp64-steps", type=int, default=200)
+    ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

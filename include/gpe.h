@@ -1,0 +1,193 @@
+/*
+ * gpe.h - C ABI of vaikkari_gb300, a Gross-Pitaevskii time-stepper for one
+ * NVIDIA GB300 (sm_103a).
+ *
+ * It integrates  i d(psi)/dt = (-1/2 Lap + V + g |psi|^2) psi  on the DEC
+ * discretisation of a body-centred-cubic tetrahedral mesh with the explicit
+ * staggered leapfrog of the reference solver (markus-kivioja/vaikkari,
+ * koodit/GrossPitaevskii/GPUGrossPitaevskii_BCC.cu), plus an imaginary-time
+ * (ground-state) mode.  Many independent condensates ("instances") of uneven
+ * sizes, couplings and traps advance together.
+ *
+ * Replaces, in the reference:
+ *   integrateInTime(state, block_scale, minp, maxp, iteration_period, iterations)
+ *       koodit/GrossPitaevskii/GPUGrossPitaevskii_BCC.cu:218-499
+ *       -> gpe_create + gpe_upload + gpe_step + gpe_download + gpe_destroy, or in
+ *          one call gpe_integrate_in_time (the drop-in driver).
+ *   __global__ update(next, prev, potentials, lapind, lapfacs, g, dimensions)
+ *       GPUGrossPitaevskii_BCC.cu:176-216 (and its copies in the multi-GPU and
+ *       MPI variants) -> the half-step inside gpe_step.
+ *   getLaplacian / getPositions (GPUGrossPitaevskii_BCC.cu:69-142)
+ *       -> gpe_lattice_describe.
+ *   The reference reports errors by exit(EXIT_FAILURE) (helper_cuda.h
+ *   checkCudaErrors, GPUGrossPitaevskii_BCC.cu:491-496); every call here
+ *   returns a gpe_status instead and never exits.
+ *
+ * Host arrays use the reference's block order: index
+ *   (((z * ny) + y) * nx + x) * slots + slot
+ * for block (x, y, z) and value `slot` of that block; complex values are
+ * interleaved (re, im).  The element type follows the handle's precision
+ * (double for GPE_FP64, float for GPE_FP32).
+ *
+ * Threading: one handle per host thread; a handle owns its CUDA stream.
+ */
+#ifndef VAIKKARI_GB300_GPE_H
+#define VAIKKARI_GB300_GPE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPE_ABI_VERSION 1
+
+typedef enum gpe_status {
+    GPE_OK = 0,
+    GPE_ERR_INVALID_ARGUMENT = 1, /* bad size, pointer, enum or state           */
+    GPE_ERR_CUDA = 2,             /* a CUDA runtime call failed (see gpe_last_error) */
+    GPE_ERR_OUT_OF_MEMORY = 3,    /* device or pinned host allocation failed     */
+    GPE_ERR_NOT_FINITE = 4,       /* NaN/Inf seen by the observables watchdog    */
+    GPE_ERR_UNSUPPORTED = 5,      /* combination not built (e.g. fused TETRA12)  */
+    GPE_ERR_TOO_LARGE = 6,        /* size beyond a documented maximum            */
+    GPE_ERR_INTERNAL = 7          /* lattice construction failed a self-check    */
+} gpe_status;
+
+typedef enum gpe_lattice {
+    /* Reference discretisation: 12 values per block at the circumcentres of the
+     * BCC Delaunay tetrahedra, 4 neighbours each (GPUGrossPitaevskii_BCC.cu:69-142).
+     * block_scale = the reference's block_scale; block edge = sqrt(8)*block_scale. */
+    GPE_LATTICE_TETRA12 = 0,
+    /* Primal-node discretisation: 2 values per block (cube corner + centre),
+     * 14 Hodge-weighted edges (8 diagonal, 6 axial); block_scale = cube edge. */
+    GPE_LATTICE_BCC2 = 1
+} gpe_lattice;
+
+typedef enum gpe_precision { GPE_FP64 = 0, GPE_FP32 = 1 } gpe_precision;
+
+typedef enum gpe_time_mode {
+    GPE_REAL_TIME = 0,      /* staggered leapfrog, two fields (even, odd)      */
+    GPE_IMAGINARY_TIME = 1  /* psi <- normalise(psi - dt H psi), one field      */
+} gpe_time_mode;
+
+typedef enum gpe_kernel_kind {
+    GPE_KERNEL_AUTO = 0,   /* fused where built (BCC2), plain otherwise          */
+    GPE_KERNEL_PLAIN = 1,  /* table-driven, one value per thread, any lattice    */
+    GPE_KERNEL_FUSED = 2   /* BCC2 only: shared-memory tiled, z-marching, batched */
+} gpe_kernel_kind;
+
+typedef enum gpe_potential_kind {
+    GPE_POTENTIAL_ARRAY = 0, /* V uploaded per value with gpe_upload               */
+    GPE_POTENTIAL_TRAP = 1   /* V = 0.5*(trap[0] x^2 + trap[1] y^2 + trap[2] z^2),
+                                evaluated in the kernel from per-axis tables       */
+} gpe_potential_kind;
+
+#define GPE_MAX_SLOTS 12
+#define GPE_MAX_NEIGHBOURS 14
+#define GPE_MAX_CLASSES 2
+
+/* Stencil of a lattice, as the kernels apply it. */
+typedef struct gpe_lattice_info {
+    int32_t lattice;                 /* gpe_lattice                                  */
+    int32_t slots;                   /* values per block                             */
+    int32_t neighbours;              /* neighbours per value                         */
+    int32_t classes;                 /* distinct Laplacian weights                   */
+    double block_width;              /* block edge / block_scale                     */
+    double cell_volume;              /* volume per value / block_scale^3             */
+    double class_weight[GPE_MAX_CLASSES]; /* weight per class * block_scale^2        */
+    double position[GPE_MAX_SLOTS][3];    /* value position in its block / block_scale */
+    /* (dx, dy, dz, slot, class) of each neighbour, in summation order */
+    int32_t entry[GPE_MAX_SLOTS][GPE_MAX_NEIGHBOURS][5];
+} gpe_lattice_info;
+
+/* One condensate. */
+typedef struct gpe_instance {
+    int32_t nx, ny, nz;   /* blocks per axis (>= 1)                                     */
+    double block_scale;   /* length unit of the lattice (see gpe_lattice)               */
+    double origin[3];     /* position of the low corner of block (0,0,0)                */
+    double dt;            /* time step                                                  */
+    double g;             /* interaction strength                                       */
+    double trap[3];       /* harmonic trap coefficients (GPE_POTENTIAL_TRAP only)       */
+} gpe_instance;
+
+typedef struct gpe_config {
+    int32_t lattice;        /* gpe_lattice        */
+    int32_t precision;      /* gpe_precision      */
+    int32_t mode;           /* gpe_time_mode      */
+    int32_t kernel;         /* gpe_kernel_kind    */
+    int32_t potential;      /* gpe_potential_kind */
+    int32_t num_instances;  /* >= 1               */
+    const gpe_instance *instances;
+    int32_t graph_steps;    /* steps per captured CUDA graph; 0 = 100, < 0 = no graphs */
+    int32_t tile;           /* fused-kernel tile variant; 0 = autotuned/default   */
+    int32_t zchunk;         /* planes per work item of the fused kernel; 0 = auto  */
+    int32_t device;         /* CUDA device ordinal                                 */
+} gpe_config;
+
+/* Observables of one instance, all in FP64 (Kahan-compensated sums):
+ *   norm        = sum vol |psi|^2
+ *   kinetic     = sum vol Re(conj(psi) (-1/2 Lap psi))
+ *   potential   = sum vol V |psi|^2
+ *   interaction = sum vol g/2 |psi|^4
+ *   energy      = kinetic + potential + interaction
+ *   mu          = (kinetic + potential + 2 interaction) / norm                  */
+typedef struct gpe_observables {
+    double norm, energy, mu, kinetic, potential, interaction;
+    int32_t finite; /* 0 if any sum is NaN/Inf */
+    int32_t pad_;
+} gpe_observables;
+
+typedef struct gpe_handle_ *gpe_handle;
+
+/* Version of this ABI (GPE_ABI_VERSION). */
+int32_t gpe_abi_version(void);
+const char *gpe_status_string(gpe_status s);
+/* Message of the last failing call on this host thread ("" if none). */
+const char *gpe_last_error(void);
+
+/* Stencil tables derived from the lattice geometry.
+ * Replaces getLaplacian/getPositions, GPUGrossPitaevskii_BCC.cu:69-142. */
+gpe_status gpe_lattice_describe(int32_t lattice, gpe_lattice_info *out);
+
+/* Allocates device memory for all instances (fields zeroed).  Replaces the
+ * allocation and set-up part of integrateInTime, GPUGrossPitaevskii_BCC.cu:268-405. */
+gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out);
+gpe_status gpe_destroy(gpe_handle h);
+
+/* Copies one instance's fields to the device.  even/odd: complex values in block
+ * order; potential: V per value (unscaled; required for GPE_POTENTIAL_ARRAY,
+ * ignored otherwise).  odd may be NULL in imaginary time.  Replaces the host
+ * staging and cudaMemcpy3D of GPUGrossPitaevskii_BCC.cu:313-392. */
+gpe_status gpe_upload(gpe_handle h, int32_t instance, const void *even, const void *odd,
+                      const void *potential);
+/* Copies one instance's fields back (either pointer may be NULL). */
+gpe_status gpe_download(gpe_handle h, int32_t instance, void *even, void *odd);
+
+/* Real time: advances every instance by `steps` leapfrog steps (odd <- even,
+ * then even <- odd; GPUGrossPitaevskii_BCC.cu:475-481).  Imaginary time:
+ * `steps` normalised Euler steps.  Asynchronous on the handle's stream. */
+gpe_status gpe_step(gpe_handle h, int64_t steps);
+gpe_status gpe_synchronize(gpe_handle h);
+
+/* Observables of field 0 (even / psi) or 1 (odd) for every instance;
+ * out has num_instances entries.  Returns GPE_ERR_NOT_FINITE if any is NaN/Inf. */
+gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out);
+
+/* Imaginary time until |mu_k - mu_{k-1}| < tol for every instance or max_steps.
+ * Steps run in graph-sized chunks; convergence is checked on the device each step
+ * and the host polls between chunks.  Outputs may be NULL. */
+gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64_t *steps_done,
+                              int32_t *converged, double *mu_out);
+
+/* Kernel launches the handle has issued (for accounting). */
+int64_t gpe_launch_count(gpe_handle h);
+
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or record CUDA events against the library's launches. */
+void *gpe_stream(gpe_handle h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VAIKKARI_GB300_GPE_H */

@@ -1,0 +1,213 @@
+/*
+ * gpe_oracle.c - CPU oracle for the GPE stepper (test infrastructure only; see
+ * gpe_oracle.h).  Build: make -C oracle oracle  (or vaikkari_gb300.build), with
+ * -ffp-contract=off so that a*b+c is never fused behind our back: every fused
+ * multiply-add below is an explicit fma()/fmaf(), matching the GPU kernels.
+ */
+#include "gpe_oracle.h"
+
+#include <math.h>
+#include <stddef.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static int g_threads = 0;
+
+void oracle_set_threads(int n) { g_threads = n; }
+int oracle_get_threads(void)
+{
+#ifdef _OPENMP
+    return g_threads > 0 ? g_threads : omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+#define IDX(g, x, y, z, s) (((((size_t)(z) * (g)->ny) + (size_t)(y)) * (g)->nx + (size_t)(x)) * (g)->slots + (size_t)(s))
+
+/*
+ * The per-value update, GPUGrossPitaevskii_BCC.cu:207-215:
+ *   sum  = lapfac * (n0 + n1 + n2 + n3) + (lapfac0 + pot + g*|prev|^2) * prev
+ *   next += (sum.y, -sum.x)
+ * generalised to per-class neighbour sums S[c] and weights Lc[c]:
+ *   nrm = fma(p.x, p.x, p.y*p.y);  c = fma(gdt, nrm, L0 + vdt)
+ *   a   = Lc[0]*S[0] (then a = fma(Lc[c], S[c], a));  h = fma(c, p, a)
+ * Out-of-grid neighbours are zero (the reference's padding blocks, :269-287).
+ */
+#define HALF_STEP_BODY(T, FMA)                                                                      \
+    const int ns = g->slots, nb = g->neighbours;                                                   \
+    const T L0 = (T)g->L0, gdt = (T)g->gdt;                                                         \
+    const T Lc0 = (T)g->Lc[0], Lc1 = (T)g->Lc[1];                                                   \
+    int z;                                                                                          \
+    _Pragma("omp parallel for schedule(static) num_threads(oracle_get_threads())")                  \
+    for (z = 0; z < g->nz; z++) {                                                                   \
+        for (int y = 0; y < g->ny; y++)                                                             \
+            for (int x = 0; x < g->nx; x++)                                                         \
+                for (int s = 0; s < ns; s++) {                                                      \
+                    T sx[2] = {0, 0}, sy[2] = {0, 0};                                               \
+                    int seen[2] = {0, 0};                                                           \
+                    int ncls = 1;                                                                   \
+                    for (int k = 0; k < nb; k++) {                                                  \
+                        const int *e = g->entry + ((size_t)s * nb + k) * 5;                         \
+                        const int xx = x + e[0], yy = y + e[1], zz = z + e[2], c = e[4];            \
+                        T vx = 0, vy = 0;                                                           \
+                        if (xx >= 0 && xx < g->nx && yy >= 0 && yy < g->ny && zz >= 0 && zz < g->nz) { \
+                            const size_t o = IDX(g, xx, yy, zz, e[3]);                              \
+                            vx = prev[2 * o];                                                       \
+                            vy = prev[2 * o + 1];                                                   \
+                            if (mode == 1) {                                                        \
+                                vx = sigma * vx;                                                    \
+                                vy = sigma * vy;                                                    \
+                            }                                                                       \
+                        }                                                                           \
+                        if (c + 1 > ncls) ncls = c + 1;                                             \
+                        if (!seen[c]) {                                                             \
+                            sx[c] = vx;                                                             \
+                            sy[c] = vy;                                                             \
+                            seen[c] = 1;                                                            \
+                        } else {                                                                    \
+                            sx[c] = sx[c] + vx;                                                     \
+                            sy[c] = sy[c] + vy;                                                     \
+                        }                                                                           \
+                    }                                                                               \
+                    const size_t o = IDX(g, x, y, z, s);                                            \
+                    T px = prev[2 * o], py = prev[2 * o + 1];                                       \
+                    if (mode == 1) {                                                                \
+                        px = sigma * px;                                                            \
+                        py = sigma * py;                                                            \
+                    }                                                                               \
+                    const T nrm = FMA(px, px, py * py);                                             \
+                    const T cc = FMA(gdt, nrm, L0 + vdt[o]);                                        \
+                    T ax = Lc0 * sx[0], ay = Lc0 * sy[0];                                           \
+                    if (ncls > 1) {                                                                 \
+                        ax = FMA(Lc1, sx[1], ax);                                                   \
+                        ay = FMA(Lc1, sy[1], ay);                                                   \
+                    }                                                                               \
+                    const T hx = FMA(cc, px, ax), hy = FMA(cc, py, ay);                             \
+                    if (mode == 0) {                                                                \
+                        next[2 * o] = next[2 * o] + hy;                                             \
+                        next[2 * o + 1] = next[2 * o + 1] - hx;                                     \
+                    } else {                                                                        \
+                        next[2 * o] = px - hx;                                                      \
+                        next[2 * o + 1] = py - hy;                                                  \
+                    }                                                                               \
+                }                                                                                   \
+    }
+
+void oracle_half_step_f64(const oracle_grid *g, const double *prev, double *next, const double *vdt, int mode,
+                          double sigma)
+{
+    HALF_STEP_BODY(double, fma)
+}
+
+void oracle_half_step_f32(const oracle_grid *g, const float *prev, float *next, const float *vdt, int mode,
+                          float sigma)
+{
+    HALF_STEP_BODY(float, fmaf)
+}
+
+/* GPUGrossPitaevskii_BCC.cu:475-481: update odd from even, then even from odd. */
+void oracle_leapfrog_f64(const oracle_grid *g, double *even, double *odd, const double *vdt, long steps)
+{
+    for (long k = 0; k < steps; k++) {
+        oracle_half_step_f64(g, even, odd, vdt, 0, 1.0);
+        oracle_half_step_f64(g, odd, even, vdt, 0, 1.0);
+    }
+}
+
+void oracle_leapfrog_f32(const oracle_grid *g, float *even, float *odd, const float *vdt, long steps)
+{
+    for (long k = 0; k < steps; k++) {
+        oracle_half_step_f32(g, even, odd, vdt, 0, 1.0f);
+        oracle_half_step_f32(g, odd, even, vdt, 0, 1.0f);
+    }
+}
+
+typedef struct {
+    double s, c;
+} kahan_t;
+
+static void kahan_add(kahan_t *k, double v)
+{
+    const double y = v - k->c;
+    const double t = k->s + y;
+    k->c = (t - k->s) - y;
+    k->s = t;
+}
+
+#define OBSERVABLES_BODY(T)                                                                          \
+    const int ns = g->slots, nb = g->neighbours;                                                    \
+    double wsum = 0.0;                                                                               \
+    for (int k = 0; k < nb; k++) wsum += w[g->entry[k * 5 + 4]];                                     \
+    kahan_t k0 = {0, 0}, k1 = {0, 0}, k2 = {0, 0}, k3 = {0, 0};                                      \
+    for (int z = 0; z < g->nz; z++)                                                                  \
+        for (int y = 0; y < g->ny; y++)                                                              \
+            for (int x = 0; x < g->nx; x++)                                                          \
+                for (int s = 0; s < ns; s++) {                                                       \
+                    double lx = 0.0, ly = 0.0;                                                       \
+                    for (int k = 0; k < nb; k++) {                                                   \
+                        const int *e = g->entry + ((size_t)s * nb + k) * 5;                          \
+                        const int xx = x + e[0], yy = y + e[1], zz = z + e[2];                       \
+                        if (xx < 0 || xx >= g->nx || yy < 0 || yy >= g->ny || zz < 0 || zz >= g->nz) \
+                            continue;                                                                \
+                        const size_t o = IDX(g, xx, yy, zz, e[3]);                                   \
+                        lx += w[e[4]] * (double)psi[2 * o];                                          \
+                        ly += w[e[4]] * (double)psi[2 * o + 1];                                      \
+                    }                                                                                \
+                    const size_t o = IDX(g, x, y, z, s);                                             \
+                    const double px = (double)psi[2 * o], py = (double)psi[2 * o + 1];               \
+                    lx -= wsum * px;                                                                 \
+                    ly -= wsum * py;                                                                 \
+                    const double n2 = px * px + py * py;                                             \
+                    kahan_add(&k0, n2);                                                              \
+                    kahan_add(&k1, -0.5 * (px * lx + py * ly));                                      \
+                    kahan_add(&k2, ((double)vdt[o] / dt) * n2);                                      \
+                    kahan_add(&k3, 0.5 * gcoef * n2 * n2);                                           \
+                }                                                                                    \
+    out[0] = k0.s;                                                                                   \
+    out[1] = k1.s;                                                                                   \
+    out[2] = k2.s;                                                                                   \
+    out[3] = k3.s;
+
+void oracle_observables_f64(const oracle_grid *g, const double *psi, const double *vdt, double dt, double gcoef,
+                            const double *w, double *out)
+{
+    OBSERVABLES_BODY(double)
+}
+
+void oracle_observables_f32(const oracle_grid *g, const float *psi, const float *vdt, double dt, double gcoef,
+                            const double *w, double *out)
+{
+    OBSERVABLES_BODY(float)
+}
+
+long oracle_imaginary_f64(const oracle_grid *g, double *psi, double *work, const double *vdt, double dt,
+                          double gcoef, const double *w, double vol, long steps, double tol, double *mu_hist)
+{
+    const size_t n = (size_t)g->nx * g->ny * g->nz * g->slots * 2;
+    double *cur = psi, *nxt = work;
+    double mu_prev = 0.0;
+    long conv = -1;
+    for (long k = 0; k < steps; k++) {
+        double s[4];
+        oracle_observables_f64(g, cur, vdt, dt, gcoef, w, s);
+        const double nn = vol * s[0];
+        const double mu = vol * (s[1] + s[2]) / nn + 2.0 * vol * s[3] / (nn * nn);
+        if (mu_hist) mu_hist[k] = mu;
+        if (k > 0 && conv < 0 && fabs(mu - mu_prev) < tol) conv = k;
+        mu_prev = mu;
+        oracle_half_step_f64(g, cur, nxt, vdt, 1, 1.0 / sqrt(nn));
+        double *t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    double s[4];
+    oracle_observables_f64(g, cur, vdt, dt, gcoef, w, s);
+    const double sig = 1.0 / sqrt(vol * s[0]);
+    for (size_t i = 0; i < n; i++) cur[i] = sig * cur[i];
+    if (cur != psi) memcpy(psi, cur, n * sizeof(double));
+    return conv;
+}

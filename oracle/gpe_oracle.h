@@ -1,0 +1,72 @@
+/*
+ * gpe_oracle.h - CPU oracle for the GPE stepper.  TEST INFRASTRUCTURE ONLY:
+ * loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as
+ * the checker; never part of the shipped library.
+ *
+ * A plain-C restatement of the reference's algorithm
+ * (markus-kivioja/vaikkari, koodit/GrossPitaevskii/GPUGrossPitaevskii_BCC.cu):
+ *   - update():        :176-216 (neighbour sum, potential, nonlinearity, next -= i*sum)
+ *   - dt scaling:      :289-307 (lapfac = -0.5*hodge/bs^2*dt, lapfac0 = -sum(lapfac))
+ *   - leapfrog order:  :475-481 (odd <- even, then even <- odd)
+ *   - zero padding:    :269-287 (psi = 0 outside the block grid)
+ * over a generic neighbour table (the reference's 48-entry table of :90-142, or
+ * the 14-edge BCC table); the imaginary-time step and the observables have no
+ * counterpart in the reference and are restated from their definitions.
+ *
+ * Layout: the reference's block order, index (((z*ny)+y)*nx+x)*slots+s;
+ * complex values interleaved (re, im).
+ *
+ * The _f32 functions perform exactly the rounded operations of the GPU kernels
+ * (fmaf/multiply/add in the same order, no contraction), so the GPU FP32 path
+ * can be compared bit for bit; the _f64 functions do the same in double.
+ */
+#ifndef GPE_ORACLE_H
+#define GPE_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_grid {
+    int nx, ny, nz;
+    int slots, neighbours;
+    const int *entry;   /* slots*neighbours*5: (dx, dy, dz, slot, class), classes ascending per slot */
+    double Lc[2];       /* -0.5 * w_c * dt */
+    double L0;          /* 0.5 * dt * sum of weights */
+    double gdt;         /* g * dt */
+} oracle_grid;
+
+/* One half-step.  mode 0: next += -i*h(prev); mode 1: next = p - h(p) with
+ * p = sigma*prev (imaginary time).  vdt = V*dt per value. */
+void oracle_half_step_f64(const oracle_grid *g, const double *prev, double *next, const double *vdt, int mode,
+                          double sigma);
+void oracle_half_step_f32(const oracle_grid *g, const float *prev, float *next, const float *vdt, int mode,
+                          float sigma);
+
+/* `steps` leapfrog steps (odd <- even, even <- odd). */
+void oracle_leapfrog_f64(const oracle_grid *g, double *even, double *odd, const double *vdt, long steps);
+void oracle_leapfrog_f32(const oracle_grid *g, float *even, float *odd, const float *vdt, long steps);
+
+/* Sums over values (no volume factor), Kahan-compensated, sequential order:
+ * out[0] = |psi|^2, out[1] = Re(conj(psi) * (-1/2 Lap psi)), out[2] = V|psi|^2,
+ * out[3] = g/2 |psi|^4.  w = unscaled class weights; vdt/dt recovers V. */
+void oracle_observables_f64(const oracle_grid *g, const double *psi, const double *vdt, double dt, double gcoef,
+                            const double *w, double *out);
+void oracle_observables_f32(const oracle_grid *g, const float *psi, const float *vdt, double dt, double gcoef,
+                            const double *w, double *out);
+
+/* Imaginary time in FP64: `steps` normalised Euler steps of psi (psi and work
+ * ping-pong; the result ends in psi, normalised).  mu_hist[k] (may be NULL)
+ * receives mu of the normalised field entering step k.  Returns the first step
+ * with |mu_k - mu_{k-1}| < tol, or -1.  vol = volume per value. */
+long oracle_imaginary_f64(const oracle_grid *g, double *psi, double *work, const double *vdt, double dt,
+                          double gcoef, const double *w, double vol, long steps, double tol, double *mu_hist);
+
+/* Worker threads used by the parallel loops (OpenMP). */
+void oracle_set_threads(int n);
+int oracle_get_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,132 @@
+"""Python binding of the CPU oracle (oracle/gpe_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker.  The product never imports it.
+
+It also restates, in numpy, how the reference turns a lattice and a time step
+into the update's factors (koodit/GrossPitaevskii/GPUGrossPitaevskii_BCC.cu:
+289-307: lapfac = -0.5*hodge/bs^2, lapfac0 = -(neighbours)*lapfac, both and g
+and V multiplied by dt).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgpe_oracle.so")
+
+
+class _Grid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("slots", C.c_int), ("neighbours", C.c_int),
+                ("entry", C.POINTER(C.c_int)), ("Lc", C.c_double * 2), ("L0", C.c_double), ("gdt", C.c_double)]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        cc = os.environ.get("CC", "gcc")
+        os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+        subprocess.run([cc, "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+                        "-fno-fast-math", os.path.join(HERE, "gpe_oracle.c"), "-o", LIB_PATH, "-lm"], check=True)
+    lib = C.CDLL(LIB_PATH)
+    vp, dp = C.c_void_p, C.c_double
+    G = C.POINTER(_Grid)
+    lib.oracle_half_step_f64.argtypes = [G, vp, vp, vp, C.c_int, dp]
+    lib.oracle_half_step_f32.argtypes = [G, vp, vp, vp, C.c_int, C.c_float]
+    lib.oracle_leapfrog_f64.argtypes = [G, vp, vp, vp, C.c_long]
+    lib.oracle_leapfrog_f32.argtypes = [G, vp, vp, vp, C.c_long]
+    lib.oracle_observables_f64.argtypes = [G, vp, vp, dp, dp, vp, vp]
+    lib.oracle_observables_f32.argtypes = [G, vp, vp, dp, dp, vp, vp]
+    lib.oracle_imaginary_f64.argtypes = [G, vp, vp, vp, dp, dp, vp, dp, C.c_long, dp, vp]
+    lib.oracle_imaginary_f64.restype = C.c_long
+    lib.oracle_set_threads.argtypes = [C.c_int]
+    lib.oracle_get_threads.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def set_threads(n: int):
+    load().oracle_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return int(load().oracle_get_threads())
+
+
+def factors(class_weight, entry_classes, block_scale, dt, g):
+    """Update factors as the reference computes them (GPUGrossPitaevskii_BCC.cu:291-307),
+    one per weight class: Lc = -0.5*w_c/bs^2*dt, L0 = (0.5*sum_c n_c*w_c/bs^2)*dt
+    (n_c = neighbours in class c; the reference's lapfac0 = 4*(-lapfac)), gdt = g*dt."""
+    w = [cw / (block_scale * block_scale) for cw in class_weight]
+    Lc = [-0.5 * wc * dt for wc in w] + [0.0] * (2 - len(w))
+    counts = [sum(1 for c in entry_classes if c == k) for k in range(len(w))]
+    wsum = counts[0] * w[0]
+    if len(w) > 1:
+        wsum = wsum + counts[1] * w[1]
+    L0 = (0.5 * wsum) * dt
+    return {"Lc": Lc, "L0": L0, "gdt": g * dt, "w": w + [0.0] * (2 - len(w))}
+
+
+class Grid:
+    """A grid of nx*ny*nz blocks with a neighbour table entry[slot][k] = (dx,dy,dz,slot,class)."""
+
+    def __init__(self, nx, ny, nz, entry, class_weight, block_scale, dt, g):
+        self.entry = np.ascontiguousarray(np.asarray(entry, dtype=np.int32))
+        self.slots, self.neighbours = self.entry.shape[0], self.entry.shape[1]
+        f = factors(class_weight, [int(c) for c in self.entry[0, :, 4]], block_scale, dt, g)
+        self.Lc, self.L0, self.gdt, self.w = f["Lc"], f["L0"], f["gdt"], f["w"]
+        self.dt, self.g = dt, g
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self._w = np.array(self.w, dtype=np.float64)
+        self._g = _Grid(nx, ny, nz, self.slots, self.neighbours,
+                        self.entry.ctypes.data_as(C.POINTER(C.c_int)), (C.c_double * 2)(*self.Lc), self.L0,
+                        self.gdt)
+
+    @property
+    def shape(self):
+        return (self.nz, self.ny, self.nx, self.slots)
+
+    def _p(self, a):
+        return a.ctypes.data_as(C.c_void_p)
+
+    def half_step(self, prev, next_, vdt, mode=0, sigma=1.0):
+        lib = load()
+        if prev.dtype == np.float64:
+            lib.oracle_half_step_f64(C.byref(self._g), self._p(prev), self._p(next_), self._p(vdt), mode, sigma)
+        else:
+            lib.oracle_half_step_f32(C.byref(self._g), self._p(prev), self._p(next_), self._p(vdt), mode,
+                                     C.c_float(sigma))
+
+    def leapfrog(self, even, odd, vdt, steps):
+        """In place: `steps` leapfrog steps (GPUGrossPitaevskii_BCC.cu:475-481)."""
+        lib = load()
+        for a in (even, odd, vdt):
+            assert a.flags.c_contiguous
+        fn = lib.oracle_leapfrog_f64 if even.dtype == np.float64 else lib.oracle_leapfrog_f32
+        fn(C.byref(self._g), self._p(even), self._p(odd), self._p(vdt), int(steps))
+
+    def observables(self, psi, vdt, vol):
+        lib = load()
+        out = np.zeros(4)
+        fn = lib.oracle_observables_f64 if psi.dtype == np.float64 else lib.oracle_observables_f32
+        fn(C.byref(self._g), self._p(psi), self._p(vdt), self.dt, self.g, self._p(self._w), self._p(out))
+        norm, kin, pot, inter = vol * out
+        return {"norm": norm, "kinetic": kin, "potential": pot, "interaction": inter,
+                "energy": kin + pot + inter, "mu": (kin + pot + 2 * inter) / norm}
+
+    def imaginary(self, psi, vdt, vol, steps, tol):
+        lib = load()
+        work = np.zeros_like(psi)
+        mu = np.zeros(max(int(steps), 1))
+        conv = lib.oracle_imaginary_f64(C.byref(self._g), self._p(psi), self._p(work), self._p(vdt), self.dt,
+                                        self.g, self._p(self._w), vol, int(steps), tol, self._p(mu))
+        return int(conv), mu[: int(steps)]

@@ -1,0 +1,71 @@
+"""Regenerate the golden fixtures in this folder from the reference's own code.
+
+Runs only where the reference source tree is present (it is read, never
+copied): builds ``oracle/_ref/ref_fixtures`` with ``make -C oracle ref`` (the
+reference's GPUGrossPitaevskii_BCC.cu host code, VortexState, Mesh library and
+MT19937, compiled from their sources) and records what it prints.
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+Outputs (committed):
+  ref_tables.json        getPositions/getLaplacian (GPUGrossPitaevskii_BCC.cu:73-142)
+  ref_mesh_hodge.json    Mesh-library Hodge weights around interior BCC nodes/bodies
+  ref_vortex_state.json  state.dat diagnostics, psi/phase samples, Random(54363) stream
+  ref_vortex_state2.json the same for state2.dat
+  ref_setup_bs2.json/.bin  integrateInTime host set-up (GPUGrossPitaevskii_BCC.cu:222-348)
+                           at block_scale 2.0 on state.dat
+  ref_state_header.json  the binary header fields of state.dat (VortexState.cpp:49-72)
+"""
+import argparse
+import json
+import os
+import struct
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+ORACLE = os.path.join(ROOT, "oracle")
+
+
+def run(args):
+    out = subprocess.run(args, check=True, capture_output=True, text=True).stdout
+    return json.loads(out)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    a = ap.parse_args()
+    gp = os.path.join(a.ref, "koodit", "GrossPitaevskii")
+    if not os.path.isdir(gp):
+        sys.exit(f"reference tree not found at {a.ref}")
+    subprocess.run(["make", "-C", ORACLE, "ref", f"REF={a.ref}", "-j8"], check=True,
+                   stdout=subprocess.DEVNULL)
+    exe = os.path.join(ORACLE, "_ref", "ref_fixtures")
+
+    def dump(name, obj):
+        with open(os.path.join(HERE, name), "w") as f:
+            json.dump(obj, f, indent=1)
+            f.write("\n")
+
+    dump("ref_tables.json", run([exe, "tables"]))
+    dump("ref_mesh_hodge.json", run([exe, "mesh"]))
+    dump("ref_vortex_state.json", run([exe, "vortex", os.path.join(gp, "state.dat")]))
+    dump("ref_vortex_state2.json", run([exe, "vortex", os.path.join(gp, "state2.dat")]))
+    binp = os.path.join(HERE, "ref_setup_bs2.bin")
+    dump("ref_setup_bs2.json", run([exe, "setup", os.path.join(gp, "state.dat"), "2.0", binp]))
+
+    # Header of the state file, decoded with the field order of VortexState::load.
+    with open(os.path.join(gp, "state.dat"), "rb") as f:
+        raw = f.read()
+    kappa, g, rsize, zsize, rplug, rstep, zstep, mu = struct.unpack_from("<IdIIdddd", raw, 0)
+    dump("ref_state_header.json", {
+        "source": "koodit/GrossPitaevskii/VortexState.cpp:49-72 (state.dat)",
+        "kappa": kappa, "g": g, "rsize": rsize, "zsize": zsize, "rplug": rplug,
+        "rstep": rstep, "zstep": zstep, "mu": mu, "file_bytes": len(raw)})
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

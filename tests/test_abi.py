@@ -1,0 +1,97 @@
+"""The C-ABI library: loads, exports every function include/gpe.h declares, and
+returns status codes (never exits) on bad input.  No GPU needed."""
+import ctypes as C
+
+import numpy as np
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+from vaikkari_gb300 import gpe
+from vaikkari_gb300.gpe import GpeError, Instance, Lattice, Status, Stepper
+
+
+def _declared():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", fn)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            names |= set(re.findall(r"\b(gpe_[a-z0-9_]+)\s*\(", txt))
+    return names
+
+
+def test_every_declared_symbol_is_exported():
+    lib = gpe.load_library()
+    out = subprocess.run(["nm", "-D", "--defined-only", gpe.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (gpe_[a-z0-9_]+)$", out, flags=re.M))
+    declared = _declared()
+    assert declared, "no declarations parsed"
+    missing = declared - exported
+    assert not missing, f"declared but not exported: {sorted(missing)}"
+    for name in declared:
+        getattr(lib, name)
+
+
+def test_version_and_status_strings():
+    lib = gpe.load_library()
+    assert lib.gpe_abi_version() == 1
+    for s in Status:
+        assert lib.gpe_status_string(int(s))
+    assert lib.gpe_status_string(999) == b"unknown status"
+
+
+def test_invalid_arguments_return_status():
+    lib = gpe.load_library()
+    assert lib.gpe_create(None, None) == Status.INVALID_ARGUMENT
+    assert b"null" in lib.gpe_last_error()
+    assert lib.gpe_step(None, 1) == Status.INVALID_ARGUMENT
+    assert lib.gpe_upload(None, 0, None, None, None) == Status.INVALID_ARGUMENT
+    assert lib.gpe_destroy(None) == Status.OK
+    assert lib.gpe_lattice_describe(7, None) == Status.INVALID_ARGUMENT
+    with pytest.raises(GpeError) as e:
+        Stepper([Instance(0, 4, 4, 0.5, 1e-3, 1.0)])
+    assert e.value.status == Status.INVALID_ARGUMENT
+    with pytest.raises(GpeError) as e:
+        Stepper([Instance(4, 4, 4, -1.0, 1e-3, 1.0)])
+    assert e.value.status == Status.INVALID_ARGUMENT
+    with pytest.raises(GpeError) as e:
+        Stepper([Instance(4, 4, 4, 0.5, 1e-3, 1.0)], lattice=Lattice.TETRA12, kernel=gpe.Kernel.FUSED)
+    assert e.value.status == Status.UNSUPPORTED
+    with pytest.raises(GpeError) as e:
+        Stepper([Instance(4, 4, 6000, 0.5, 1e-3, 1.0)], lattice=Lattice.TETRA12)
+    assert e.value.status == Status.TOO_LARGE
+
+
+def test_no_gpu_is_a_cuda_status_not_a_crash(has_gpu):
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(GpeError) as e:
+        Stepper([Instance(4, 4, 4, 0.5, 1e-3, 1.0)])
+    assert e.value.status == Status.CUDA
+
+
+def test_binding_rejects_wrong_shapes():
+    """A raw pointer carries no size: the binding checks array shapes before the
+    library copies nx*ny*nz*slots values from them."""
+    st = Stepper.__new__(Stepper)
+    st.instances = [Instance(4, 3, 2, 0.5, 1e-3, 1.0)]
+    st.slots = 2
+    st.dtype = np.float32
+    shp = st.shape(0)
+    assert shp == (2, 3, 4, 2)
+    with pytest.raises(ValueError):
+        st._carray(np.ones(shp), shp)           # real without the (re, im) axis
+    with pytest.raises(ValueError):
+        st._carray(np.ones((2, 3, 4, 3), complex), shp)
+    with pytest.raises(ValueError):
+        st._carray(np.ones(shp, complex), shp, complex_=False)
+    a, p = st._carray(np.ones(shp, complex), shp)
+    assert a.shape == shp + (2,) and a.dtype == np.float32
+    a, p = st._carray(np.ones(shp), shp, complex_=False)
+    assert a.shape == shp
+    with pytest.raises(IndexError):
+        st.shape(1)

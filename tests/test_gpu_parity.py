@@ -1,0 +1,154 @@
+"""GPU parity: every kernel path against the CPU oracle on the same seeded
+inputs, through the C ABI.
+
+Real-time stepping is bit-exact (the kernels and the oracle perform the same
+rounded operations in the same order).  Reductions and imaginary time sum in a
+different order and are compared with the tolerances written in each test.
+"""
+import numpy as np
+import pytest
+
+from helpers import grid_for, interleave, random_state, rel_l2, vdt_for, vol_for
+from vaikkari_gb300.gpe import Instance, Kernel, Lattice, Mode, Potential, Precision, Stepper
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(1, 1, 1), (3, 5, 7), (13, 7, 9), (40, 9, 20), (33, 17, 5)]
+
+
+def _dtype(prec):
+    return np.float64 if prec == Precision.FP64 else np.float32
+
+
+def _run_real(lattice, prec, kernel, potential, dims_list, steps=3, tile=0, graph_steps=-1, seed=0):
+    T = _dtype(prec)
+    rng = np.random.default_rng(seed)
+    insts = []
+    bw = 8 ** 0.5 if lattice == Lattice.TETRA12 else 1.0
+    for k, (nx, ny, nz) in enumerate(dims_list):
+        bs = (0.3 + 0.05 * k) / bw
+        # centred grid, moderate trap: dt * (largest eigenvalue of H) stays ~0.1,
+        # inside the leapfrog's stability bound
+        origin = tuple(-0.5 * n * bs * bw + 0.1 * k for n in (nx, ny, nz))
+        insts.append(Instance(nx, ny, nz, block_scale=bs, dt=1e-3 * (1 + 0.2 * k), g=50.0 + 10 * k,
+                              origin=origin, trap=(1.0, 1.5 + 0.1 * k, 0.7)))
+    st = Stepper(insts, lattice=lattice, precision=prec, kernel=kernel, potential=potential, tile=tile,
+                 graph_steps=graph_steps)
+    want = []
+    for i, inst in enumerate(insts):
+        shp = st.shape(i)
+        even = random_state(shp, seed + 10 * i, 0.3)
+        odd = random_state(shp, seed + 10 * i + 1, 0.3)
+        V = rng.uniform(0.0, 10.0, size=shp)
+        st.upload(i, even, odd, V if potential == Potential.ARRAY else None)
+        g = grid_for(st, i)
+        vdt = vdt_for(st, i, V)
+        e, o = interleave(even, T), interleave(odd, T)
+        g.leapfrog(e, o, vdt, steps)
+        want.append((e, o))
+    st.step(steps)
+    for i in range(len(insts)):
+        ge, go = st.download(i)
+        we, wo = want[i]
+        assert ge.dtype == T
+        np.testing.assert_array_equal(ge, we, err_msg=f"even, instance {i}")
+        np.testing.assert_array_equal(go, wo, err_msg=f"odd, instance {i}")
+    n = st.launch_count()
+    st.close()
+    return n
+
+
+@pytest.mark.parametrize("prec", [Precision.FP64, Precision.FP32])
+@pytest.mark.parametrize("dims", SIZES)
+def test_plain_tetra12_bit_exact(prec, dims):
+    _run_real(Lattice.TETRA12, prec, Kernel.PLAIN, Potential.ARRAY, [dims])
+
+
+@pytest.mark.parametrize("prec", [Precision.FP64, Precision.FP32])
+@pytest.mark.parametrize("kernel", [Kernel.PLAIN, Kernel.FUSED])
+@pytest.mark.parametrize("dims", SIZES)
+def test_bcc2_bit_exact(prec, kernel, dims):
+    _run_real(Lattice.BCC2, prec, kernel, Potential.ARRAY, [dims])
+
+
+@pytest.mark.parametrize("tile", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("prec", [Precision.FP64, Precision.FP32])
+def test_fused_tiles_batch_trap_bit_exact(tile, prec):
+    _run_real(Lattice.BCC2, prec, Kernel.FUSED, Potential.TRAP, SIZES, steps=4, tile=tile)
+
+
+@pytest.mark.parametrize("lattice", [Lattice.TETRA12, Lattice.BCC2])
+def test_trap_potential_plain_bit_exact(lattice):
+    _run_real(lattice, Precision.FP32, Kernel.PLAIN, Potential.TRAP, SIZES[:3], steps=2)
+
+
+def test_graph_replay_equals_direct_launches():
+    """A CUDA graph of 4 steps replayed, plus a remainder, equals 10 direct steps."""
+    n_graph = _run_real(Lattice.BCC2, Precision.FP32, Kernel.FUSED, Potential.TRAP, SIZES, steps=10, graph_steps=4)
+    n_direct = _run_real(Lattice.BCC2, Precision.FP32, Kernel.FUSED, Potential.TRAP, SIZES, steps=10, graph_steps=-1)
+    assert n_graph == n_direct
+
+
+@pytest.mark.parametrize("lattice,kernel", [(Lattice.TETRA12, Kernel.PLAIN), (Lattice.BCC2, Kernel.FUSED)])
+@pytest.mark.parametrize("prec", [Precision.FP64, Precision.FP32])
+def test_observables_match_oracle(lattice, kernel, prec):
+    T = _dtype(prec)
+    insts = [Instance(12, 10, 8, 0.4, 1e-3, 300.0, origin=(-2.4, -2.0, -1.6)),
+             Instance(5, 7, 9, 0.5, 2e-3, 20.0, origin=(-1.0, -2.0, -2.0))]
+    st = Stepper(insts, lattice=lattice, precision=prec, kernel=kernel, potential=Potential.ARRAY)
+    rng = np.random.default_rng(5)
+    wants = []
+    for i in range(2):
+        shp = st.shape(i)
+        psi = random_state(shp, 40 + i, 0.1)
+        V = rng.uniform(0, 5, size=shp)
+        st.upload(i, psi, psi, V)
+        g = grid_for(st, i)
+        wants.append(g.observables(interleave(psi, T), vdt_for(st, i, V), vol_for(st, i)))
+    got = st.observables(0)
+    st.close()
+    for w, o in zip(wants, got):
+        for k in ("norm", "kinetic", "potential", "interaction", "energy", "mu"):
+            assert o[k] == pytest.approx(w[k], rel=1e-12, abs=1e-14), k
+
+
+@pytest.mark.parametrize("lattice,kernel", [(Lattice.TETRA12, Kernel.PLAIN), (Lattice.BCC2, Kernel.PLAIN),
+                                            (Lattice.BCC2, Kernel.FUSED)])
+def test_imaginary_time_fp64_matches_oracle(lattice, kernel):
+    """FP64 imaginary time: psi and mu after 60 normalised Euler steps within 1e-11."""
+    inst = Instance(10, 9, 8, 0.45, 2e-3, 40.0, origin=(-2.25, -2.0, -1.8), trap=(1.0, 1.0, 4.0))
+    st = Stepper([inst], lattice=lattice, precision=Precision.FP64, mode=Mode.IMAGINARY, kernel=kernel,
+                 potential=Potential.TRAP, graph_steps=20)
+    shp = st.shape(0)
+    rng = np.random.default_rng(7)
+    psi0 = np.exp(1j * rng.uniform(0, 2 * np.pi, size=shp))
+    st.upload(0, psi0)
+    steps, conv, mu = st.imaginary_time(60, 0.0)
+    got, _ = st.download(0, odd=False)
+    st.close()
+    g = grid_for(st, 0)
+    psi = interleave(psi0, np.float64)
+    vdt = vdt_for(st, 0)
+    _, mu_hist = g.imaginary(psi, vdt, vol_for(st, 0), 60, 0.0)
+    assert steps == 60 and not conv
+    assert rel_l2(got, psi) < 1e-11
+    assert mu[0] == pytest.approx(mu_hist[-1], rel=1e-11)
+
+
+@pytest.mark.parametrize("kernel", [Kernel.PLAIN, Kernel.FUSED])
+def test_imaginary_time_converges_to_harmonic_ground_state(kernel):
+    """g = 0, isotropic trap: mu -> 3/2 up to the O(a^2) discretisation error."""
+    n = 24
+    a = 10.0 / n
+    inst = Instance(n, n, n, a, 2e-3, 0.0, origin=(-5.0, -5.0, -5.0))
+    st = Stepper([inst], lattice=Lattice.BCC2, precision=Precision.FP64, mode=Mode.IMAGINARY, kernel=kernel,
+                 potential=Potential.TRAP)
+    rng = np.random.default_rng(3)
+    st.upload(0, (1.0 + 0.1 * rng.standard_normal(st.shape(0))).astype(np.complex128))
+    steps, conv, mu = st.imaginary_time(20000, 1e-10)
+    obs = st.observables(0)[0]
+    st.close()
+    assert conv
+    assert mu[0] == pytest.approx(1.5, rel=3e-2)
+    assert obs["norm"] == pytest.approx(1.0, rel=1e-12)
+    assert obs["mu"] == pytest.approx(mu[0], rel=1e-8)

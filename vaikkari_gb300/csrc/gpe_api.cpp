@@ -1,0 +1,806 @@
+// gpe_api.cpp - the C ABI (include/gpe.h): handles, device arenas, uploads and
+// downloads, work lists, CUDA-graph replay of step chunks, observables, and the
+// imaginary-time driver.
+//
+// Corresponds to the host half of the reference's integrateInTime
+// (koodit/GrossPitaevskii/GPUGrossPitaevskii_BCC.cu:218-499): grid sizing,
+// device allocation, pre-scaling by dt (:289-307), host->device copies
+// (:370-392) and the launch loop (:475-481).  Differences by design: all
+// instances of a batch share one allocation and one launch per half-step, step
+// chunks are replayed from captured CUDA graphs, and errors come back as status
+// codes instead of exit().
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "gpe_internal.h"
+
+namespace gpe {
+
+static thread_local std::string g_last_error;
+
+gpe_status fail(gpe_status s, const std::string &msg)
+{
+    g_last_error = msg;
+    return s;
+}
+
+gpe_status cuda_fail(cudaError_t e, const char *what)
+{
+    g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    if (e == cudaErrorMemoryAllocation) return GPE_ERR_OUT_OF_MEMORY;
+    return GPE_ERR_CUDA;
+}
+
+
+}  // namespace gpe
+
+using namespace gpe;
+
+struct GraphKey {
+    long long steps;
+    int parity;
+    double tol;
+    bool operator<(const GraphKey &o) const { return std::tie(steps, parity, tol) < std::tie(o.steps, o.parity, o.tol); }
+};
+
+struct gpe_handle_ {
+    gpe_config cfg{};
+    std::vector<gpe_instance> inst;
+    gpe_lattice_info lat{};
+    int ns = 0;
+    size_t esize = 0;  // bytes per real element
+    std::vector<InstDev> idev_host;
+    InstDev *idev = nullptr;
+    size_t field_elems = 0, v_elems = 0;
+    void *buf[2] = {nullptr, nullptr};  // even, odd (or psi and its ping-pong partner)
+    void *vpot = nullptr;
+    bool fused = false;
+    int tile = 0, tx = 32, ty = 8, zchunk = 0;
+    std::vector<WorkItem> items;
+    WorkItem *items_dev = nullptr;
+    int *item_begin_dev = nullptr;
+    int grid = 0;
+    ImagScalars *imag = nullptr;
+    double *partials = nullptr;       // fused imaginary-time rows
+    unsigned int *counter = nullptr;
+    double *obs_partials = nullptr;   // observables CTA rows
+    double *obs_sums = nullptr;       // per instance, 6 sums
+    int obs_max_ctas = 2048;
+    void *staging = nullptr;
+    size_t staging_bytes = 0;
+    cudaStream_t stream = nullptr;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    int parity = 0;      // imaginary time: which buffer holds psi
+    bool imag_ready = false;
+    double tol = 0.0;
+    long long launches = 0;
+};
+
+namespace {
+
+size_t round_up(size_t v, size_t m) { return (v + m - 1) / m * m; }
+
+gpe_status check_handle(gpe_handle h)
+{
+    if (!h) return fail(GPE_ERR_INVALID_ARGUMENT, "null handle");
+    return GPE_OK;
+}
+
+// Per-axis trap tables, dt-scaled, rounded to the handle's precision:
+// Vx[s][i] = 0.5*trap[0]*x^2 at the value's x position, etc.
+void build_trap_tables(const gpe_handle_ &h, int ii, std::vector<double> &out)
+{
+    const gpe_instance &in = h.inst[ii];
+    const int n[3] = {in.nx, in.ny, in.nz};
+    out.clear();
+    for (int axis = 0; axis < 3; axis++)
+        for (int s = 0; s < h.ns; s++)
+            for (int i = 0; i < n[axis]; i++) {
+                const double p = in.origin[axis] + in.block_scale * (i * h.lat.block_width + h.lat.position[s][axis]);
+                out.push_back(0.5 * in.trap[axis] * p * p * in.dt);
+            }
+}
+
+gpe_status upload_raw(gpe_handle h, const void *src, size_t bytes)
+{
+    GPE_CUDA_TRY(cudaMemcpyAsync(h->staging, src, bytes, cudaMemcpyHostToDevice, h->stream));
+    return GPE_OK;
+}
+
+gpe_status enqueue_step_real(gpe_handle h)
+{
+    // odd <- even, then even <- odd (GPUGrossPitaevskii_BCC.cu:475-481)
+    for (int half = 0; half < 2; half++) {
+        void *prev = h->buf[half == 0 ? 0 : 1];
+        void *next = h->buf[half == 0 ? 1 : 0];
+        if (h->fused) {
+            FusedLaunch l{};
+            l.precision = h->cfg.precision;
+            l.mode = GPE_REAL_TIME;
+            l.potential = h->cfg.potential;
+            l.tile = h->tile;
+            l.inst = h->idev;
+            l.items = h->items_dev;
+            l.num_items = int(h->items.size());
+            l.grid = h->grid;
+            l.prev = prev;
+            l.next = next;
+            l.vpot = h->vpot;
+            l.num_instances = h->cfg.num_instances;
+            GPE_CUDA_TRY(launch_fused_step(l, h->stream));
+            h->launches++;
+        } else {
+            for (int i = 0; i < h->cfg.num_instances; i++) {
+                StepLaunch l{};
+                l.lattice = h->cfg.lattice;
+                l.precision = h->cfg.precision;
+                l.mode = GPE_REAL_TIME;
+                l.potential = h->cfg.potential;
+                l.inst = h->idev;
+                l.inst_index = i;
+                l.nx = h->inst[i].nx;
+                l.ny = h->inst[i].ny;
+                l.nz = h->inst[i].nz;
+                l.slots = h->ns;
+                l.prev = prev;
+                l.next = next;
+                l.vpot = h->vpot;
+                GPE_CUDA_TRY(launch_plain_step(l, h->stream));
+                h->launches++;
+            }
+        }
+    }
+    return GPE_OK;
+}
+
+gpe_status enqueue_observables(gpe_handle h, const void *field, int i, double *sums_dev)
+{
+    ObsLaunch o{};
+    o.lattice = h->cfg.lattice;
+    o.precision = h->cfg.precision;
+    o.potential = h->cfg.potential;
+    o.inst = h->idev;
+    o.inst_index = i;
+    o.nx = h->inst[i].nx;
+    o.ny = h->inst[i].ny;
+    o.nz = h->inst[i].nz;
+    o.slots = h->ns;
+    o.field = field;
+    o.vpot = h->vpot;
+    o.partials = h->obs_partials;
+    o.max_ctas = h->obs_max_ctas;
+    int ctas = 0;
+    GPE_CUDA_TRY(launch_observables(o, h->stream, &ctas));
+    GPE_CUDA_TRY(launch_reduce_partials(h->obs_partials, ctas, 6, sums_dev, h->stream));
+    h->launches += 2;
+    return GPE_OK;
+}
+
+// One imaginary-time step for every instance; flips the parity.
+gpe_status enqueue_step_imag(gpe_handle h, int parity)
+{
+    void *prev = h->buf[parity], *next = h->buf[1 - parity];
+    if (h->fused) {
+        FusedLaunch l{};
+        l.precision = h->cfg.precision;
+        l.mode = GPE_IMAGINARY_TIME;
+        l.potential = h->cfg.potential;
+        l.tile = h->tile;
+        l.inst = h->idev;
+        l.items = h->items_dev;
+        l.num_items = int(h->items.size());
+        l.grid = h->grid;
+        l.prev = prev;
+        l.next = next;
+        l.vpot = h->vpot;
+        l.imag = h->imag;
+        l.partials = h->partials;
+        l.counter = h->counter;
+        l.inst_item_begin = h->item_begin_dev;
+        l.num_instances = h->cfg.num_instances;
+        l.tol = h->tol;
+        GPE_CUDA_TRY(launch_fused_step(l, h->stream));
+        h->launches++;
+        return GPE_OK;
+    }
+    for (int i = 0; i < h->cfg.num_instances; i++) {
+        double *sums = h->obs_sums + 6 * i;
+        gpe_status st = enqueue_observables(h, prev, i, sums);
+        if (st != GPE_OK) return st;
+        GPE_CUDA_TRY(launch_imag_finalize_plain(sums, h->idev, i, h->imag, h->tol, nullptr, h->stream));
+        StepLaunch l{};
+        l.lattice = h->cfg.lattice;
+        l.precision = h->cfg.precision;
+        l.mode = GPE_IMAGINARY_TIME;
+        l.potential = h->cfg.potential;
+        l.inst = h->idev;
+        l.inst_index = i;
+        l.nx = h->inst[i].nx;
+        l.ny = h->inst[i].ny;
+        l.nz = h->inst[i].nz;
+        l.slots = h->ns;
+        l.prev = prev;
+        l.next = next;
+        l.vpot = h->vpot;
+        l.imag = h->imag;
+        GPE_CUDA_TRY(launch_plain_step(l, h->stream));
+        h->launches += 2;
+    }
+    return GPE_OK;
+}
+
+// Imaginary time: compute sigma of the current field and scale it in place so
+// that the stored field is normalised and sigma = 1.
+gpe_status imag_normalise(gpe_handle h, bool recompute)
+{
+    for (int i = 0; i < h->cfg.num_instances; i++) {
+        if (recompute) {
+            double *sums = h->obs_sums + 6 * i;
+            gpe_status st = enqueue_observables(h, h->buf[h->parity], i, sums);
+            if (st != GPE_OK) return st;
+            GPE_CUDA_TRY(launch_imag_init(sums, h->idev, i, h->imag, h->stream));
+        }
+        GPE_CUDA_TRY(launch_scale_field(h->cfg.precision, h->idev, i, h->inst[i].nx, h->inst[i].ny, h->inst[i].nz,
+                                        h->ns, h->buf[h->parity], h->imag, h->stream));
+        h->launches += 1;
+    }
+    GPE_CUDA_TRY(launch_set_sigma_one(h->imag, h->cfg.num_instances, h->stream));
+    h->launches++;
+    return GPE_OK;
+}
+
+gpe_status imag_prepare(gpe_handle h)
+{
+    if (h->imag_ready) return GPE_OK;
+    gpe_status st = imag_normalise(h, true);
+    if (st != GPE_OK) return st;
+    h->imag_ready = true;
+    return GPE_OK;
+}
+
+// Enqueues `steps` steps starting from the current parity.
+gpe_status enqueue_steps(gpe_handle h, long long steps)
+{
+    for (long long k = 0; k < steps; k++) {
+        gpe_status st;
+        if (h->cfg.mode == GPE_REAL_TIME) {
+            st = enqueue_step_real(h);
+        } else {
+            st = enqueue_step_imag(h, h->parity);
+            h->parity = 1 - h->parity;
+        }
+        if (st != GPE_OK) return st;
+    }
+    return GPE_OK;
+}
+
+gpe_status run_steps(gpe_handle h, long long steps)
+{
+    const long long G = h->cfg.graph_steps == 0 ? 100 : h->cfg.graph_steps;
+    if (h->cfg.graph_steps < 0 || steps < G) return enqueue_steps(h, steps);
+    long long done = 0;
+    while (steps - done >= G) {
+        GraphKey key{G, h->parity, h->tol};
+        auto it = h->graphs.find(key);
+        if (it == h->graphs.end()) {
+            const int parity0 = h->parity;
+            const long long launches0 = h->launches;
+            GPE_CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            gpe_status st = enqueue_steps(h, G);
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+            if (st != GPE_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                return st;
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            cudaGraphExec_t exec = nullptr;
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+            h->graphs[key] = exec;
+            it = h->graphs.find(key);
+            // capture only recorded the launches; restore the host-side state
+            h->parity = parity0;
+            h->launches = launches0;
+        }
+        GPE_CUDA_TRY(cudaGraphLaunch(it->second, h->stream));
+        // account for the launches inside the graph and the parity it leaves
+        const long long per_step = (h->cfg.mode == GPE_REAL_TIME)
+                                       ? (h->fused ? 2 : 2ll * h->cfg.num_instances)
+                                       : (h->fused ? 1 : 4ll * h->cfg.num_instances);
+        h->launches += per_step * G;
+        if (h->cfg.mode == GPE_IMAGINARY_TIME && (G % 2) == 1) h->parity = 1 - h->parity;
+        done += G;
+    }
+    return enqueue_steps(h, steps - done);
+}
+
+void free_handle(gpe_handle h)
+{
+    if (!h) return;
+    for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    cudaFree(h->idev);
+    cudaFree(h->buf[0]);
+    cudaFree(h->buf[1]);
+    cudaFree(h->vpot);
+    cudaFree(h->items_dev);
+    cudaFree(h->item_begin_dev);
+    cudaFree(h->imag);
+    cudaFree(h->partials);
+    cudaFree(h->counter);
+    cudaFree(h->obs_partials);
+    cudaFree(h->obs_sums);
+    cudaFree(h->staging);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+// The fused kernel hard-wires the BCC2 summation order; check it against the
+// geometry-derived table.
+bool bcc2_order_matches(const gpe_lattice_info &info)
+{
+    static const int want[2][14][5] = {
+        {{-1, -1, -1, 1, 0}, {0, -1, -1, 1, 0}, {-1, 0, -1, 1, 0}, {0, 0, -1, 1, 0},
+         {-1, -1, 0, 1, 0}, {0, -1, 0, 1, 0}, {-1, 0, 0, 1, 0}, {0, 0, 0, 1, 0},
+         {0, 0, -1, 0, 1}, {0, -1, 0, 0, 1}, {-1, 0, 0, 0, 1}, {1, 0, 0, 0, 1}, {0, 1, 0, 0, 1}, {0, 0, 1, 0, 1}},
+        {{0, 0, 0, 0, 0}, {1, 0, 0, 0, 0}, {0, 1, 0, 0, 0}, {1, 1, 0, 0, 0},
+         {0, 0, 1, 0, 0}, {1, 0, 1, 0, 0}, {0, 1, 1, 0, 0}, {1, 1, 1, 0, 0},
+         {0, 0, -1, 1, 1}, {0, -1, 0, 1, 1}, {-1, 0, 0, 1, 1}, {1, 0, 0, 1, 1}, {0, 1, 0, 1, 1}, {0, 0, 1, 1, 1}}};
+    for (int s = 0; s < 2; s++)
+        for (int k = 0; k < 14; k++)
+            for (int c = 0; c < 5; c++)
+                if (info.entry[s][k][c] != want[s][k][c]) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t gpe_abi_version(void) { return GPE_ABI_VERSION; }
+
+const char *gpe_status_string(gpe_status s)
+{
+    switch (s) {
+    case GPE_OK: return "ok";
+    case GPE_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case GPE_ERR_CUDA: return "CUDA error";
+    case GPE_ERR_OUT_OF_MEMORY: return "out of memory";
+    case GPE_ERR_NOT_FINITE: return "non-finite values";
+    case GPE_ERR_UNSUPPORTED: return "unsupported";
+    case GPE_ERR_TOO_LARGE: return "too large";
+    case GPE_ERR_INTERNAL: return "internal error";
+    }
+    return "unknown status";
+}
+
+const char *gpe_last_error(void) { return g_last_error.c_str(); }
+
+gpe_status gpe_lattice_describe(int32_t lattice, gpe_lattice_info *out)
+{
+    if (!out) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_lattice_describe: null output");
+    if (lattice != GPE_LATTICE_TETRA12 && lattice != GPE_LATTICE_BCC2)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_lattice_describe: unknown lattice");
+    gpe_status st = build_lattice(gpe_lattice(lattice), out);
+    if (st != GPE_OK) return fail(st, "lattice construction failed its self-check");
+    return GPE_OK;
+}
+
+gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
+{
+    if (!cfg || !out) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: null argument");
+    *out = nullptr;
+    if (cfg->lattice != GPE_LATTICE_TETRA12 && cfg->lattice != GPE_LATTICE_BCC2)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: unknown lattice");
+    if (cfg->precision != GPE_FP64 && cfg->precision != GPE_FP32)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: unknown precision");
+    if (cfg->mode != GPE_REAL_TIME && cfg->mode != GPE_IMAGINARY_TIME)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: unknown time mode");
+    if (cfg->potential != GPE_POTENTIAL_ARRAY && cfg->potential != GPE_POTENTIAL_TRAP)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: unknown potential kind");
+    if (cfg->kernel < GPE_KERNEL_AUTO || cfg->kernel > GPE_KERNEL_FUSED)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: unknown kernel kind");
+    if (cfg->num_instances < 1 || !cfg->instances)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: need at least one instance");
+    if (cfg->kernel == GPE_KERNEL_FUSED && cfg->lattice != GPE_LATTICE_BCC2)
+        return fail(GPE_ERR_UNSUPPORTED, "gpe_create: the fused kernel is built for the BCC2 lattice only");
+    for (int i = 0; i < cfg->num_instances; i++) {
+        const gpe_instance &in = cfg->instances[i];
+        if (in.nx < 1 || in.ny < 1 || in.nz < 1)
+            return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: instance " + std::to_string(i) + " has an empty grid");
+        // blockIdx.z of the plain kernel carries nz*slots; x/y tiles are bounded by int range
+        if ((long long)in.nz * (cfg->lattice == GPE_LATTICE_TETRA12 ? 12 : 2) > 65535 || in.nx > (1 << 24) ||
+            in.ny > (1 << 24))
+            return fail(GPE_ERR_TOO_LARGE, "gpe_create: instance " + std::to_string(i) +
+                                               " exceeds the grid limits (nz*slots <= 65535)");
+        if (!(in.block_scale > 0.0) || !std::isfinite(in.block_scale) || !(in.dt > 0.0) || !std::isfinite(in.dt) ||
+            !std::isfinite(in.g))
+            return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: instance " + std::to_string(i) +
+                                                      " needs finite block_scale > 0, dt > 0 and finite g");
+    }
+    gpe_handle h = new (std::nothrow) gpe_handle_();
+    if (!h) return fail(GPE_ERR_OUT_OF_MEMORY, "gpe_create: host allocation");
+    h->cfg = *cfg;
+    h->inst.assign(cfg->instances, cfg->instances + cfg->num_instances);
+    h->cfg.instances = h->inst.data();
+    gpe_status st = build_lattice(gpe_lattice(cfg->lattice), &h->lat);
+    if (st != GPE_OK) {
+        free_handle(h);
+        return fail(st, "lattice construction failed its self-check");
+    }
+    h->ns = h->lat.slots;
+    h->esize = cfg->precision == GPE_FP64 ? 8 : 4;
+    h->fused = (cfg->lattice == GPE_LATTICE_BCC2) && (cfg->kernel != GPE_KERNEL_PLAIN);
+    if (h->fused && !bcc2_order_matches(h->lat)) {
+        free_handle(h);
+        return fail(GPE_ERR_INTERNAL, "BCC2 table order differs from the fused kernel's");
+    }
+    cudaError_t e = cudaSetDevice(cfg->device);
+    if (e != cudaSuccess) {
+        free_handle(h);
+        return cuda_fail(e, "cudaSetDevice");
+    }
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        gpe_status s2 = cuda_fail(e, "cudaStreamCreate");
+        free_handle(h);
+        return s2;
+    }
+#define GPE_CREATE_TRY(expr)                           \
+    do {                                               \
+        cudaError_t e_ = (expr);                       \
+        if (e_ != cudaSuccess) {                       \
+            gpe_status s_ = cuda_fail(e_, #expr);      \
+            free_handle(h);                            \
+            return s_;                                 \
+        }                                              \
+    } while (0)
+    GPE_CREATE_TRY(set_plain_table(h->lat));
+
+    // Arena layout.
+    size_t off = 0, voff = 0, max_vals = 0;
+    std::vector<std::vector<double>> traps(cfg->num_instances);
+    for (int i = 0; i < cfg->num_instances; i++) {
+        const gpe_instance &in = h->inst[i];
+        InstDev d{};
+        d.nx = in.nx;
+        d.ny = in.ny;
+        d.nz = in.nz;
+        d.px = int(round_up(size_t(in.nx) + 3, 4));
+        d.py = in.ny + 2;
+        d.slots = h->ns;
+        d.plane = (long long)d.px * d.py;
+        d.zstride = (long long)h->ns * d.plane;
+        d.base = (long long)off;
+        off += round_up(size_t(d.zstride) * (in.nz + 2), 64);
+        if (cfg->potential == GPE_POTENTIAL_ARRAY) {
+            d.vbase = (long long)voff;
+            voff += round_up(size_t(d.zstride) * (in.nz + 2), 64);
+        } else {
+            build_trap_tables(*h, i, traps[i]);
+            d.vbase = (long long)voff;
+            voff += round_up(traps[i].size(), 64);
+        }
+        const double s2 = in.block_scale * in.block_scale;
+        d.w[0] = h->lat.class_weight[0] / s2;
+        d.w[1] = h->lat.classes > 1 ? h->lat.class_weight[1] / s2 : 0.0;
+        d.Lc[0] = -0.5 * d.w[0] * in.dt;
+        d.Lc[1] = -0.5 * d.w[1] * in.dt;
+        // L0 = (0.5 * sum_c n_c w_c) * dt, classes in order; for TETRA12 this is
+        // the reference's lapfac0 = 4 * 0.5 * hodge / bs^2, times dt (:291-306).
+        int ncls[2] = {0, 0};
+        for (int k = 0; k < h->lat.neighbours; k++) ncls[h->lat.entry[0][k][4]]++;
+        double wsum = ncls[0] * d.w[0];
+        if (h->lat.classes > 1) wsum = wsum + ncls[1] * d.w[1];
+        d.L0 = (0.5 * wsum) * in.dt;
+        d.gdt = in.g * in.dt;
+        d.dt = in.dt;
+        d.g = in.g;
+        d.vol = h->lat.cell_volume * in.block_scale * in.block_scale * in.block_scale;
+        h->idev_host.push_back(d);
+        max_vals = std::max(max_vals, size_t(in.nx) * in.ny * in.nz * h->ns);
+    }
+    h->field_elems = off;
+    h->v_elems = voff;
+    const size_t cbytes = 2 * h->esize;
+    // Every set-up copy and fill below is ordered on the handle's own
+    // (non-blocking) stream: a non-blocking stream does not synchronise with the
+    // legacy default stream, so mixing cudaMemcpy with cudaMemsetAsync here would
+    // let a fill overwrite a copy.  Host sources stay alive until the final
+    // stream synchronisation.
+    GPE_CREATE_TRY(cudaMalloc(&h->idev, sizeof(InstDev) * h->idev_host.size()));
+    GPE_CREATE_TRY(cudaMemcpyAsync(h->idev, h->idev_host.data(), sizeof(InstDev) * h->idev_host.size(),
+                                   cudaMemcpyHostToDevice, h->stream));
+    GPE_CREATE_TRY(cudaMalloc(&h->buf[0], cbytes * h->field_elems));
+    GPE_CREATE_TRY(cudaMalloc(&h->buf[1], cbytes * h->field_elems));
+    GPE_CREATE_TRY(cudaMemsetAsync(h->buf[0], 0, cbytes * h->field_elems, h->stream));
+    GPE_CREATE_TRY(cudaMemsetAsync(h->buf[1], 0, cbytes * h->field_elems, h->stream));
+    GPE_CREATE_TRY(cudaMalloc(&h->vpot, h->esize * std::max<size_t>(h->v_elems, 1)));
+    GPE_CREATE_TRY(cudaMemsetAsync(h->vpot, 0, h->esize * std::max<size_t>(h->v_elems, 1), h->stream));
+    std::vector<std::vector<float>> traps32(cfg->num_instances);
+    if (cfg->potential == GPE_POTENTIAL_TRAP) {
+        for (int i = 0; i < cfg->num_instances; i++) {
+            const size_t n = traps[i].size();
+            if (cfg->precision == GPE_FP64) {
+                GPE_CREATE_TRY(cudaMemcpyAsync((double *)h->vpot + h->idev_host[i].vbase, traps[i].data(), 8 * n,
+                                               cudaMemcpyHostToDevice, h->stream));
+            } else {
+                traps32[i].assign(traps[i].begin(), traps[i].end());
+                GPE_CREATE_TRY(cudaMemcpyAsync((float *)h->vpot + h->idev_host[i].vbase, traps32[i].data(), 4 * n,
+                                               cudaMemcpyHostToDevice, h->stream));
+            }
+        }
+    }
+    h->staging_bytes = std::max<size_t>(max_vals * cbytes, 64);
+    GPE_CREATE_TRY(cudaMalloc(&h->staging, h->staging_bytes));
+    GPE_CREATE_TRY(cudaMalloc(&h->imag, sizeof(ImagScalars) * cfg->num_instances));
+    std::vector<ImagScalars> imag_init(cfg->num_instances);
+    for (auto &sc : imag_init) {
+        sc = ImagScalars{};
+        sc.sigma = 1.0;
+        sc.conv_step = -1;
+    }
+    GPE_CREATE_TRY(cudaMemcpyAsync(h->imag, imag_init.data(), sizeof(ImagScalars) * imag_init.size(),
+                                   cudaMemcpyHostToDevice, h->stream));
+    GPE_CREATE_TRY(cudaMalloc(&h->obs_partials, sizeof(double) * 6 * h->obs_max_ctas));
+    GPE_CREATE_TRY(cudaMalloc(&h->obs_sums, sizeof(double) * 6 * cfg->num_instances));
+
+    if (h->fused) {
+        h->tile = cfg->tile > 0 && cfg->tile < fused_tile_count() ? cfg->tile : 0;
+        fused_tile_shape(h->tile, &h->tx, &h->ty);
+        // Instances in decreasing size; each instance's items contiguous,
+        // x fastest, then y, then z-chunk.
+        std::vector<int> order(cfg->num_instances);
+        for (int i = 0; i < cfg->num_instances; i++) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            const gpe_instance &A = h->inst[a], &B = h->inst[b];
+            return (long long)A.nx * A.ny * A.nz > (long long)B.nx * B.ny * B.nz;
+        });
+        int zc = cfg->zchunk;
+        if (zc <= 0) {
+            // Aim for >= ~4 waves of 152 SMs x 8 CTAs while keeping chunks >= 8 planes.
+            const long long target = 152ll * 8 * 4;
+            long long maxnz = 1;
+            for (auto &in : h->inst) maxnz = std::max<long long>(maxnz, in.nz);
+            zc = int(maxnz);
+            while (zc > 8) {
+                long long items = 0;
+                for (auto &in : h->inst)
+                    items += (long long)((in.nx + h->tx - 1) / h->tx) * ((in.ny + h->ty - 1) / h->ty) *
+                             ((in.nz + zc - 1) / zc);
+                if (items >= target) break;
+                zc = (zc + 1) / 2;
+            }
+            if (zc < 8) zc = std::min<long long>(8, maxnz);
+        }
+        h->zchunk = zc;
+        std::vector<std::vector<WorkItem>> per(cfg->num_instances);
+        for (int i = 0; i < cfg->num_instances; i++) {
+            const gpe_instance &in = h->inst[i];
+            for (int z0 = 0; z0 < in.nz; z0 += zc)
+                for (int y0 = 0; y0 < in.ny; y0 += h->ty)
+                    for (int x0 = 0; x0 < in.nx; x0 += h->tx)
+                        per[i].push_back(WorkItem{i, x0, y0, z0, std::min(in.nz, z0 + zc)});
+        }
+        std::vector<int> first(cfg->num_instances);
+        for (int oi : order) {
+            first[oi] = int(h->items.size());
+            h->items.insert(h->items.end(), per[oi].begin(), per[oi].end());
+        }
+        // Items of instance i occupy rows [first[i], first[i] + per[i].size()).
+        std::vector<int> ranges(2 * cfg->num_instances);
+        for (int i = 0; i < cfg->num_instances; i++) {
+            ranges[2 * i] = first[i];
+            ranges[2 * i + 1] = first[i] + int(per[i].size());
+        }
+        GPE_CREATE_TRY(cudaMalloc(&h->items_dev, sizeof(WorkItem) * h->items.size()));
+        GPE_CREATE_TRY(cudaMemcpyAsync(h->items_dev, h->items.data(), sizeof(WorkItem) * h->items.size(),
+                                       cudaMemcpyHostToDevice, h->stream));
+        GPE_CREATE_TRY(cudaMalloc(&h->item_begin_dev, sizeof(int) * ranges.size()));
+        GPE_CREATE_TRY(cudaMemcpyAsync(h->item_begin_dev, ranges.data(), sizeof(int) * ranges.size(),
+                                       cudaMemcpyHostToDevice, h->stream));
+        h->grid = int(h->items.size());
+        if (cfg->mode == GPE_IMAGINARY_TIME) {
+            GPE_CREATE_TRY(cudaMalloc(&h->partials, sizeof(double) * 4 * h->items.size()));
+            GPE_CREATE_TRY(cudaMalloc(&h->counter, sizeof(unsigned int)));
+            GPE_CREATE_TRY(cudaMemsetAsync(h->counter, 0, sizeof(unsigned int), h->stream));
+        }
+        // ranges must outlive the copy above
+        e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) {
+            gpe_status s2 = cuda_fail(e, "gpe_create: initialisation");
+            free_handle(h);
+            return s2;
+        }
+    }
+#undef GPE_CREATE_TRY
+    e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        gpe_status s2 = cuda_fail(e, "gpe_create: initialisation");
+        free_handle(h);
+        return s2;
+    }
+    *out = h;
+    return GPE_OK;
+}
+
+gpe_status gpe_destroy(gpe_handle h)
+{
+    if (!h) return GPE_OK;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    free_handle(h);
+    if (e != cudaSuccess) return cuda_fail(e, "gpe_destroy");
+    return GPE_OK;
+}
+
+gpe_status gpe_upload(gpe_handle h, int32_t instance, const void *even, const void *odd, const void *potential)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (instance < 0 || instance >= h->cfg.num_instances) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_upload: bad instance");
+    if (!even) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_upload: even field is required");
+    if (h->cfg.mode == GPE_REAL_TIME && !odd)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_upload: odd field is required in real time");
+    if (h->cfg.potential == GPE_POTENTIAL_ARRAY && !potential)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_upload: potential array is required");
+    const gpe_instance &in = h->inst[instance];
+    const size_t vals = size_t(in.nx) * in.ny * in.nz * h->ns;
+    const int prec = h->cfg.precision;
+    int target0 = 0;
+    if (h->cfg.mode == GPE_IMAGINARY_TIME) target0 = h->parity;
+    const void *srcs[2] = {even, odd};
+    for (int f = 0; f < 2; f++) {
+        if (!srcs[f]) continue;
+        const int target = (f == 0) ? target0 : 1 - target0;
+        st = upload_raw(h, srcs[f], vals * 2 * h->esize);
+        if (st != GPE_OK) return st;
+        GPE_CUDA_TRY(launch_pack(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->staging, h->buf[target], 1,
+                                 1.0, h->stream));
+        h->launches++;
+        GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    }
+    if (h->cfg.potential == GPE_POTENTIAL_ARRAY) {
+        st = upload_raw(h, potential, vals * h->esize);
+        if (st != GPE_OK) return st;
+        GPE_CUDA_TRY(launch_pack(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->staging, h->vpot, 0, in.dt,
+                                 h->stream));
+        h->launches++;
+    }
+    GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->imag_ready = false;
+    return GPE_OK;
+}
+
+gpe_status gpe_download(gpe_handle h, int32_t instance, void *even, void *odd)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (instance < 0 || instance >= h->cfg.num_instances)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_download: bad instance");
+    const gpe_instance &in = h->inst[instance];
+    const size_t vals = size_t(in.nx) * in.ny * in.nz * h->ns;
+    int src0 = (h->cfg.mode == GPE_IMAGINARY_TIME) ? h->parity : 0;
+    void *dsts[2] = {even, odd};
+    for (int f = 0; f < 2; f++) {
+        if (!dsts[f]) continue;
+        const int src = (f == 0) ? src0 : 1 - src0;
+        GPE_CUDA_TRY(launch_unpack(h->cfg.precision, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->buf[src],
+                                   h->staging, nullptr, h->stream));
+        h->launches++;
+        GPE_CUDA_TRY(cudaMemcpyAsync(dsts[f], h->staging, vals * 2 * h->esize, cudaMemcpyDeviceToHost, h->stream));
+        GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    }
+    return GPE_OK;
+}
+
+gpe_status gpe_step(gpe_handle h, int64_t steps)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (steps < 0) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_step: negative step count");
+    if (steps == 0) return GPE_OK;
+    if (h->cfg.mode == GPE_IMAGINARY_TIME) {
+        st = imag_prepare(h);
+        if (st != GPE_OK) return st;
+    }
+    st = run_steps(h, steps);
+    if (st != GPE_OK) return st;
+    if (h->cfg.mode == GPE_IMAGINARY_TIME) {
+        st = imag_normalise(h, !h->fused);
+        if (st != GPE_OK) return st;
+    }
+    return GPE_OK;
+}
+
+gpe_status gpe_synchronize(gpe_handle h)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return GPE_OK;
+}
+
+gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (!out || (field != 0 && field != 1)) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_observables_get: bad arguments");
+    const int src = (h->cfg.mode == GPE_IMAGINARY_TIME) ? (field == 0 ? h->parity : 1 - h->parity) : field;
+    for (int i = 0; i < h->cfg.num_instances; i++) {
+        st = enqueue_observables(h, h->buf[src], i, h->obs_sums + 6 * i);
+        if (st != GPE_OK) return st;
+    }
+    std::vector<double> sums(6 * h->cfg.num_instances);
+    GPE_CUDA_TRY(cudaMemcpyAsync(sums.data(), h->obs_sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost,
+                                 h->stream));
+    GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    bool all_finite = true;
+    for (int i = 0; i < h->cfg.num_instances; i++) {
+        const double vol = h->idev_host[i].vol;
+        gpe_observables &o = out[i];
+        o.norm = vol * sums[6 * i + 0];
+        o.kinetic = vol * sums[6 * i + 1];
+        o.potential = vol * sums[6 * i + 2];
+        o.interaction = vol * sums[6 * i + 3];
+        o.energy = o.kinetic + o.potential + o.interaction;
+        o.mu = (o.kinetic + o.potential + 2.0 * o.interaction) / o.norm;
+        o.finite = std::isfinite(o.norm) && std::isfinite(o.energy) && std::isfinite(o.mu);
+        o.pad_ = 0;
+        all_finite = all_finite && o.finite;
+    }
+    if (!all_finite) return fail(GPE_ERR_NOT_FINITE, "gpe_observables_get: NaN or Inf in the field");
+    return GPE_OK;
+}
+
+gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64_t *steps_done, int32_t *converged,
+                              double *mu_out)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (h->cfg.mode != GPE_IMAGINARY_TIME)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_imaginary_time: handle is not in imaginary-time mode");
+    if (max_steps < 0 || !(tol >= 0.0)) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_imaginary_time: bad arguments");
+    h->tol = tol;
+    st = imag_prepare(h);
+    if (st != GPE_OK) return st;
+    const long long G = h->cfg.graph_steps == 0 ? 100 : (h->cfg.graph_steps < 0 ? 100 : h->cfg.graph_steps);
+    long long done = 0;
+    bool all = false;
+    std::vector<ImagScalars> sc(h->cfg.num_instances);
+    while (done < max_steps) {
+        const long long n = std::min<long long>(G, max_steps - done);
+        st = run_steps(h, n);
+        if (st != GPE_OK) return st;
+        done += n;
+        st = imag_normalise(h, !h->fused);
+        if (st != GPE_OK) return st;
+        GPE_CUDA_TRY(cudaMemcpyAsync(sc.data(), h->imag, sizeof(ImagScalars) * sc.size(), cudaMemcpyDeviceToHost,
+                                     h->stream));
+        GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+        all = true;
+        for (auto &s : sc) all = all && (s.conv_step >= 0);
+        if (all) break;
+    }
+    if (steps_done) *steps_done = done;
+    if (converged) *converged = all ? 1 : 0;
+    if (mu_out)
+        for (int i = 0; i < h->cfg.num_instances; i++) mu_out[i] = sc[i].mu;
+    return GPE_OK;
+}
+
+int64_t gpe_launch_count(gpe_handle h) { return h ? h->launches : 0; }
+
+void *gpe_stream(gpe_handle h) { return h ? (void *)h->stream : nullptr; }
+
+}  // extern "C"

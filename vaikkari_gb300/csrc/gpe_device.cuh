@@ -1,0 +1,149 @@
+// gpe_device.cuh - device-side data layout and the update arithmetic shared by
+// every stepping kernel.
+//
+// Device layout of one field of one instance ("block-ordered structure of
+// arrays"): index
+//     base + (z+1)*zstride + s*plane + (y+1)*px + (x+2)
+// for block (x,y,z), slot s; plane = px*(ny+2), zstride = slots*plane.  Each
+// instance carries a ring of zero values around its blocks (one plane below and
+// above, one row at each y end, one column before and after x, plus one more
+// column in front so that interior rows start on a 16-byte boundary for FP32
+// pairs).  The zeros are the Dirichlet psi = 0 boundary that the reference gets
+// from its padding blocks (GPUGrossPitaevskii_BCC.cu:269-287); they are never
+// written, so stencil reads need no bounds checks.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gpe {
+
+struct InstDev {
+    int nx, ny, nz;   // blocks
+    int px, py;       // padded row pitch (elements), padded rows (ny + 2)
+    int slots;
+    long long plane;   // px * py
+    long long zstride; // slots * plane
+    long long base;    // element offset of this instance in the field arenas
+    long long vbase;   // ARRAY: offset in the potential arena (same layout as a field)
+                       // TRAP : offset of the per-axis tables [axis][slot][i]
+    double Lc[2];      // -0.5 * w_c * dt     (class weights pre-multiplied by dt)
+    double L0;         // 0.5 * dt * sum_k w_k (diagonal term, GPUGrossPitaevskii_BCC.cu:293)
+    double gdt;        // g * dt
+    double dt, g;
+    double vol;        // volume per value
+    double w[2];       // unscaled class weights
+};
+
+struct WorkItem {
+    int inst;
+    int x0, y0;
+    int z0, z1;
+};
+
+// Imaginary-time bookkeeping of one instance (device resident).
+struct ImagScalars {
+    double sigma;      // scale that normalises the field entering the next step
+    double mu;         // chemical potential of the normalised field entering the last step
+    double mu_prev;
+    double dmu;        // |mu - mu_prev|
+    double energy;     // energy of that normalised field
+    double norm_in;    // norm of the unscaled field entering the last step
+    long long conv_step;  // first step with dmu < tol, -1 while not converged
+    long long steps;      // steps taken
+};
+
+__host__ __device__ inline long long field_index(const InstDev &d, int s, int x, int y, int z)
+{
+    return d.base + (long long)(z + 1) * d.zstride + (long long)s * d.plane + (long long)(y + 1) * d.px + (x + 2);
+}
+
+#ifdef __CUDACC__
+// Rounded arithmetic without contraction, so that the CPU oracle (C fma(),
+// -ffp-contract=off) reproduces every result bit for bit.
+__device__ __forceinline__ float d_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float d_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float d_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float d_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double d_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double d_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double d_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double d_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+template <typename T> struct Cplx;
+template <> struct Cplx<float> { using type = float2; };
+template <> struct Cplx<double> { using type = double2; };
+
+template <typename T>
+__device__ __forceinline__ typename Cplx<T>::type c_add(typename Cplx<T>::type a, typename Cplx<T>::type b)
+{
+    typename Cplx<T>::type r;
+    r.x = d_add(a.x, b.x);
+    r.y = d_add(a.y, b.y);
+    return r;
+}
+
+template <typename T>
+__device__ __forceinline__ typename Cplx<T>::type c_scale(T s, typename Cplx<T>::type a)
+{
+    typename Cplx<T>::type r;
+    r.x = d_mul(s, a.x);
+    r.y = d_mul(s, a.y);
+    return r;
+}
+
+// dt * H psi for one value, given the per-class neighbour sums S[c]
+// (each summed in table order).  Restates the arithmetic of the reference's
+// update (GPUGrossPitaevskii_BCC.cu:211-213):
+//     sum = lapfac * sum_nbr + (lapfac0 + V*dt + g*dt*|psi|^2) * psi
+// with one weight per class:
+//     nrm = fma(p.x, p.x, p.y*p.y)
+//     c   = fma(gdt, nrm, L0 + Vdt)
+//     a   = L[0]*S[0] (+ fma(L[c], S[c], a) for further classes)
+//     h   = fma(c, p, a)
+template <typename T, int NC>
+__device__ __forceinline__ void hpsi(typename Cplx<T>::type p, const typename Cplx<T>::type *S, const T *L, T L0,
+                                     T vdt, T gdt, T &hx, T &hy, T &nrm)
+{
+    nrm = d_fma(p.x, p.x, d_mul(p.y, p.y));
+    const T c = d_fma(gdt, nrm, d_add(L0, vdt));
+    T ax = d_mul(L[0], S[0].x);
+    T ay = d_mul(L[0], S[0].y);
+#pragma unroll
+    for (int k = 1; k < NC; k++) {
+        ax = d_fma(L[k], S[k].x, ax);
+        ay = d_fma(L[k], S[k].y, ay);
+    }
+    hx = d_fma(c, p.x, ax);
+    hy = d_fma(c, p.y, ay);
+}
+
+// Real time: next += -i * h (GPUGrossPitaevskii_BCC.cu:215).
+// Imaginary time: next = p - h.
+template <typename T, int MODE>
+__device__ __forceinline__ typename Cplx<T>::type integrate(typename Cplx<T>::type next, typename Cplx<T>::type p, T hx,
+                                                            T hy)
+{
+    typename Cplx<T>::type r;
+    if (MODE == 0) {
+        r.x = d_add(next.x, hy);
+        r.y = d_sub(next.y, hx);
+    } else {
+        r.x = d_sub(p.x, hx);
+        r.y = d_sub(p.y, hy);
+    }
+    return r;
+}
+
+// Harmonic trap from per-axis tables (dt-scaled): V = (Vx + Vy) + Vz.
+template <typename T>
+__device__ __forceinline__ T trap_vdt(const T *tab, const InstDev &d, int s, int x, int y, int z)
+{
+    const T *tx = tab + d.vbase;
+    const T *ty = tx + (long long)d.slots * d.nx;
+    const T *tz = ty + (long long)d.slots * d.ny;
+    return d_add(d_add(tx[s * d.nx + x], ty[s * d.ny + y]), tz[s * d.nz + z]);
+}
+#endif  // __CUDACC__
+
+}  // namespace gpe

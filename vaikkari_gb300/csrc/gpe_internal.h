@@ -1,0 +1,102 @@
+// gpe_internal.h - host-side declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/gpe.h"
+#include "gpe_device.cuh"
+
+namespace gpe {
+
+// Lattice tables from the BCC geometry (gpe_lattice.cpp).
+gpe_status build_lattice(gpe_lattice lattice, gpe_lattice_info *info);
+
+// Records a message for gpe_last_error() and returns `s`.
+gpe_status fail(gpe_status s, const std::string &msg);
+gpe_status cuda_fail(cudaError_t e, const char *what);
+
+#define GPE_CUDA_TRY(expr)                                        \
+    do {                                                          \
+        cudaError_t gpe_e_ = (expr);                              \
+        if (gpe_e_ != cudaSuccess) return ::gpe::cuda_fail(gpe_e_, #expr); \
+    } while (0)
+
+// Uploads a lattice's neighbour table to constant memory (gpe_plain.cu).
+cudaError_t set_plain_table(const gpe_lattice_info &info);
+
+// Kernel launchers; each returns cudaGetLastError() after the launch.
+struct StepLaunch {
+    int lattice;          // gpe_lattice
+    int precision;        // gpe_precision
+    int mode;             // gpe_time_mode
+    int potential;        // gpe_potential_kind
+    const InstDev *inst;  // device array
+    int inst_index;       // plain kernel: which instance
+    int nx, ny, nz, slots;
+    void *prev, *next;    // field arenas (T2*)
+    const void *vpot;     // potential arena (T*) or trap tables
+    const ImagScalars *imag;  // imaginary time: per-instance scale of prev (device), may be null
+};
+cudaError_t launch_plain_step(const StepLaunch &l, cudaStream_t s);
+
+struct FusedLaunch {
+    int precision, mode, potential, tile;
+    const InstDev *inst;
+    const WorkItem *items;
+    int num_items;
+    int grid;             // CTAs
+    void *prev, *next;
+    const void *vpot;
+    ImagScalars *imag;    // imaginary time: per-instance scalars (device), else null
+    double *partials;     // imaginary time: 4 sums per work item
+    unsigned int *counter;  // last-block-done counter
+    const int *inst_item_begin;  // per instance id: [begin, end) item rows (2 ints each)
+    int num_instances;
+    double tol;
+    long long step;       // host-side step index (for convergence bookkeeping)
+    const long long *step_dev;  // device step counter (graphs)
+};
+cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s);
+int fused_tile_count();
+void fused_tile_shape(int tile, int *tx, int *ty);
+
+struct ObsLaunch {
+    int lattice, precision, potential;
+    const InstDev *inst;
+    int inst_index;
+    int nx, ny, nz, slots;
+    const void *field;
+    const void *vpot;
+    double *partials;       // 6 sums per CTA
+    int max_ctas;
+};
+// Per-value observables partial sums for one instance; returns CTAs used.
+cudaError_t launch_observables(const ObsLaunch &l, cudaStream_t s, int *ctas_used);
+// Reduces `ctas` partial rows (6 doubles each) in fixed order with Kahan
+// compensation into out[6] (device).
+cudaError_t launch_reduce_partials(const double *partials, int ctas, int width, double *out, cudaStream_t s);
+// Imaginary time, plain path: from the 6 observables sums of psi_n, write
+// sigma_n, mu_n and the convergence bookkeeping.
+cudaError_t launch_imag_finalize_plain(const double *sums, const InstDev *inst, int inst_index,
+                                       ImagScalars *imag, double tol, const long long *step_dev,
+                                       cudaStream_t s);
+
+// Layout conversion between host block order and the padded device layout.
+cudaError_t launch_pack(int precision, const InstDev *inst, int inst_index, int nx, int ny, int nz,
+                        int slots, const void *host_order, void *field, int is_complex, double scale,
+                        cudaStream_t s);
+cudaError_t launch_unpack(int precision, const InstDev *inst, int inst_index, int nx, int ny, int nz,
+                          int slots, const void *field, void *host_order, const ImagScalars *imag,
+                          cudaStream_t s);
+cudaError_t launch_scale_field(int precision, const InstDev *inst, int inst_index, int nx, int ny, int nz,
+                               int slots, void *field, const ImagScalars *imag, cudaStream_t s);
+// Imaginary time: sigma = 1/sqrt(norm) from observables sums (no mu update).
+cudaError_t launch_imag_init(const double *sums, const InstDev *inst, int inst_index, ImagScalars *imag,
+                             cudaStream_t s);
+cudaError_t launch_set_sigma_one(ImagScalars *imag, int n, cudaStream_t s);
+
+}  // namespace gpe

@@ -1,0 +1,415 @@
+// gpe_plain.cu - table-driven half-step for any lattice, one value per thread;
+// FP64 observables; layout conversion.
+//
+// The plain step is the reference's update kernel (koodit/GrossPitaevskii/
+// GPUGrossPitaevskii_BCC.cu:176-216) re-expressed for the padded slot-major
+// layout: a warp covers 32 consecutive blocks along x of one slot, so every
+// load of a neighbour slot is a coalesced 256/512-byte row segment (the
+// reference's lanes are 192 bytes apart), and the neighbour table is read from
+// constant memory with a warp-uniform index.
+
+#include <cuda_runtime.h>
+
+#include "gpe_internal.h"
+
+namespace gpe {
+
+// Packed neighbour entry: (dx+1) | (dy+1)<<2 | (dz+1)<<4 | slot<<6 | class<<10.
+__constant__ int c_tab_tetra12[12 * 4];
+__constant__ int c_tab_bcc2[2 * 14];
+
+template <int LAT> struct Lat;
+template <> struct Lat<GPE_LATTICE_TETRA12> {
+    static constexpr int NS = 12, NB = 4, NC = 1, N0 = 4;
+    __device__ static int entry(int k) { return c_tab_tetra12[k]; }
+};
+template <> struct Lat<GPE_LATTICE_BCC2> {
+    static constexpr int NS = 2, NB = 14, NC = 2, N0 = 8;
+    __device__ static int entry(int k) { return c_tab_bcc2[k]; }
+};
+
+cudaError_t set_plain_table(const gpe_lattice_info &info)
+{
+    int packed[12 * 14];
+    const int nb = info.neighbours;
+    for (int s = 0; s < info.slots; s++)
+        for (int k = 0; k < nb; k++) {
+            const int *e = info.entry[s][k];
+            packed[s * nb + k] = (e[0] + 1) | ((e[1] + 1) << 2) | ((e[2] + 1) << 4) | (e[3] << 6) | (e[4] << 10);
+        }
+    if (info.lattice == GPE_LATTICE_TETRA12)
+        return cudaMemcpyToSymbol(c_tab_tetra12, packed, sizeof(int) * 12 * 4);
+    return cudaMemcpyToSymbol(c_tab_bcc2, packed, sizeof(int) * 2 * 14);
+}
+
+template <typename T, int LAT, int MODE, int POT>
+__global__ void __launch_bounds__(256) plain_step_kernel(const InstDev *__restrict__ insts, int ii,
+                                                         const typename Cplx<T>::type *__restrict__ prev,
+                                                         typename Cplx<T>::type *__restrict__ next,
+                                                         const T *__restrict__ vpot, const ImagScalars *__restrict__ imag)
+{
+    using T2 = typename Cplx<T>::type;
+    using L = Lat<LAT>;
+    const InstDev &d = insts[ii];
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    const int y = blockIdx.y * 8 + threadIdx.y;
+    const int z = blockIdx.z / L::NS;
+    const int s = blockIdx.z - z * L::NS;
+    if (x >= d.nx || y >= d.ny) return;
+    const T sig = (MODE == 1) ? T(imag[ii].sigma) : T(1);
+
+    T2 S[L::NC];
+#pragma unroll
+    for (int k = 0; k < L::NB; k++) {
+        const int e = L::entry(s * L::NB + k);
+        const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
+        T2 v = prev[field_index(d, sl, x + dx, y + dy, z + dz)];
+        if (MODE == 1) v = c_scale<T>(sig, v);
+        const int c = (k < L::N0) ? 0 : 1;
+        if (k == 0 || k == L::N0) S[c] = v;
+        else S[c] = c_add<T>(S[c], v);
+    }
+    const long long self = field_index(d, s, x, y, z);
+    T2 p = prev[self];
+    if (MODE == 1) p = c_scale<T>(sig, p);
+    T vdt;
+    if (POT == GPE_POTENTIAL_ARRAY) vdt = vpot[self - d.base + d.vbase];
+    else vdt = trap_vdt<T>(vpot, d, s, x, y, z);
+    T Lw[L::NC];
+    Lw[0] = T(d.Lc[0]);
+    if (L::NC > 1) Lw[L::NC - 1] = T(d.Lc[1]);
+    T hx, hy, nrm;
+    hpsi<T, L::NC>(p, S, Lw, T(d.L0), vdt, T(d.gdt), hx, hy, nrm);
+    T2 n;
+    if (MODE == 0) n = next[self];
+    next[self] = integrate<T, MODE>(n, p, hx, hy);
+}
+
+template <typename T, int LAT>
+static cudaError_t plain_dispatch_mode(const StepLaunch &l, cudaStream_t st)
+{
+    using T2 = typename Cplx<T>::type;
+    dim3 block(32, 8, 1);
+    dim3 grid((l.nx + 31) / 32, (l.ny + 7) / 8, l.nz * Lat<LAT>::NS);
+    const T2 *prev = (const T2 *)l.prev;
+    T2 *next = (T2 *)l.next;
+    const T *v = (const T *)l.vpot;
+    if (l.mode == GPE_REAL_TIME) {
+        if (l.potential == GPE_POTENTIAL_ARRAY)
+            plain_step_kernel<T, LAT, 0, 0><<<grid, block, 0, st>>>(l.inst, l.inst_index, prev, next, v, l.imag);
+        else
+            plain_step_kernel<T, LAT, 0, 1><<<grid, block, 0, st>>>(l.inst, l.inst_index, prev, next, v, l.imag);
+    } else {
+        if (l.potential == GPE_POTENTIAL_ARRAY)
+            plain_step_kernel<T, LAT, 1, 0><<<grid, block, 0, st>>>(l.inst, l.inst_index, prev, next, v, l.imag);
+        else
+            plain_step_kernel<T, LAT, 1, 1><<<grid, block, 0, st>>>(l.inst, l.inst_index, prev, next, v, l.imag);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_plain_step(const StepLaunch &l, cudaStream_t s)
+{
+    if (l.precision == GPE_FP64) {
+        if (l.lattice == GPE_LATTICE_TETRA12) return plain_dispatch_mode<double, GPE_LATTICE_TETRA12>(l, s);
+        return plain_dispatch_mode<double, GPE_LATTICE_BCC2>(l, s);
+    }
+    if (l.lattice == GPE_LATTICE_TETRA12) return plain_dispatch_mode<float, GPE_LATTICE_TETRA12>(l, s);
+    return plain_dispatch_mode<float, GPE_LATTICE_BCC2>(l, s);
+}
+
+// ---------------------------------------------------------------------------
+// Observables: per-value sums in FP64 with Kahan compensation per thread, a
+// fixed-shape tree per CTA, one row of 6 partial sums per CTA.  Sums (without the
+// volume factor): |psi|^2, Re(conj(psi)(-1/2 Lap psi)), V|psi|^2, g/2 |psi|^4,
+// and two spares (0).
+
+struct Kahan {
+    double s = 0.0, c = 0.0;
+    __device__ void add(double v)
+    {
+        const double y = v - c;
+        const double t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+template <int W>
+__device__ void cta_tree_store(double (&v)[W], double *out)
+{
+    __shared__ double sm[W][256];
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < W; k++) sm[k][t] = v[k];
+    __syncthreads();
+    for (int half = 128; half > 0; half >>= 1) {
+        if (t < half) {
+#pragma unroll
+            for (int k = 0; k < W; k++) sm[k][t] = sm[k][t] + sm[k][t + half];
+        }
+        __syncthreads();
+    }
+    if (t < W) out[t] = sm[t][0];
+}
+
+template <typename T, int LAT, int POT>
+__global__ void __launch_bounds__(256) observables_kernel(const InstDev *__restrict__ insts, int ii,
+                                                          const typename Cplx<T>::type *__restrict__ f,
+                                                          const T *__restrict__ vpot, double *__restrict__ partials)
+{
+    using T2 = typename Cplx<T>::type;
+    using L = Lat<LAT>;
+    const InstDev &d = insts[ii];
+    const long long total = (long long)d.nx * d.ny * d.nz * L::NS;
+    Kahan k0, k1, k2, k3;
+    const double wsum = L::N0 * d.w[0] + (L::NB - L::N0) * d.w[1];
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
+         v += (long long)gridDim.x * blockDim.x) {
+        long long r = v;
+        const int x = int(r % d.nx);
+        r /= d.nx;
+        const int y = int(r % d.ny);
+        r /= d.ny;
+        const int s = int(r % L::NS);
+        const int z = int(r / L::NS);
+        double sx[2] = {0.0, 0.0}, sy[2] = {0.0, 0.0};
+#pragma unroll
+        for (int k = 0; k < L::NB; k++) {
+            const int e = L::entry(s * L::NB + k);
+            const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
+            const T2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
+            const int c = (k < L::N0) ? 0 : 1;
+            sx[c] += double(q.x);
+            sy[c] += double(q.y);
+        }
+        const long long self = field_index(d, s, x, y, z);
+        const T2 pt = f[self];
+        const double px = double(pt.x), py = double(pt.y);
+        const double lx = d.w[0] * sx[0] + d.w[1] * sx[1] - wsum * px;
+        const double ly = d.w[0] * sy[0] + d.w[1] * sy[1] - wsum * py;
+        double vdt;
+        if (POT == GPE_POTENTIAL_ARRAY) vdt = double(vpot[self - d.base + d.vbase]);
+        else vdt = double(trap_vdt<T>(vpot, d, s, x, y, z));
+        const double n2 = px * px + py * py;
+        k0.add(n2);
+        k1.add(-0.5 * (px * lx + py * ly));
+        k2.add((vdt / d.dt) * n2);
+        k3.add(0.5 * d.g * n2 * n2);
+    }
+    double acc[6] = {k0.s, k1.s, k2.s, k3.s, 0.0, 0.0};
+    cta_tree_store<6>(acc, partials + 6ll * blockIdx.x);
+}
+
+cudaError_t launch_observables(const ObsLaunch &l, cudaStream_t s, int *ctas_used)
+{
+    const long long total = (long long)l.nx * l.ny * l.nz * l.slots;
+    long long want = (total + 255) / 256;
+    int ctas = int(want < l.max_ctas ? want : l.max_ctas);
+    if (ctas < 1) ctas = 1;
+    *ctas_used = ctas;
+#define GPE_OBS(T, LAT, POT) \
+    observables_kernel<T, LAT, POT><<<ctas, 256, 0, s>>>(l.inst, l.inst_index, (const Cplx<T>::type *)l.field, (const T *)l.vpot, l.partials)
+    const bool arr = l.potential == GPE_POTENTIAL_ARRAY;
+    if (l.precision == GPE_FP64) {
+        if (l.lattice == GPE_LATTICE_TETRA12) { if (arr) GPE_OBS(double, 0, 0); else GPE_OBS(double, 0, 1); }
+        else { if (arr) GPE_OBS(double, 1, 0); else GPE_OBS(double, 1, 1); }
+    } else {
+        if (l.lattice == GPE_LATTICE_TETRA12) { if (arr) GPE_OBS(float, 0, 0); else GPE_OBS(float, 0, 1); }
+        else { if (arr) GPE_OBS(float, 1, 0); else GPE_OBS(float, 1, 1); }
+    }
+#undef GPE_OBS
+    return cudaGetLastError();
+}
+
+// One CTA: thread t folds rows t, t+256, ... with Kahan, then a fixed tree.
+__global__ void __launch_bounds__(256) reduce_partials_kernel(const double *__restrict__ partials, int rows, int width,
+                                                              double *__restrict__ out)
+{
+    double acc[6];
+    for (int k = 0; k < 6; k++) {
+        Kahan kk;
+        if (k < width)
+            for (int r = threadIdx.x; r < rows; r += 256) kk.add(partials[(long long)r * width + k]);
+        acc[k] = kk.s;
+    }
+    cta_tree_store<6>(acc, out);
+}
+
+cudaError_t launch_reduce_partials(const double *partials, int ctas, int width, double *out, cudaStream_t s)
+{
+    reduce_partials_kernel<<<1, 256, 0, s>>>(partials, ctas, width, out);
+    return cudaGetLastError();
+}
+
+__global__ void imag_finalize_plain_kernel(const double *__restrict__ sums, const InstDev *__restrict__ insts, int ii,
+                                           ImagScalars *__restrict__ imag, double tol)
+{
+    const InstDev &d = insts[ii];
+    ImagScalars &st = imag[ii];
+    const double n = d.vol * sums[0];
+    const double kin = d.vol * sums[1], pot = d.vol * sums[2], inter = d.vol * sums[3];
+    // Observables of the normalised field sigma*psi, sigma^2 = 1/n.
+    const double mu = (kin + pot) / n + 2.0 * inter / (n * n);
+    st.sigma = 1.0 / sqrt(n);
+    st.norm_in = n;
+    st.energy = (kin + pot) / n + inter / (n * n);
+    st.mu_prev = st.mu;
+    st.mu = mu;
+    st.dmu = (st.steps > 0) ? fabs(mu - st.mu_prev) : INFINITY;
+    if (st.steps > 0 && st.conv_step < 0 && st.dmu < tol) st.conv_step = st.steps;
+    st.steps += 1;
+}
+
+cudaError_t launch_imag_finalize_plain(const double *sums, const InstDev *inst, int inst_index, ImagScalars *imag,
+                                       double tol, const long long *, cudaStream_t s)
+{
+    imag_finalize_plain_kernel<<<1, 1, 0, s>>>(sums, inst, inst_index, imag, tol);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Layout conversion.  Host order: (((z*ny)+y)*nx+x)*slots+s.
+
+template <typename T, bool CPLX>
+__global__ void pack_kernel(const InstDev *__restrict__ insts, int ii, const T *__restrict__ src, T *__restrict__ dst,
+                            double scale)
+{
+    const InstDev &d = insts[ii];
+    const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
+         v += (long long)gridDim.x * blockDim.x) {
+        long long r = v;
+        const int s = int(r % d.slots);
+        r /= d.slots;
+        const int x = int(r % d.nx);
+        r /= d.nx;
+        const int y = int(r % d.ny);
+        const int z = int(r / d.ny);
+        if (CPLX) {
+            const long long o = field_index(d, s, x, y, z);
+            dst[2 * o] = src[2 * v];
+            dst[2 * o + 1] = src[2 * v + 1];
+        } else {
+            const long long o = field_index(d, s, x, y, z) - d.base + d.vbase;
+            dst[o] = T(double(src[v]) * scale);
+        }
+    }
+}
+
+template <typename T>
+__global__ void unpack_kernel(const InstDev *__restrict__ insts, int ii, const T *__restrict__ src, T *__restrict__ dst,
+                              const ImagScalars *__restrict__ imag)
+{
+    const InstDev &d = insts[ii];
+    const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
+    const T sig = imag ? T(imag[ii].sigma) : T(1);
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
+         v += (long long)gridDim.x * blockDim.x) {
+        long long r = v;
+        const int s = int(r % d.slots);
+        r /= d.slots;
+        const int x = int(r % d.nx);
+        r /= d.nx;
+        const int y = int(r % d.ny);
+        const int z = int(r / d.ny);
+        const long long o = field_index(d, s, x, y, z);
+        if (imag) {
+            dst[2 * v] = d_mul(sig, src[2 * o]);
+            dst[2 * v + 1] = d_mul(sig, src[2 * o + 1]);
+        } else {
+            dst[2 * v] = src[2 * o];
+            dst[2 * v + 1] = src[2 * o + 1];
+        }
+    }
+}
+
+template <typename T>
+__global__ void scale_field_kernel(const InstDev *__restrict__ insts, int ii, T *__restrict__ f,
+                                   const ImagScalars *__restrict__ imag)
+{
+    const InstDev &d = insts[ii];
+    const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
+    const T sig = T(imag[ii].sigma);
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
+         v += (long long)gridDim.x * blockDim.x) {
+        long long r = v;
+        const int x = int(r % d.nx);
+        r /= d.nx;
+        const int y = int(r % d.ny);
+        r /= d.ny;
+        const int s = int(r % d.slots);
+        const int z = int(r / d.slots);
+        const long long o = field_index(d, s, x, y, z);
+        f[2 * o] = d_mul(sig, f[2 * o]);
+        f[2 * o + 1] = d_mul(sig, f[2 * o + 1]);
+    }
+}
+
+static int grid_for(long long total)
+{
+    long long g = (total + 255) / 256;
+    if (g > 152 * 32) g = 152 * 32;
+    return int(g < 1 ? 1 : g);
+}
+
+cudaError_t launch_pack(int precision, const InstDev *inst, int ii, int nx, int ny, int nz, int slots,
+                        const void *host_order, void *field, int is_complex, double scale, cudaStream_t s)
+{
+    const int g = grid_for((long long)nx * ny * nz * slots);
+    if (precision == GPE_FP64) {
+        if (is_complex) pack_kernel<double, true><<<g, 256, 0, s>>>(inst, ii, (const double *)host_order, (double *)field, scale);
+        else pack_kernel<double, false><<<g, 256, 0, s>>>(inst, ii, (const double *)host_order, (double *)field, scale);
+    } else {
+        if (is_complex) pack_kernel<float, true><<<g, 256, 0, s>>>(inst, ii, (const float *)host_order, (float *)field, scale);
+        else pack_kernel<float, false><<<g, 256, 0, s>>>(inst, ii, (const float *)host_order, (float *)field, scale);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(int precision, const InstDev *inst, int ii, int nx, int ny, int nz, int slots,
+                          const void *field, void *host_order, const ImagScalars *imag, cudaStream_t s)
+{
+    const int g = grid_for((long long)nx * ny * nz * slots);
+    if (precision == GPE_FP64)
+        unpack_kernel<double><<<g, 256, 0, s>>>(inst, ii, (const double *)field, (double *)host_order, imag);
+    else
+        unpack_kernel<float><<<g, 256, 0, s>>>(inst, ii, (const float *)field, (float *)host_order, imag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scale_field(int precision, const InstDev *inst, int ii, int nx, int ny, int nz, int slots,
+                               void *field, const ImagScalars *imag, cudaStream_t s)
+{
+    const int g = grid_for((long long)nx * ny * nz * slots);
+    if (precision == GPE_FP64) scale_field_kernel<double><<<g, 256, 0, s>>>(inst, ii, (double *)field, imag);
+    else scale_field_kernel<float><<<g, 256, 0, s>>>(inst, ii, (float *)field, imag);
+    return cudaGetLastError();
+}
+
+__global__ void imag_init_kernel(const double *__restrict__ sums, const InstDev *__restrict__ insts, int ii,
+                                 ImagScalars *__restrict__ imag)
+{
+    const double n = insts[ii].vol * sums[0];
+    imag[ii].sigma = 1.0 / sqrt(n);
+    imag[ii].norm_in = n;
+}
+
+cudaError_t launch_imag_init(const double *sums, const InstDev *inst, int ii, ImagScalars *imag, cudaStream_t s)
+{
+    imag_init_kernel<<<1, 1, 0, s>>>(sums, inst, ii, imag);
+    return cudaGetLastError();
+}
+
+__global__ void set_sigma_one_kernel(ImagScalars *__restrict__ imag, int n)
+{
+    for (int i = threadIdx.x; i < n; i += blockDim.x) imag[i].sigma = 1.0;
+}
+
+cudaError_t launch_set_sigma_one(ImagScalars *imag, int n, cudaStream_t s)
+{
+    set_sigma_one_kernel<<<1, 128, 0, s>>>(imag, n);
+    return cudaGetLastError();
+}
+
+}  // namespace gpe

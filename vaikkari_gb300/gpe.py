@@ -1,0 +1,323 @@
+"""ctypes binding of the C ABI in include/gpe.h (libvaikkari_gpe.so).
+
+This is the host-side mirror of the reference's solver call,
+``integrateInTime(state, block_scale, minp, maxp, iteration_period,
+number_of_iterations)`` (koodit/GrossPitaevskii/GPUGrossPitaevskii_BCC.cu:218):
+a :class:`Stepper` owns the device fields of one or many condensates, takes host
+arrays in the reference's block order, advances them with the GB300 kernels and
+returns fields and FP64 observables.  Every failing call raises
+:class:`GpeError` carrying the library's status and message (the reference
+exits the process instead, helper_cuda.h checkCudaErrors).
+
+There is no CPU fallback: if the native library is missing the import of the
+library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libvaikkari_gpe.so")
+
+
+class Lattice(enum.IntEnum):
+    TETRA12 = 0  # reference discretisation: 12 circumcentre values per block, 4 faces
+    BCC2 = 1     # 2 lattice-point values per block, 14 Hodge-weighted edges
+
+
+class Precision(enum.IntEnum):
+    FP64 = 0
+    FP32 = 1
+
+
+class Mode(enum.IntEnum):
+    REAL = 0
+    IMAGINARY = 1
+
+
+class Kernel(enum.IntEnum):
+    AUTO = 0
+    PLAIN = 1
+    FUSED = 2
+
+
+class Potential(enum.IntEnum):
+    ARRAY = 0
+    TRAP = 1
+
+
+class Status(enum.IntEnum):
+    OK = 0
+    INVALID_ARGUMENT = 1
+    CUDA = 2
+    OUT_OF_MEMORY = 3
+    NOT_FINITE = 4
+    UNSUPPORTED = 5
+    TOO_LARGE = 6
+    INTERNAL = 7
+
+
+class GpeError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        self.status = Status(status) if status in Status._value2member_map_ else status
+        super().__init__(f"{self.status!r}: {message}")
+
+
+class _LatticeInfo(C.Structure):
+    _fields_ = [
+        ("lattice", C.c_int32), ("slots", C.c_int32), ("neighbours", C.c_int32), ("classes", C.c_int32),
+        ("block_width", C.c_double), ("cell_volume", C.c_double), ("class_weight", C.c_double * 2),
+        ("position", (C.c_double * 3) * 12), ("entry", ((C.c_int32 * 5) * 14) * 12),
+    ]
+
+
+class _Instance(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+        ("block_scale", C.c_double), ("origin", C.c_double * 3), ("dt", C.c_double), ("g", C.c_double),
+        ("trap", C.c_double * 3),
+    ]
+
+
+class _Config(C.Structure):
+    _fields_ = [
+        ("lattice", C.c_int32), ("precision", C.c_int32), ("mode", C.c_int32), ("kernel", C.c_int32),
+        ("potential", C.c_int32), ("num_instances", C.c_int32), ("instances", C.POINTER(_Instance)),
+        ("graph_steps", C.c_int32), ("tile", C.c_int32), ("zchunk", C.c_int32), ("device", C.c_int32),
+    ]
+
+
+class _Observables(C.Structure):
+    _fields_ = [
+        ("norm", C.c_double), ("energy", C.c_double), ("mu", C.c_double), ("kinetic", C.c_double),
+        ("potential", C.c_double), ("interaction", C.c_double), ("finite", C.c_int32), ("pad_", C.c_int32),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads (once) and returns the native library; raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"native library not built: {path} (run `python -m vaikkari_gb300.build`)")
+    lib = C.CDLL(path)
+    st = C.c_int
+    lib.gpe_abi_version.restype = C.c_int32
+    lib.gpe_status_string.restype = C.c_char_p
+    lib.gpe_status_string.argtypes = [st]
+    lib.gpe_last_error.restype = C.c_char_p
+    lib.gpe_lattice_describe.restype = st
+    lib.gpe_lattice_describe.argtypes = [C.c_int32, C.POINTER(_LatticeInfo)]
+    lib.gpe_create.restype = st
+    lib.gpe_create.argtypes = [C.POINTER(_Config), C.POINTER(C.c_void_p)]
+    lib.gpe_destroy.restype = st
+    lib.gpe_destroy.argtypes = [C.c_void_p]
+    lib.gpe_upload.restype = st
+    lib.gpe_upload.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.gpe_download.restype = st
+    lib.gpe_download.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
+    lib.gpe_step.restype = st
+    lib.gpe_step.argtypes = [C.c_void_p, C.c_int64]
+    lib.gpe_synchronize.restype = st
+    lib.gpe_synchronize.argtypes = [C.c_void_p]
+    lib.gpe_observables_get.restype = st
+    lib.gpe_observables_get.argtypes = [C.c_void_p, C.c_int32, C.POINTER(_Observables)]
+    lib.gpe_imaginary_time.restype = st
+    lib.gpe_imaginary_time.argtypes = [C.c_void_p, C.c_int64, C.c_double, C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+    lib.gpe_launch_count.restype = C.c_int64
+    lib.gpe_launch_count.argtypes = [C.c_void_p]
+    lib.gpe_stream.restype = C.c_void_p
+    lib.gpe_stream.argtypes = [C.c_void_p]
+    _lib = lib
+    return lib
+
+
+def _check(status: int, what: str):
+    if status != 0:
+        msg = _lib.gpe_last_error().decode(errors="replace")
+        raise GpeError(status, f"{what}: {msg}")
+
+
+def lattice_info(lattice: Lattice) -> dict:
+    """Stencil tables of a lattice (replaces getLaplacian/getPositions,
+    GPUGrossPitaevskii_BCC.cu:69-142)."""
+    lib = load_library()
+    info = _LatticeInfo()
+    _check(lib.gpe_lattice_describe(int(lattice), C.byref(info)), "gpe_lattice_describe")
+    ns, nb = info.slots, info.neighbours
+    entry = np.array([[list(info.entry[s][k]) for k in range(nb)] for s in range(ns)], dtype=np.int32)
+    return {
+        "lattice": Lattice(info.lattice), "slots": ns, "neighbours": nb, "classes": info.classes,
+        "block_width": info.block_width, "cell_volume": info.cell_volume,
+        "class_weight": [info.class_weight[0], info.class_weight[1]][: info.classes],
+        "position": np.array([list(info.position[s]) for s in range(ns)]),
+        "entry": entry,
+    }
+
+
+@dataclass
+class Instance:
+    """One condensate: nx*ny*nz blocks of the lattice; see include/gpe.h."""
+    nx: int
+    ny: int
+    nz: int
+    block_scale: float
+    dt: float
+    g: float
+    origin: Sequence[float] = (0.0, 0.0, 0.0)
+    trap: Sequence[float] = (1.0, 1.0, 1.0)
+
+    def c(self) -> _Instance:
+        s = _Instance()
+        s.nx, s.ny, s.nz = self.nx, self.ny, self.nz
+        s.block_scale, s.dt, s.g = self.block_scale, self.dt, self.g
+        for k in range(3):
+            s.origin[k] = self.origin[k]
+            s.trap[k] = self.trap[k]
+        return s
+
+
+def value_positions(inst: Instance, info: dict) -> np.ndarray:
+    """Positions of every value of an instance, shape (nz, ny, nx, slots, 3), in
+    the reference's block order (GPUGrossPitaevskii_BCC.cu:258)."""
+    bw = info["block_width"]
+    i = np.arange(inst.nx)[None, None, :, None]
+    j = np.arange(inst.ny)[None, :, None, None]
+    k = np.arange(inst.nz)[:, None, None, None]
+    pos = info["position"]
+    out = np.empty((inst.nz, inst.ny, inst.nx, info["slots"], 3))
+    out[..., 0] = inst.origin[0] + inst.block_scale * (i * bw + pos[None, None, None, :, 0])
+    out[..., 1] = inst.origin[1] + inst.block_scale * (j * bw + pos[None, None, None, :, 1])
+    out[..., 2] = inst.origin[2] + inst.block_scale * (k * bw + pos[None, None, None, :, 2])
+    return out
+
+
+class Stepper:
+    """Device state of a batch of condensates (wraps gpe_create/gpe_destroy)."""
+
+    def __init__(self, instances: List[Instance], lattice=Lattice.BCC2, precision=Precision.FP32,
+                 mode=Mode.REAL, kernel=Kernel.AUTO, potential=Potential.ARRAY, graph_steps=0, tile=0,
+                 zchunk=0, device=0):
+        self.lib = load_library()
+        self.instances = list(instances)
+        self.lattice, self.precision, self.mode = Lattice(lattice), Precision(precision), Mode(mode)
+        self.potential = Potential(potential)
+        self.info = lattice_info(self.lattice)
+        self.slots = self.info["slots"]
+        self._carr = (_Instance * len(self.instances))(*[i.c() for i in self.instances])
+        cfg = _Config()
+        cfg.lattice, cfg.precision, cfg.mode = int(lattice), int(precision), int(mode)
+        cfg.kernel, cfg.potential = int(kernel), int(potential)
+        cfg.num_instances = len(self.instances)
+        cfg.instances = C.cast(self._carr, C.POINTER(_Instance))
+        cfg.graph_steps, cfg.tile, cfg.zchunk, cfg.device = graph_steps, tile, zchunk, device
+        h = C.c_void_p()
+        _check(self.lib.gpe_create(C.byref(cfg), C.byref(h)), "gpe_create")
+        self.h = h
+        self.dtype = np.float64 if self.precision == Precision.FP64 else np.float32
+
+    # -- helpers ------------------------------------------------------------
+    def shape(self, i: int):
+        if not 0 <= i < len(self.instances):
+            raise IndexError(f"instance {i} out of range")
+        inst = self.instances[i]
+        return (inst.nz, inst.ny, inst.nx, self.slots)
+
+    def _carray(self, a, shape, complex_=True):
+        """Host array in the handle's element type; complex fields may be given
+        as complex (shape) or interleaved real (shape + (2,))."""
+        if a is None:
+            return None, None
+        a = np.asarray(a)
+        if complex_:
+            if np.iscomplexobj(a):
+                a = np.stack([a.real, a.imag], axis=-1)
+            want = tuple(shape) + (2,)
+        else:
+            if np.iscomplexobj(a):
+                raise ValueError("the potential must be real")
+            want = tuple(shape)
+        if a.shape != want:
+            raise ValueError(f"array shape {a.shape} does not match {want} "
+                             "(block order (nz, ny, nx, slots), complex or interleaved (..., 2))")
+        a = np.ascontiguousarray(a, dtype=self.dtype)
+        return a, a.ctypes.data_as(C.c_void_p)
+
+    # -- API ----------------------------------------------------------------
+    def upload(self, i: int, even, odd=None, potential=None):
+        """even/odd: complex arrays (nz, ny, nx, slots) or real (..., 2); potential: V (unscaled)."""
+        shp = self.shape(i)
+        e, pe = self._carray(even, shp)
+        o, po = self._carray(odd, shp)
+        v, pv = self._carray(potential, shp, complex_=False)
+        _check(self.lib.gpe_upload(self.h, i, pe, po, pv), "gpe_upload")
+
+    def download(self, i: int, odd: bool = True):
+        shp = self.shape(i) + (2,)
+        e = np.empty(shp, self.dtype)
+        o = np.empty(shp, self.dtype) if odd else None
+        _check(self.lib.gpe_download(self.h, i, e.ctypes.data_as(C.c_void_p),
+                                     o.ctypes.data_as(C.c_void_p) if odd else None), "gpe_download")
+        return e, o
+
+    def step(self, steps: int):
+        _check(self.lib.gpe_step(self.h, int(steps)), "gpe_step")
+
+    def synchronize(self):
+        _check(self.lib.gpe_synchronize(self.h), "gpe_synchronize")
+
+    def observables(self, field_: int = 0) -> List[dict]:
+        n = len(self.instances)
+        arr = (_Observables * n)()
+        st = self.lib.gpe_observables_get(self.h, field_, arr)
+        out = [{k: getattr(o, k) for k in ("norm", "energy", "mu", "kinetic", "potential", "interaction")}
+               | {"finite": bool(o.finite)} for o in arr]
+        _check(st, "gpe_observables_get")
+        return out
+
+    def imaginary_time(self, max_steps: int, tol: float):
+        steps = C.c_int64()
+        conv = C.c_int32()
+        mu = (C.c_double * len(self.instances))()
+        _check(self.lib.gpe_imaginary_time(self.h, int(max_steps), float(tol), C.byref(steps), C.byref(conv), mu),
+               "gpe_imaginary_time")
+        return steps.value, bool(conv.value), list(mu)
+
+    def launch_count(self) -> int:
+        return int(self.lib.gpe_launch_count(self.h))
+
+    def stream_handle(self) -> int:
+        """The cudaStream_t the library launches on (as an integer)."""
+        return int(self.lib.gpe_stream(self.h) or 0)
+
+    def total_values(self) -> int:
+        return sum(i.nx * i.ny * i.nz for i in self.instances) * self.slots
+
+    def close(self):
+        if getattr(self, "h", None):
+            st = self.lib.gpe_destroy(self.h)
+            self.h = None
+            _check(st, "gpe_destroy")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
