@@ -51,7 +51,10 @@ typedef enum gpe_status {
     GPE_ERR_NOT_FINITE = 4,       /* NaN/Inf seen by the observables watchdog    */
     GPE_ERR_UNSUPPORTED = 5,      /* combination not built (e.g. fused TETRA12)  */
     GPE_ERR_TOO_LARGE = 6,        /* size beyond a documented maximum            */
-    GPE_ERR_INTERNAL = 7          /* lattice construction failed a self-check    */
+    GPE_ERR_INTERNAL = 7,         /* lattice construction failed a self-check    */
+    GPE_ERR_TIMEOUT = 8           /* a bounded wait inside a kernel ran out; the
+                                     launch returned early and the fields of that
+                                     step are not valid                           */
 } gpe_status;
 
 typedef enum gpe_lattice {

@@ -126,6 +126,105 @@ void oracle_leapfrog_f32(const oracle_grid *g, float *even, float *odd, const fl
     }
 }
 
+/* BCC2 in the fused kernel's order (see gpe_oracle.h). */
+#define BCC2_BODY(T, FMA)                                                                           \
+    const int nx = g->nx, ny = g->ny, nz = g->nz;                                                  \
+    const T L0 = (T)g->L0, gdt = (T)g->gdt;                                                         \
+    const T Lc0 = (T)g->Lc[0], Lc1 = (T)g->Lc[1];                                                   \
+    int z;                                                                                          \
+    _Pragma("omp parallel for schedule(static) num_threads(oracle_get_threads())")                  \
+    for (z = 0; z < nz; z++) {                                                                      \
+        for (int y = 0; y < ny; y++)                                                                \
+            for (int x = 0; x < nx; x++) {                                                          \
+                T vx[2][3][3][3], vy[2][3][3][3]; /* [slot][dz+1][dy+1][dx+1] */                    \
+                for (int s = 0; s < 2; s++)                                                         \
+                    for (int dz = -1; dz <= 1; dz++)                                                \
+                        for (int dy = -1; dy <= 1; dy++)                                            \
+                            for (int dx = -1; dx <= 1; dx++) {                                      \
+                                const int xx = x + dx, yy = y + dy, zz = z + dz;                    \
+                                T a = 0, b = 0;                                                     \
+                                if (xx >= 0 && xx < nx && yy >= 0 && yy < ny && zz >= 0 && zz < nz) { \
+                                    const size_t o = IDX(g, xx, yy, zz, s);                         \
+                                    a = prev[2 * o];                                                \
+                                    b = prev[2 * o + 1];                                            \
+                                    if (mode == 1) {                                                \
+                                        a = sigma * a;                                              \
+                                        b = sigma * b;                                              \
+                                    }                                                               \
+                                }                                                                   \
+                                vx[s][dz + 1][dy + 1][dx + 1] = a;                                  \
+                                vy[s][dz + 1][dy + 1][dx + 1] = b;                                  \
+                            }                                                                       \
+                for (int s = 0; s < 2; s++) {                                                       \
+                    T sdx, sdy, sax, say;                                                           \
+                    const T(*X)[3][3] = vx[s];                                                      \
+                    const T(*Y)[3][3] = vy[s];                                                      \
+                    const T(*OX)[3][3] = vx[1 - s];                                                 \
+                    const T(*OY)[3][3] = vy[1 - s];                                                 \
+                    if (s == 0) { /* boxes of B at planes z-1, z around (x-1..x, y-1..y) */         \
+                        const T b0x = (OX[0][0][0] + OX[0][0][1]) + (OX[0][1][0] + OX[0][1][1]);    \
+                        const T b0y = (OY[0][0][0] + OY[0][0][1]) + (OY[0][1][0] + OY[0][1][1]);    \
+                        const T b1x = (OX[1][0][0] + OX[1][0][1]) + (OX[1][1][0] + OX[1][1][1]);    \
+                        const T b1y = (OY[1][0][0] + OY[1][0][1]) + (OY[1][1][0] + OY[1][1][1]);    \
+                        sdx = b0x + b1x;                                                            \
+                        sdy = b0y + b1y;                                                            \
+                    } else { /* boxes of C at planes z, z+1 around (x..x+1, y..y+1) */              \
+                        const T b0x = (OX[1][1][1] + OX[1][1][2]) + (OX[1][2][1] + OX[1][2][2]);    \
+                        const T b0y = (OY[1][1][1] + OY[1][1][2]) + (OY[1][2][1] + OY[1][2][2]);    \
+                        const T b1x = (OX[2][1][1] + OX[2][1][2]) + (OX[2][2][1] + OX[2][2][2]);    \
+                        const T b1y = (OY[2][1][1] + OY[2][1][2]) + (OY[2][2][1] + OY[2][2][2]);    \
+                        sdx = b0x + b1x;                                                            \
+                        sdy = b0y + b1y;                                                            \
+                    }                                                                               \
+                    sax = (X[0][1][1] + X[2][1][1]) + ((X[1][1][0] + X[1][1][2]) + (X[1][0][1] + X[1][2][1])); \
+                    say = (Y[0][1][1] + Y[2][1][1]) + ((Y[1][1][0] + Y[1][1][2]) + (Y[1][0][1] + Y[1][2][1])); \
+                    const T px = X[1][1][1], py = Y[1][1][1];                                       \
+                    const size_t o = IDX(g, x, y, z, s);                                            \
+                    const T nrm = FMA(px, px, py * py);                                             \
+                    const T cc = FMA(gdt, nrm, L0 + vdt[o]);                                        \
+                    T ax = Lc0 * sdx, ay = Lc0 * sdy;                                               \
+                    ax = FMA(Lc1, sax, ax);                                                         \
+                    ay = FMA(Lc1, say, ay);                                                         \
+                    const T hx = FMA(cc, px, ax), hy = FMA(cc, py, ay);                             \
+                    if (mode == 0) {                                                                \
+                        next[2 * o] = next[2 * o] + hy;                                             \
+                        next[2 * o + 1] = next[2 * o + 1] - hx;                                     \
+                    } else {                                                                        \
+                        next[2 * o] = px - hx;                                                      \
+                        next[2 * o + 1] = py - hy;                                                  \
+                    }                                                                               \
+                }                                                                                   \
+            }                                                                                       \
+    }
+
+void oracle_half_step_bcc2_f64(const oracle_grid *g, const double *prev, double *next, const double *vdt, int mode,
+                               double sigma)
+{
+    BCC2_BODY(double, fma)
+}
+
+void oracle_half_step_bcc2_f32(const oracle_grid *g, const float *prev, float *next, const float *vdt, int mode,
+                               float sigma)
+{
+    BCC2_BODY(float, fmaf)
+}
+
+void oracle_leapfrog_bcc2_f64(const oracle_grid *g, double *even, double *odd, const double *vdt, long steps)
+{
+    for (long k = 0; k < steps; k++) {
+        oracle_half_step_bcc2_f64(g, even, odd, vdt, 0, 1.0);
+        oracle_half_step_bcc2_f64(g, odd, even, vdt, 0, 1.0);
+    }
+}
+
+void oracle_leapfrog_bcc2_f32(const oracle_grid *g, float *even, float *odd, const float *vdt, long steps)
+{
+    for (long k = 0; k < steps; k++) {
+        oracle_half_step_bcc2_f32(g, even, odd, vdt, 0, 1.0f);
+        oracle_half_step_bcc2_f32(g, odd, even, vdt, 0, 1.0f);
+    }
+}
+
 typedef struct {
     double s, c;
 } kahan_t;

@@ -43,6 +43,24 @@ void oracle_half_step_f64(const oracle_grid *g, const double *prev, double *next
 void oracle_half_step_f32(const oracle_grid *g, const float *prev, float *next, const float *vdt, int mode,
                           float sigma);
 
+/* BCC2 lattice only, in the summation order of the fused GPU kernel, which
+ * reuses 2x2 diagonal box sums and axial pair sums across planes.  With
+ * C = slot 0 (cube corner), B = slot 1 (cube centre), zero outside the grid,
+ * every value pre-multiplied by sigma in imaginary time:
+ *   bB(x,y,q) = (B(x-1,y-1,q) + B(x,y-1,q)) + (B(x-1,y,q) + B(x,y,q))
+ *   bC(x,y,q) = (C(x,y,q) + C(x+1,y,q)) + (C(x,y+1,q) + C(x+1,y+1,q))
+ *   slot 0:  Sd = bB(z-1) + bB(z)
+ *            Sa = (C(z-1) + C(z+1)) + ((C(x-1) + C(x+1)) + (C(y-1) + C(y+1)))
+ *   slot 1:  Sd = bC(z) + bC(z+1)
+ *            Sa = (B(z-1) + B(z+1)) + ((B(x-1) + B(x+1)) + (B(y-1) + B(y+1)))
+ * then the same h and integrator as oracle_half_step_*. */
+void oracle_half_step_bcc2_f64(const oracle_grid *g, const double *prev, double *next, const double *vdt, int mode,
+                               double sigma);
+void oracle_half_step_bcc2_f32(const oracle_grid *g, const float *prev, float *next, const float *vdt, int mode,
+                               float sigma);
+void oracle_leapfrog_bcc2_f64(const oracle_grid *g, double *even, double *odd, const double *vdt, long steps);
+void oracle_leapfrog_bcc2_f32(const oracle_grid *g, float *even, float *odd, const float *vdt, long steps);
+
 /* `steps` leapfrog steps (odd <- even, even <- odd). */
 void oracle_leapfrog_f64(const oracle_grid *g, double *even, double *odd, const double *vdt, long steps);
 void oracle_leapfrog_f32(const oracle_grid *g, float *even, float *odd, const float *vdt, long steps);

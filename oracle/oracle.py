@@ -42,6 +42,10 @@ def load():
     G = C.POINTER(_Grid)
     lib.oracle_half_step_f64.argtypes = [G, vp, vp, vp, C.c_int, dp]
     lib.oracle_half_step_f32.argtypes = [G, vp, vp, vp, C.c_int, C.c_float]
+    lib.oracle_half_step_bcc2_f64.argtypes = [G, vp, vp, vp, C.c_int, dp]
+    lib.oracle_half_step_bcc2_f32.argtypes = [G, vp, vp, vp, C.c_int, C.c_float]
+    lib.oracle_leapfrog_bcc2_f64.argtypes = [G, vp, vp, vp, C.c_long]
+    lib.oracle_leapfrog_bcc2_f32.argtypes = [G, vp, vp, vp, C.c_long]
     lib.oracle_leapfrog_f64.argtypes = [G, vp, vp, vp, C.c_long]
     lib.oracle_leapfrog_f32.argtypes = [G, vp, vp, vp, C.c_long]
     lib.oracle_observables_f64.argtypes = [G, vp, vp, dp, dp, vp, vp]
@@ -112,6 +116,15 @@ class Grid:
         for a in (even, odd, vdt):
             assert a.flags.c_contiguous
         fn = lib.oracle_leapfrog_f64 if even.dtype == np.float64 else lib.oracle_leapfrog_f32
+        fn(C.byref(self._g), self._p(even), self._p(odd), self._p(vdt), int(steps))
+
+    def leapfrog_bcc2(self, even, odd, vdt, steps):
+        """In place, BCC2 only, in the fused GPU kernel's summation order."""
+        lib = load()
+        assert self.slots == 2 and self.neighbours == 14
+        for a in (even, odd, vdt):
+            assert a.flags.c_contiguous
+        fn = lib.oracle_leapfrog_bcc2_f64 if even.dtype == np.float64 else lib.oracle_leapfrog_bcc2_f32
         fn(C.byref(self._g), self._p(even), self._p(odd), self._p(vdt), int(steps))
 
     def observables(self, psi, vdt, vol):

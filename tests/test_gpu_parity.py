@@ -44,7 +44,10 @@ def _run_real(lattice, prec, kernel, potential, dims_list, steps=3, tile=0, grap
         g = grid_for(st, i)
         vdt = vdt_for(st, i, V)
         e, o = interleave(even, T), interleave(odd, T)
-        g.leapfrog(e, o, vdt, steps)
+        if lattice == Lattice.BCC2 and kernel != Kernel.PLAIN:
+            g.leapfrog_bcc2(e, o, vdt, steps)   # the fused kernel's summation order
+        else:
+            g.leapfrog(e, o, vdt, steps)
         want.append((e, o))
     st.step(steps)
     for i in range(len(insts)):

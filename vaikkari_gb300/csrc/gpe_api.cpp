@@ -10,6 +10,7 @@
 // chunks are replayed from captured CUDA graphs, and errors come back as status
 // codes instead of exit().
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -65,7 +66,7 @@ struct gpe_handle_ {
     void *buf[2] = {nullptr, nullptr};  // even, odd (or psi and its ping-pong partner)
     void *vpot = nullptr;
     bool fused = false;
-    int tile = 0, tx = 32, ty = 8, zchunk = 0;
+    int tile = 0, tx = 32, ty = 8, zchunk = 0, zcmax = 1;
     std::vector<WorkItem> items;
     WorkItem *items_dev = nullptr;
     int *item_begin_dev = nullptr;
@@ -73,6 +74,8 @@ struct gpe_handle_ {
     ImagScalars *imag = nullptr;
     double *partials = nullptr;       // fused imaginary-time rows
     unsigned int *counter = nullptr;
+    void *maps = nullptr;             // fused: CUtensorMap[num_instances][2]
+    int *err = nullptr;               // device error word of the bounded waits
     double *obs_partials = nullptr;   // observables CTA rows
     double *obs_sums = nullptr;       // per instance, 6 sums
     int obs_max_ctas = 2048;
@@ -93,6 +96,20 @@ size_t round_up(size_t v, size_t m) { return (v + m - 1) / m * m; }
 gpe_status check_handle(gpe_handle h)
 {
     if (!h) return fail(GPE_ERR_INVALID_ARGUMENT, "null handle");
+    return GPE_OK;
+}
+
+// Synchronises the stream and reads the kernels' error word.
+gpe_status sync_and_check(gpe_handle h)
+{
+    GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    int err = 0;
+    GPE_CUDA_TRY(cudaMemcpy(&err, h->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err != 0) {
+        cudaMemsetAsync(h->err, 0, sizeof(int), h->stream);
+        cudaStreamSynchronize(h->stream);
+        return fail(GPE_ERR_TIMEOUT, "a bounded wait in the fused kernel ran out; the step was abandoned");
+    }
     return GPE_OK;
 }
 
@@ -136,6 +153,10 @@ gpe_status enqueue_step_real(gpe_handle h)
             l.prev = prev;
             l.next = next;
             l.vpot = h->vpot;
+            l.maps = h->maps;
+            l.zcmax = h->zcmax;
+            l.src = half == 0 ? 0 : 1;
+            l.err = h->err;
             l.num_instances = h->cfg.num_instances;
             GPE_CUDA_TRY(launch_fused_step(l, h->stream));
             h->launches++;
@@ -203,6 +224,10 @@ gpe_status enqueue_step_imag(gpe_handle h, int parity)
         l.prev = prev;
         l.next = next;
         l.vpot = h->vpot;
+        l.maps = h->maps;
+        l.zcmax = h->zcmax;
+        l.src = parity;
+        l.err = h->err;
         l.imag = h->imag;
         l.partials = h->partials;
         l.counter = h->counter;
@@ -341,6 +366,8 @@ void free_handle(gpe_handle h)
     cudaFree(h->counter);
     cudaFree(h->obs_partials);
     cudaFree(h->obs_sums);
+    cudaFree(h->maps);
+    cudaFree(h->err);
     cudaFree(h->staging);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -381,6 +408,7 @@ const char *gpe_status_string(gpe_status s)
     case GPE_ERR_UNSUPPORTED: return "unsupported";
     case GPE_ERR_TOO_LARGE: return "too large";
     case GPE_ERR_INTERNAL: return "internal error";
+    case GPE_ERR_TIMEOUT: return "device wait timed out";
     }
     return "unknown status";
 }
@@ -553,6 +581,8 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
     }
     GPE_CREATE_TRY(cudaMemcpyAsync(h->imag, imag_init.data(), sizeof(ImagScalars) * imag_init.size(),
                                    cudaMemcpyHostToDevice, h->stream));
+    GPE_CREATE_TRY(cudaMalloc(&h->err, sizeof(int)));
+    GPE_CREATE_TRY(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
     GPE_CREATE_TRY(cudaMalloc(&h->obs_partials, sizeof(double) * 6 * h->obs_max_ctas));
     GPE_CREATE_TRY(cudaMalloc(&h->obs_sums, sizeof(double) * 6 * cfg->num_instances));
 
@@ -585,6 +615,8 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
             if (zc < 8) zc = std::min<long long>(8, maxnz);
         }
         h->zchunk = zc;
+        h->zcmax = 1;
+        for (auto &in : h->inst) h->zcmax = std::max(h->zcmax, std::min(in.nz, zc));
         std::vector<std::vector<WorkItem>> per(cfg->num_instances);
         for (int i = 0; i < cfg->num_instances; i++) {
             const gpe_instance &in = h->inst[i];
@@ -604,6 +636,19 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
             ranges[2 * i] = first[i];
             ranges[2 * i + 1] = first[i] + int(per[i].size());
         }
+        // TMA halo maps, one per instance and field.
+        std::vector<CUtensorMap> maps(4 * cfg->num_instances);
+        for (int i = 0; i < cfg->num_instances; i++)
+            for (int f = 0; f < 2; f++) {
+                gpe_status ms = make_halo_map(&maps[4 * i + 2 * f], cfg->precision, h->idev_host[i], h->buf[f], h->tile);
+                if (ms != GPE_OK) {
+                    free_handle(h);
+                    return ms;
+                }
+            }
+        GPE_CREATE_TRY(cudaMalloc(&h->maps, sizeof(CUtensorMap) * maps.size()));
+        GPE_CREATE_TRY(cudaMemcpyAsync(h->maps, maps.data(), sizeof(CUtensorMap) * maps.size(),
+                                       cudaMemcpyHostToDevice, h->stream));
         GPE_CREATE_TRY(cudaMalloc(&h->items_dev, sizeof(WorkItem) * h->items.size()));
         GPE_CREATE_TRY(cudaMemcpyAsync(h->items_dev, h->items.data(), sizeof(WorkItem) * h->items.size(),
                                        cudaMemcpyHostToDevice, h->stream));
@@ -688,6 +733,8 @@ gpe_status gpe_download(gpe_handle h, int32_t instance, void *even, void *odd)
     if (st != GPE_OK) return st;
     if (instance < 0 || instance >= h->cfg.num_instances)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_download: bad instance");
+    st = sync_and_check(h);
+    if (st != GPE_OK) return st;
     const gpe_instance &in = h->inst[instance];
     const size_t vals = size_t(in.nx) * in.ny * in.nz * h->ns;
     int src0 = (h->cfg.mode == GPE_IMAGINARY_TIME) ? h->parity : 0;
@@ -727,8 +774,7 @@ gpe_status gpe_synchronize(gpe_handle h)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
-    GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
-    return GPE_OK;
+    return sync_and_check(h);
 }
 
 gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out)
@@ -744,7 +790,8 @@ gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out
     std::vector<double> sums(6 * h->cfg.num_instances);
     GPE_CUDA_TRY(cudaMemcpyAsync(sums.data(), h->obs_sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost,
                                  h->stream));
-    GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    st = sync_and_check(h);
+    if (st != GPE_OK) return st;
     bool all_finite = true;
     for (int i = 0; i < h->cfg.num_instances; i++) {
         const double vol = h->idev_host[i].vol;
@@ -787,7 +834,8 @@ gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64
         if (st != GPE_OK) return st;
         GPE_CUDA_TRY(cudaMemcpyAsync(sc.data(), h->imag, sizeof(ImagScalars) * sc.size(), cudaMemcpyDeviceToHost,
                                      h->stream));
-        GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+        st = sync_and_check(h);
+        if (st != GPE_OK) return st;
         all = true;
         for (auto &s : sc) all = all && (s.conv_step >= 0);
         if (all) break;

@@ -3,22 +3,47 @@
 // instance of a batch in one launch.
 //
 // Work decomposition: a work item is (instance, TX x TY tile of block columns,
-// z-range).  A CTA of TX*TY threads owns one item at a time; thread (tx,ty)
-// owns block column (x0+tx, y0+ty) and marches up the z-range.  Shared memory
-// holds a ring of three z-planes of the previous field (both slots, tile plus a
-// one-block halo); the plane two ahead is loaded into registers while the current
-// plane is computed, so each previous-field value is read from HBM once per
-// half-step (halo re-reads hit L2).  The next field is read-modified-written with
-// coalesced row segments; V comes from the potential arena or per-axis trap
-// tables.  Update arithmetic is gpe_device.cuh's hpsi/integrate, in the summation
-// order of the BCC2 table (diagonal class first, then axial; each by dz, dy, dx).
+// z-range [z0, z1)); one CTA of TX*TY threads per item; thread (tx, ty) owns
+// block column (x0+tx, y0+ty) and marches up z.
 //
-// Imaginary time adds fused reductions: per thread FP32/FP64 partial sums, FP64
-// across the CTA, one row per work item, and the last CTA to finish reduces each
-// instance's rows in fixed order (deterministic) and updates its ImagScalars
-// (next scale, mu, energy, convergence step).
+// Data movement (sm_103a), warp-specialised:
+//  * One producer warp issues TMA copies into a STAGES-deep shared-memory ring:
+//    for every plane q in [z0-1, z1] a cp.async.bulk.tensor 4-D copy brings the
+//    previous field's tile plus halo (x0-2 .. x0+TX+1 so that the copy starts
+//    on a 16-byte boundary, y0-1 .. y0+TY, both slots), and in the same stage
+//    the next field's interior tile of plane q-1 (read-modify-write input).
+//    Each stage has a "full" mbarrier (transaction bytes) and an "empty"
+//    mbarrier (one arrival per consumer warp); the producer refills a stage
+//    once every consumer warp has released it, so warps never wait for each
+//    other at a CTA-wide barrier and up to STAGES planes are in flight.
+//  * Each consumer thread reads a plane from shared memory once (12 values of
+//    its 3x3 neighbourhood, both slots, plus its next-field values) and carries
+//    what later planes need in registers: its own values of the previous two
+//    planes, the pending diagonal sum and box sum, the in-plane axial sums.
+//  * Results are stored with coalesced row writes straight from registers.
+//    The trap potential's z-term of the CTA's z-range is staged in shared
+//    memory once; an array potential is read with plain loads.
+//
+// Summation order (the oracle's oracle_half_step_bcc2_* mirrors it bit for bit),
+// with C = slot 0 (cube corner), B = slot 1 (cube centre):
+//   bB(q) = (B(x-1,y-1) + B(x,y-1)) + (B(x-1,y) + B(x,y))      at plane q
+//   bC(q) = (C(x,y) + C(x+1,y)) + (C(x,y+1) + C(x+1,y+1))      at plane q
+//   slot 0 at z: Sd = bB(z-1) + bB(z), Sa = (C(z-1) + C(z+1)) + ((C(x-1) + C(x+1)) + (C(y-1) + C(y+1)))
+//   slot 1 at z: Sd = bC(z) + bC(z+1), Sa = (B(z-1) + B(z+1)) + ((B(x-1) + B(x+1)) + (B(y-1) + B(y+1)))
+// followed by gpe_device.cuh's hpsi/integrate (the reference's update,
+// GPUGrossPitaevskii_BCC.cu:207-215).
+//
+// Every mbarrier wait is bounded; on timeout the CTA records an error code,
+// waits (bounded) for its own copies in flight, and returns.
+//
+// Imaginary time adds fused reductions: per-thread compensated sums, FP64
+// across the CTA, one row per work item; the last CTA to finish reduces each
+// instance's rows in fixed order and updates its ImagScalars.
 
+#include <cuda.h>
 #include <cuda_runtime.h>
+
+#include <string>
 
 #include "gpe_internal.h"
 
@@ -28,6 +53,9 @@ struct FusedArgs {
     const InstDev *__restrict__ inst;
     const WorkItem *__restrict__ items;
     int num_items;
+    const CUtensorMap *maps;  // [instance][field][halo box, interior box]
+    int zcmax;                // longest z-range of a work item
+    int src;                  // field the previous values come from (0 or 1)
     const void *prev;
     void *next;
     const void *vpot;
@@ -37,15 +65,16 @@ struct FusedArgs {
     const int *inst_item_begin;
     int num_instances;
     double tol;
+    int *err;
 };
 
-template <typename T> struct Acc;      // per-thread partial sum
+template <typename T> struct Acc;
 template <> struct Acc<double> {
     double s = 0.0;
     __device__ void add(double v) { s += v; }
     __device__ double value() const { return s; }
 };
-template <> struct Acc<float> {       // compensated FP32
+template <> struct Acc<float> {  // compensated FP32
     float s = 0.f, c = 0.f;
     __device__ void add(float v)
     {
@@ -57,254 +86,447 @@ template <> struct Acc<float> {       // compensated FP32
     __device__ double value() const { return double(s) - double(c); }
 };
 
-__device__ __forceinline__ int ring_of(int zz) { return ((zz % 3) + 3) % 3; }
+// ---- PTX helpers -----------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-template <typename T, int TX, int TY, int MODE, int POT>
-__global__ void __launch_bounds__(TX *TY) fused_bcc2_kernel(const FusedArgs a)
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
 {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: about a second at most (each try_wait suspends briefly).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
+{
+    for (int i = 0; i < (1 << 22); i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(dst),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+
+constexpr int kErrTimeout = 1;
+
+template <typename T, int TX, int TY>
+struct FusedShape {
     using T2 = typename Cplx<T>::type;
-    constexpr int NT = TX * TY;
-    constexpr int PW = TX + 2, PH = TY + 2;
-    constexpr int PLANE = 2 * PW * PH;
-    constexpr int NLD = (PLANE + NT - 1) / NT;
-    __shared__ T2 ring[3][2][PH][PW];
+    static constexpr int NT = TX * TY;       // consumer threads
+    static constexpr int NTHREADS = NT + 32; // plus the producer warp
+    static constexpr int BW = TX + 4;        // x0-2 .. x0+TX+1
+    static constexpr int BH = TY + 2;        // y0-1 .. y0+TY
+    static constexpr int SLOT = BW * BH;
+    static constexpr int HALO_BYTES = 2 * SLOT * (int)sizeof(T2);
+    static constexpr int NEXT_BYTES = 2 * TX * TY * (int)sizeof(T2);
+    static constexpr int NEXT_OFF = ((HALO_BYTES + 127) / 128) * 128;
+    static constexpr int STAGE_BYTES = ((NEXT_OFF + NEXT_BYTES + 127) / 128) * 128;
+    static constexpr int XE = (int)sizeof(T2) / 8;  // 8-byte TMA elements per complex
+};
 
-    const T2 *__restrict__ prev = (const T2 *)a.prev;
-    T2 *__restrict__ next = (T2 *)a.next;
-    const T *__restrict__ vpot = (const T *)a.vpot;
+template <typename T, int TX, int TY, int STAGES>
+int fused_smem_bytes(int zcmax)
+{
+    return STAGES * FusedShape<T, TX, TY>::STAGE_BYTES + 128 /* align */ + 16 * STAGES /* barriers */ +
+           2 * zcmax * (int)sizeof(T) + 16;
+}
+
+// FP64 values need twice the registers: ask for half the resident CTAs.
+template <typename T, int MINB> struct MinBlocks {
+    static constexpr int value = sizeof(T) == 8 ? (MINB + 1) / 2 : MINB;
+};
+
+template <typename T, int TX, int TY, int MODE, int POT, int STAGES, int MINB>
+__global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_bcc2_kernel(const FusedArgs a)
+{
+    using S = FusedShape<T, TX, TY>;
+    using T2 = typename S::T2;
+    constexpr int NT = S::NT;
+    constexpr int NWARPS = S::NTHREADS / 32;
+    extern __shared__ unsigned char dyn_smem[];
+    const uint32_t raw = smem_u32(dyn_smem);
+    const uint32_t base = (raw + 127u) & ~127u;
+    unsigned char *const gbase = dyn_smem + (base - raw);
+    const uint32_t full = base + STAGES * S::STAGE_BYTES;
+    const uint32_t empty = full + 8 * STAGES;
+    T *const ztab = (T *)(gbase + STAGES * S::STAGE_BYTES + 16 * STAGES);
+    __shared__ int abort_flag;
+
     const int tid = threadIdx.x;
-    const int tx = tid % TX, ty = tid / TX;
-    const int lx = tx + 1, ly = ty + 1;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int it = blockIdx.x;
+    const WorkItem w = a.items[it];
+    const InstDev &d = a.inst[w.inst];
+    const int nplanes = w.z1 - w.z0 + 2;  // planes z0-1 .. z1
+    const int nz = d.nz;
 
-    for (int it = blockIdx.x; it < a.num_items; it += gridDim.x) {
-        const WorkItem w = a.items[it];
-        const InstDev &d = a.inst[w.inst];
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int st = 0; st < STAGES; st++) {
+            mbar_init(full + 8 * st, 1);
+            mbar_init(empty + 8 * st, NT / 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (POT == GPE_POTENTIAL_TRAP) {
+        // z-term of the trap for this item's z-range, both slots
+        const T *tz = (const T *)a.vpot + d.vbase + 2ll * d.nx + 2ll * d.ny;
+        const int zl = w.z1 - w.z0;
+        for (int i = tid; i < 2 * zl; i += S::NTHREADS) {
+            const int sl = i / zl, z = w.z0 + (i - sl * zl);
+            ztab[i] = tz[sl * nz + z];
+        }
+    }
+    __syncthreads();
+
+    if (warp == NWARPS - 1) {
+        // ---- producer warp ------------------------------------------------
+        if (lane == 0) {
+            const CUtensorMap *halo = a.maps + 4 * w.inst + 2 * a.src;
+            const CUtensorMap *inner = a.maps + 4 * w.inst + 2 * (1 - a.src) + 1;
+            int issued = 0;
+            for (int k = 0; k < nplanes; k++) {
+                const int st = k % STAGES;
+                if (k >= STAGES) {
+                    bool ok = false;
+                    for (int i = 0; i < (1 << 22) && !ok; i++) {
+                        ok = mbar_try_wait(empty + 8 * st, ((k / STAGES) - 1) & 1);
+                        if (!ok && *(volatile int *)&abort_flag) break;
+                    }
+                    if (!ok) {
+                        atomicExch(a.err, kErrTimeout);
+                        abort_flag = 1;
+                        break;
+                    }
+                }
+                const bool with_next = (MODE == 0) && (k >= 2);
+                mbar_arrive_expect_tx(full + 8 * st, S::HALO_BYTES + (with_next ? S::NEXT_BYTES : 0));
+                // padded coordinates: x0-2 -> x0, y0-1 -> y0, plane q -> q+1
+                tma_load_4d(base + st * S::STAGE_BYTES, halo, w.x0 * S::XE, w.y0, 0, w.z0 + k, full + 8 * st);
+                if (with_next)  // next field, interior tile of plane q-1 = z0+k-2
+                    tma_load_4d(base + st * S::STAGE_BYTES + S::NEXT_OFF, inner, (w.x0 + 2) * S::XE, w.y0 + 1, 0,
+                                w.z0 + k - 1, full + 8 * st);
+                issued = k + 1;
+            }
+            if (abort_flag) {
+                // let the copies this CTA issued land (bounded) before it exits
+                for (int k = (issued > STAGES ? issued - STAGES : 0); k < issued; k++)
+                    mbar_wait_bounded(full + 8 * (k % STAGES), (k / STAGES) & 1);
+            }
+        }
+    } else {
+        // ---- consumer warps ----------------------------------------------
+        const int tx = tid % TX, ty = tid / TX;
         const int x = w.x0 + tx, y = w.y0 + ty;
         const bool valid = (x < d.nx) && (y < d.ny);
+        const long long zstride = d.zstride, plane = d.plane;
+        const long long col = field_index(d, 0, x, y, 0);
+        const long long voff = d.vbase - d.base;
         const T sig = (MODE == 1) ? T(a.imag[w.inst].sigma) : T(1);
-        T Lw[2] = {T(d.Lc[0]), T(d.Lc[1])};
+        const T Lw[2] = {T(d.Lc[0]), T(d.Lc[1])};
         const T L0 = T(d.L0), gdt = T(d.gdt);
+        T2 *__restrict__ nxt = (T2 *)a.next;
+        const T *__restrict__ vpot = (const T *)a.vpot;
+        T vxy0 = T(0), vxy1 = T(0);
+        if (POT == GPE_POTENTIAL_TRAP && valid) {
+            const T *tx_ = vpot + d.vbase;
+            const T *ty_ = tx_ + 2ll * d.nx;
+            vxy0 = d_add(tx_[x], ty_[y]);
+            vxy1 = d_add(tx_[d.nx + x], ty_[d.ny + y]);
+        }
+        const int zl = w.z1 - w.z0;
+
+        // carried state (see the summation order above)
+        const T2 zero2 = {T(0), T(0)};
+        T2 cm = zero2, cc = zero2, bm = zero2, bc = zero2;  // own C, B at planes z-1, z
+        T2 axyC = zero2, axyB = zero2;                        // in-plane axial sums at plane z
+        T2 bBp = zero2, sd0 = zero2, bCc = zero2;             // bB(z), Sd of slot 0 at z, bC(z)
         Acc<T> s0, s1, s2, s3;
-
-        auto fetch = [&](int i, int zz) -> T2 {
-            const int s = i / (PW * PH);
-            const int r = i - s * (PW * PH);
-            const int py = r / PW, pxl = r - py * PW;
-            const int xx = w.x0 - 1 + pxl, yy = w.y0 - 1 + py;
-            T2 v;
-            if (xx <= d.nx && yy <= d.ny) {
-                v = prev[field_index(d, s, xx, yy, zz)];
+        const int lx = tx + 2, ly = ty + 1;
+        for (int k = 0; k < nplanes; k++) {
+            const int st = k % STAGES;
+            if (!mbar_wait_bounded(full + 8 * st, (k / STAGES) & 1)) {
+                atomicExch(a.err, kErrTimeout);
+                abort_flag = 1;
+                break;
+            }
+            const unsigned char *sb = gbase + st * S::STAGE_BYTES;
+            const T2 *Cp = (const T2 *)sb;
+            const T2 *Bp = Cp + S::SLOT;
+            auto at = [&](const T2 *P, int dx, int dy) -> T2 {
+                T2 v = P[(ly + dy) * S::BW + lx + dx];
                 if (MODE == 1) v = c_scale<T>(sig, v);
-            } else {
-                v.x = T(0);
-                v.y = T(0);
+                return v;
+            };
+            const T2 qC = at(Cp, 0, 0), qCxm = at(Cp, -1, 0), qCxp = at(Cp, 1, 0), qCym = at(Cp, 0, -1),
+                     qCyp = at(Cp, 0, 1), qCpp = at(Cp, 1, 1);
+            const T2 qB = at(Bp, 0, 0), qBxm = at(Bp, -1, 0), qBxp = at(Bp, 1, 0), qBym = at(Bp, 0, -1),
+                     qByp = at(Bp, 0, 1), qBmm = at(Bp, -1, -1);
+            T2 n0 = zero2, n1 = zero2;
+            if (MODE == 0 && k >= 2) {
+                const T2 *Np = (const T2 *)(sb + S::NEXT_OFF);
+                n0 = Np[ty * TX + tx];
+                n1 = Np[TX * TY + ty * TX + tx];
             }
-            return v;
-        };
-        auto put = [&](int i, int zz, T2 v) {
-            const int s = i / (PW * PH);
-            const int r = i - s * (PW * PH);
-            const int py = r / PW, pxl = r - py * PW;
-            ring[ring_of(zz)][s][py][pxl] = v;
-        };
+            __syncwarp();
+            if (lane == 0) mbar_arrive(empty + 8 * st);  // this warp is done with stage st
 
-        // Prologue: planes z0-1, z0, z0+1 (z0+1 <= z1 <= nz, the zero plane at most).
-        for (int zz = w.z0 - 1; zz <= w.z0 + 1; zz++)
-            for (int i = tid; i < PLANE; i += NT) put(i, zz, fetch(i, zz));
-        __syncthreads();
+            // sums of plane q = z0-1+k
+            const T2 bBq = c_add<T>(c_add<T>(qBmm, qBym), c_add<T>(qBxm, qB));
+            const T2 bCq = c_add<T>(c_add<T>(qC, qCxp), c_add<T>(qCyp, qCpp));
+            const T2 axyCq = c_add<T>(c_add<T>(qCxm, qCxp), c_add<T>(qCym, qCyp));
+            const T2 axyBq = c_add<T>(c_add<T>(qBxm, qBxp), c_add<T>(qBym, qByp));
+            const T2 sd0q = c_add<T>(bBp, bBq);  // Sd of slot 0 at plane q
 
-        for (int z = w.z0; z < w.z1; z++) {
-            const bool more = (z + 2 <= w.z1);
-            T2 pre[NLD];
-            if (more) {
-#pragma unroll
-                for (int j = 0; j < NLD; j++) {
-                    const int i = tid + j * NT;
-                    if (i < PLANE) pre[j] = fetch(i, z + 2);
-                }
-            }
-            if (valid) {
-                const long long i0 = field_index(d, 0, x, y, z);
-                const long long i1 = i0 + d.plane;
-                T2 n0, n1;
-                if (MODE == 0) {
-                    n0 = next[i0];
-                    n1 = next[i1];
-                }
-                T v0, v1;
-                if (POT == GPE_POTENTIAL_ARRAY) {
-                    v0 = vpot[i0 - d.base + d.vbase];
-                    v1 = vpot[i1 - d.base + d.vbase];
-                } else {
-                    v0 = trap_vdt<T>(vpot, d, 0, x, y, z);
-                    v1 = trap_vdt<T>(vpot, d, 1, x, y, z);
-                }
-                const int rm = ring_of(z - 1), r0 = ring_of(z), rp = ring_of(z + 1);
-                T2 S[2];
-                // slot 0 (cube corner): diagonal -> slot 1 at dz,dy,dx in {-1,0}
-                S[0] = ring[rm][1][ly - 1][lx - 1];
-                S[0] = c_add<T>(S[0], ring[rm][1][ly - 1][lx]);
-                S[0] = c_add<T>(S[0], ring[rm][1][ly][lx - 1]);
-                S[0] = c_add<T>(S[0], ring[rm][1][ly][lx]);
-                S[0] = c_add<T>(S[0], ring[r0][1][ly - 1][lx - 1]);
-                S[0] = c_add<T>(S[0], ring[r0][1][ly - 1][lx]);
-                S[0] = c_add<T>(S[0], ring[r0][1][ly][lx - 1]);
-                S[0] = c_add<T>(S[0], ring[r0][1][ly][lx]);
-                // axial -> slot 0 at (dz,dy,dx) = (-1,0,0),(0,-1,0),(0,0,-1),(0,0,1),(0,1,0),(1,0,0)
-                S[1] = ring[rm][0][ly][lx];
-                S[1] = c_add<T>(S[1], ring[r0][0][ly - 1][lx]);
-                S[1] = c_add<T>(S[1], ring[r0][0][ly][lx - 1]);
-                S[1] = c_add<T>(S[1], ring[r0][0][ly][lx + 1]);
-                S[1] = c_add<T>(S[1], ring[r0][0][ly + 1][lx]);
-                S[1] = c_add<T>(S[1], ring[rp][0][ly][lx]);
-                const T2 p0 = ring[r0][0][ly][lx];
+            if (k >= 2 && valid) {
+                const int z = w.z0 + k - 2;  // output plane (q - 1)
+                T2 S2[2];
                 T hx, hy, nrm;
-                hpsi<T, 2>(p0, S, Lw, L0, v0, gdt, hx, hy, nrm);
-                const T2 o0 = integrate<T, MODE>(n0, p0, hx, hy);
+                T v0, v1;
+                if (POT == GPE_POTENTIAL_TRAP) {
+                    v0 = d_add(vxy0, ztab[z - w.z0]);
+                    v1 = d_add(vxy1, ztab[zl + z - w.z0]);
+                } else {
+                    const long long i0 = col + z * zstride;
+                    v0 = vpot[i0 + voff];
+                    v1 = vpot[i0 + plane + voff];
+                }
+                // slot 0 (cube corner)
+                S2[0] = sd0;
+                S2[1] = c_add<T>(c_add<T>(cm, qC), axyC);
+                hpsi<T, 2>(cc, S2, Lw, L0, v0, gdt, hx, hy, nrm);
+                const T2 o0 = integrate<T, MODE>(n0, cc, hx, hy);
                 if (MODE == 1) {
                     s0.add(nrm);
-                    s1.add(d_fma(p0.x, hx, d_mul(p0.y, hy)));
+                    s1.add(d_fma(cc.x, hx, d_mul(cc.y, hy)));
                     s2.add(d_mul(nrm, nrm));
                     s3.add(d_fma(o0.x, o0.x, d_mul(o0.y, o0.y)));
                 }
-                // slot 1 (cube centre): diagonal -> slot 0 at dz,dy,dx in {0,1}
-                S[0] = ring[r0][0][ly][lx];
-                S[0] = c_add<T>(S[0], ring[r0][0][ly][lx + 1]);
-                S[0] = c_add<T>(S[0], ring[r0][0][ly + 1][lx]);
-                S[0] = c_add<T>(S[0], ring[r0][0][ly + 1][lx + 1]);
-                S[0] = c_add<T>(S[0], ring[rp][0][ly][lx]);
-                S[0] = c_add<T>(S[0], ring[rp][0][ly][lx + 1]);
-                S[0] = c_add<T>(S[0], ring[rp][0][ly + 1][lx]);
-                S[0] = c_add<T>(S[0], ring[rp][0][ly + 1][lx + 1]);
-                S[1] = ring[rm][1][ly][lx];
-                S[1] = c_add<T>(S[1], ring[r0][1][ly - 1][lx]);
-                S[1] = c_add<T>(S[1], ring[r0][1][ly][lx - 1]);
-                S[1] = c_add<T>(S[1], ring[r0][1][ly][lx + 1]);
-                S[1] = c_add<T>(S[1], ring[r0][1][ly + 1][lx]);
-                S[1] = c_add<T>(S[1], ring[rp][1][ly][lx]);
-                const T2 p1 = ring[r0][1][ly][lx];
-                hpsi<T, 2>(p1, S, Lw, L0, v1, gdt, hx, hy, nrm);
-                const T2 o1 = integrate<T, MODE>(n1, p1, hx, hy);
+                // slot 1 (cube centre)
+                S2[0] = c_add<T>(bCc, bCq);
+                S2[1] = c_add<T>(c_add<T>(bm, qB), axyB);
+                hpsi<T, 2>(bc, S2, Lw, L0, v1, gdt, hx, hy, nrm);
+                const T2 o1 = integrate<T, MODE>(n1, bc, hx, hy);
                 if (MODE == 1) {
                     s0.add(nrm);
-                    s1.add(d_fma(p1.x, hx, d_mul(p1.y, hy)));
+                    s1.add(d_fma(bc.x, hx, d_mul(bc.y, hy)));
                     s2.add(d_mul(nrm, nrm));
                     s3.add(d_fma(o1.x, o1.x, d_mul(o1.y, o1.y)));
                 }
-                next[i0] = o0;
-                next[i1] = o1;
+                const long long i0 = col + z * zstride;
+                nxt[i0] = o0;
+                nxt[i0 + plane] = o1;
             }
-            __syncthreads();
-            if (more) {
-#pragma unroll
-                for (int j = 0; j < NLD; j++) {
-                    const int i = tid + j * NT;
-                    if (i < PLANE) put(i, z + 2, pre[j]);
-                }
-            }
-            __syncthreads();
+            cm = cc;
+            cc = qC;
+            bm = bc;
+            bc = qB;
+            axyC = axyCq;
+            axyB = axyBq;
+            bBp = bBq;
+            sd0 = sd0q;
+            bCc = bCq;
         }
-
         if (MODE == 1) {
-            // CTA reduction of the four sums in FP64, fixed shape.
             double v[4] = {s0.value(), s1.value(), s2.value(), s3.value()};
 #pragma unroll
             for (int k = 0; k < 4; k++)
                 for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], off);
             __shared__ double red[NT / 32][4];
-            const int warp = tid >> 5, lane = tid & 31;
             if (lane == 0)
                 for (int k = 0; k < 4; k++) red[warp][k] = v[k];
-            __syncthreads();
+            asm volatile("bar.sync 1, %0;" ::"r"(NT) : "memory");  // consumer warps only
             if (tid < 4) {
                 double t = 0.0;
                 for (int wi = 0; wi < NT / 32; wi++) t += red[wi][tid];
                 a.partials[4ll * it + tid] = t;
             }
-            __syncthreads();
         }
     }
 
     if (MODE == 1) {
-        // Last CTA to finish reduces every instance's rows (fixed order) and
-        // updates its imaginary-time scalars.
+        // Last CTA to finish reduces every instance's rows (fixed order).
         __shared__ bool last;
         __threadfence();
         __syncthreads();
+        if (abort_flag) return;
         if (tid == 0) last = (atomicAdd(a.counter, 1u) == gridDim.x - 1);
         __syncthreads();
         if (!last) return;
         __threadfence();
-        const int warp = tid >> 5, lane = tid & 31;
-        for (int i = warp; i < a.num_instances; i += NT / 32) {
+        for (int i = warp; i < a.num_instances; i += NWARPS) {
             const int b = a.inst_item_begin[2 * i], e = a.inst_item_begin[2 * i + 1];
             double acc[4];
             for (int k = 0; k < 4; k++) {
-                double s = 0.0, c = 0.0;
+                double sk = 0.0, ck = 0.0;
                 for (int r = b + lane; r < e; r += 32) {
-                    const double yv = __ldcg(a.partials + 4ll * r + k) - c;
-                    const double t = s + yv;
-                    c = (t - s) - yv;
-                    s = t;
+                    const double yv = __ldcg(a.partials + 4ll * r + k) - ck;
+                    const double t = sk + yv;
+                    ck = (t - sk) - yv;
+                    sk = t;
                 }
-                for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-                acc[k] = s;
+                for (int off = 16; off > 0; off >>= 1) sk += __shfl_xor_sync(0xffffffffu, sk, off);
+                acc[k] = sk;
             }
             if (lane == 0) {
-                const InstDev &d = a.inst[i];
-                ImagScalars &st = a.imag[i];
+                const InstDev &di = a.inst[i];
+                ImagScalars &sc = a.imag[i];
                 // acc: |p'|^2, Re(conj(p') dt H p'), |p'|^4, |next|^2 over values
-                const double nin = d.vol * acc[0];
-                const double mu = acc[1] / (d.dt * acc[0]);
-                st.norm_in = nin;
-                st.energy = d.vol * (acc[1] / d.dt - 0.5 * d.g * acc[2]);
-                st.mu_prev = st.mu;
-                st.mu = mu;
-                st.dmu = (st.steps > 0) ? fabs(mu - st.mu_prev) : INFINITY;
-                if (st.steps > 0 && st.conv_step < 0 && st.dmu < a.tol) st.conv_step = st.steps;
-                st.steps += 1;
-                st.sigma = 1.0 / sqrt(d.vol * acc[3]);
+                const double nin = di.vol * acc[0];
+                const double mu = acc[1] / (di.dt * acc[0]);
+                sc.norm_in = nin;
+                sc.energy = di.vol * (acc[1] / di.dt - 0.5 * di.g * acc[2]);
+                sc.mu_prev = sc.mu;
+                sc.mu = mu;
+                sc.dmu = (sc.steps > 0) ? fabs(mu - sc.mu_prev) : INFINITY;
+                if (sc.steps > 0 && sc.conv_step < 0 && sc.dmu < a.tol) sc.conv_step = sc.steps;
+                sc.steps += 1;
+                sc.sigma = 1.0 / sqrt(di.vol * acc[3]);
             }
         }
         if (tid == 0) *a.counter = 0u;
     }
 }
 
-// Tile variants (TX, TY).  Index 0 is the default.
-static const int kTiles[][2] = {{32, 8}, {32, 4}, {16, 16}, {16, 8}, {64, 4}, {8, 32}};
+// Kernel variants: tile (TX, TY), pipeline depth (STAGES planes) and the
+// minimum resident CTAs per SM asked of the register allocator (MINB).  Index 0
+// is the default; the autotuner picks among them per workload.
+struct Variant {
+    int tx, ty, stages, minb;
+};
+static const Variant kVariants[] = {
+    {32, 4, 6, 6}, {32, 4, 4, 6}, {32, 8, 4, 3}, {32, 8, 6, 3}, {32, 4, 8, 5}, {64, 4, 4, 3},
+    {16, 8, 6, 6}, {32, 2, 8, 8}, {16, 16, 4, 3}, {32, 8, 4, 2}, {64, 4, 6, 2}, {32, 16, 4, 1},
+};
 
-int fused_tile_count() { return int(sizeof(kTiles) / sizeof(kTiles[0])); }
+int fused_tile_count() { return int(sizeof(kVariants) / sizeof(kVariants[0])); }
 void fused_tile_shape(int tile, int *tx, int *ty)
 {
     if (tile < 0 || tile >= fused_tile_count()) tile = 0;
-    *tx = kTiles[tile][0];
-    *ty = kTiles[tile][1];
+    *tx = kVariants[tile].tx;
+    *ty = kVariants[tile].ty;
 }
 
-template <typename T, int TX, int TY>
+int fused_box_bytes(int precision, int tile)
+{
+    int tx, ty;
+    fused_tile_shape(tile, &tx, &ty);
+    const int c = precision == GPE_FP64 ? 16 : 8;
+    return (tx + 4) * (ty + 2) * 2 * c;
+}
+
+// The two 4-D tensor maps of one field of one instance (out_map[0], out_map[1]):
+// dimensions (x in 8-byte elements, y, slot, z) over the padded layout; boxes =
+// tile plus a 2-column / 1-row halo (previous-field loads) and the interior tile
+// (next-field loads), both slots, one plane.  The padded layout puts the
+// Dirichlet zeros in memory; boxes that overhang the padded extents are
+// zero-filled by the TMA unit.
+gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *field_arena, int tile)
+{
+    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static Encode encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+            return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        encode = (Encode)fn;
+    }
+    int tx, ty;
+    fused_tile_shape(tile, &tx, &ty);
+    const int csize = precision == GPE_FP64 ? 16 : 8;
+    const int xe = csize / 8;
+    const cuuint64_t dims[4] = {(cuuint64_t)d.px * xe, (cuuint64_t)d.py, 2, (cuuint64_t)d.nz + 2};
+    const cuuint64_t strides[3] = {(cuuint64_t)d.px * csize, (cuuint64_t)d.plane * csize,
+                                   (cuuint64_t)d.zstride * csize};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    void *gaddr = (char *)field_arena + (size_t)d.base * csize;
+    // [0]: tile plus halo, both slots, one plane; [1]: interior tile, both slots, one plane
+    const cuuint32_t boxes[2][4] = {{(cuuint32_t)(tx + 4) * xe, (cuuint32_t)(ty + 2), 2, 1},
+                                    {(cuuint32_t)tx * xe, (cuuint32_t)ty, 2, 1}};
+    for (int b = 0; b < 2; b++) {
+        CUresult r = encode((CUtensorMap *)out_map + b, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, gaddr, dims, strides,
+                            boxes[b], estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    }
+    return GPE_OK;
+}
+
+template <typename T, int TX, int TY, int ST, int MB, int MODE, int POT>
+static cudaError_t launch_one(const FusedArgs &a, int grid, cudaStream_t s)
+{
+    const int bytes = fused_smem_bytes<T, TX, TY, ST>(a.zcmax);
+    auto kern = fused_bcc2_kernel<T, TX, TY, MODE, POT, ST, MB>;
+    static int allowed = 48 * 1024;  // dynamic shared memory granted to this instantiation
+    if (bytes > allowed) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        allowed = bytes;
+    }
+    kern<<<grid, FusedShape<T, TX, TY>::NTHREADS, bytes, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T, int TX, int TY, int ST, int MB>
 static cudaError_t fused_launch_t(const FusedLaunch &l, const FusedArgs &a, cudaStream_t s)
 {
-    const int g = l.grid;
     if (l.mode == GPE_REAL_TIME) {
-        if (l.potential == GPE_POTENTIAL_ARRAY) fused_bcc2_kernel<T, TX, TY, 0, 0><<<g, TX * TY, 0, s>>>(a);
-        else fused_bcc2_kernel<T, TX, TY, 0, 1><<<g, TX * TY, 0, s>>>(a);
-    } else {
-        if (l.potential == GPE_POTENTIAL_ARRAY) fused_bcc2_kernel<T, TX, TY, 1, 0><<<g, TX * TY, 0, s>>>(a);
-        else fused_bcc2_kernel<T, TX, TY, 1, 1><<<g, TX * TY, 0, s>>>(a);
+        if (l.potential == GPE_POTENTIAL_ARRAY) return launch_one<T, TX, TY, ST, MB, 0, 0>(a, l.grid, s);
+        return launch_one<T, TX, TY, ST, MB, 0, 1>(a, l.grid, s);
     }
-    return cudaGetLastError();
+    if (l.potential == GPE_POTENTIAL_ARRAY) return launch_one<T, TX, TY, ST, MB, 1, 0>(a, l.grid, s);
+    return launch_one<T, TX, TY, ST, MB, 1, 1>(a, l.grid, s);
 }
 
 template <typename T>
 static cudaError_t fused_launch_tile(const FusedLaunch &l, const FusedArgs &a, cudaStream_t s)
 {
-    switch (l.tile) {
-    case 1: return fused_launch_t<T, 32, 4>(l, a, s);
-    case 2: return fused_launch_t<T, 16, 16>(l, a, s);
-    case 3: return fused_launch_t<T, 16, 8>(l, a, s);
-    case 4: return fused_launch_t<T, 64, 4>(l, a, s);
-    case 5: return fused_launch_t<T, 8, 32>(l, a, s);
-    default: return fused_launch_t<T, 32, 8>(l, a, s);
+    switch (l.tile) {  // must list kVariants in order
+    case 1: return fused_launch_t<T, 32, 4, 4, 6>(l, a, s);
+    case 2: return fused_launch_t<T, 32, 8, 4, 3>(l, a, s);
+    case 3: return fused_launch_t<T, 32, 8, 6, 3>(l, a, s);
+    case 4: return fused_launch_t<T, 32, 4, 8, 5>(l, a, s);
+    case 5: return fused_launch_t<T, 64, 4, 4, 3>(l, a, s);
+    case 6: return fused_launch_t<T, 16, 8, 6, 6>(l, a, s);
+    case 7: return fused_launch_t<T, 32, 2, 8, 8>(l, a, s);
+    case 8: return fused_launch_t<T, 16, 16, 4, 3>(l, a, s);
+    case 9: return fused_launch_t<T, 32, 8, 4, 2>(l, a, s);
+    case 10: return fused_launch_t<T, 64, 4, 6, 2>(l, a, s);
+    case 11: return fused_launch_t<T, 32, 16, 4, 1>(l, a, s);
+    default: return fused_launch_t<T, 32, 4, 6, 6>(l, a, s);
     }
 }
 
@@ -314,6 +536,9 @@ cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s)
     a.inst = l.inst;
     a.items = l.items;
     a.num_items = l.num_items;
+    a.maps = (const CUtensorMap *)l.maps;
+    a.zcmax = l.zcmax;
+    a.src = l.src;
     a.prev = l.prev;
     a.next = l.next;
     a.vpot = l.vpot;
@@ -323,6 +548,7 @@ cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s)
     a.inst_item_begin = l.inst_item_begin;
     a.num_instances = l.num_instances;
     a.tol = l.tol;
+    a.err = l.err;
     if (l.precision == GPE_FP64) return fused_launch_tile<double>(l, a, s);
     return fused_launch_tile<float>(l, a, s);
 }

@@ -45,6 +45,10 @@ cudaError_t launch_plain_step(const StepLaunch &l, cudaStream_t s);
 
 struct FusedLaunch {
     int precision, mode, potential, tile;
+    const void *maps;     // CUtensorMap[num_instances][2 fields][2 boxes] in device memory
+    int zcmax;            // longest z-range of a work item
+    int src;              // field index of prev (0 or 1)
+    int *err;             // device error word (bounded-wait timeouts)
     const InstDev *inst;
     const WorkItem *items;
     int num_items;
@@ -63,6 +67,11 @@ struct FusedLaunch {
 cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s);
 int fused_tile_count();
 void fused_tile_shape(int tile, int *tx, int *ty);
+// Bytes of one TMA box (tile plus halo, both slots) of the fused kernel.
+int fused_box_bytes(int precision, int tile);
+// Encodes the fused kernel's two 4-D tensor maps (halo box, interior box) of
+// one field of one instance into out_map[0..1].
+gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *field_arena, int tile);
 
 struct ObsLaunch {
     int lattice, precision, potential;

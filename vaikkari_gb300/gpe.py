@@ -61,6 +61,7 @@ class Status(enum.IntEnum):
     UNSUPPORTED = 5
     TOO_LARGE = 6
     INTERNAL = 7
+    TIMEOUT = 8
 
 
 class GpeError(RuntimeError):
