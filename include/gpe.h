@@ -190,6 +190,30 @@ int64_t gpe_launch_count(gpe_handle h);
  * work or record CUDA events against the library's launches. */
 void *gpe_stream(gpe_handle h);
 
+/* Observables without allocating.  No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc - programs whose device memory is all
+ * handed out by their own pool, or latency-critical code where an allocation
+ * (which may synchronise the device) is not allowed.  It needs no handle.
+ *
+ * field: caller-owned device memory, the condensate's complex values in block
+ * order (element type by `precision`); potential: caller-owned device memory, V
+ * per value (unscaled, same order and type), or NULL for the harmonic trap in
+ * `inst->trap`.  Runs on `stream` (a cudaStream_t; NULL = default stream) on the
+ * current device, waits for it, and fills `out` (host memory).
+ *
+ * Scratch memory is one array of GPE_NOALLOC_MAX_ROWS partial-sum rows held by
+ * every GPU that loads the library; each row covers GPE_NOALLOC_VALUES_PER_ROW
+ * values, so inputs of more than 16,777,216 values return GPE_ERR_TOO_LARGE.
+ * All calls share that array: calls that overlap on a GPU race and must be
+ * serialised by the caller.  The first call on a device looks the array up and
+ * should come before any stream capture.  It allocates nothing when it
+ * succeeds; a failure records its message for gpe_last_error() as every call does. */
+#define GPE_NOALLOC_MAX_ROWS 8192
+#define GPE_NOALLOC_VALUES_PER_ROW 2048
+gpe_status gpe_observables_noalloc(int32_t lattice, int32_t precision, const gpe_instance *inst,
+                                   const void *field, const void *potential, void *stream,
+                                   gpe_observables *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -140,6 +140,9 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_launch_count.argtypes = [C.c_void_p]
     lib.gpe_stream.restype = C.c_void_p
     lib.gpe_stream.argtypes = [C.c_void_p]
+    lib.gpe_observables_noalloc.restype = st
+    lib.gpe_observables_noalloc.argtypes = [C.c_int32, C.c_int32, C.POINTER(_Instance), C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.POINTER(_Observables)]
     _lib = lib
     return lib
 
@@ -165,6 +168,23 @@ def lattice_info(lattice: Lattice) -> dict:
         "position": np.array([list(info.position[s]) for s in range(ns)]),
         "entry": entry,
     }
+
+
+def observables_noalloc(lattice: Lattice, precision: Precision, inst: "Instance", field_ptr: int,
+                        potential_ptr: int = 0, stream: int = 0) -> dict:
+    """Observables of one condensate that already sits in device memory, without
+    any allocation (gpe_observables_noalloc).  For callers that cannot allocate
+    device memory: field_ptr / potential_ptr are device addresses of the
+    condensate's values and potential in block order; potential_ptr = 0 uses the
+    instance's harmonic trap.  Calls that overlap on one GPU share scratch memory
+    and must not run concurrently."""
+    lib = load_library()
+    out = _Observables()
+    c = inst.c()
+    _check(lib.gpe_observables_noalloc(int(lattice), int(precision), C.byref(c), C.c_void_p(field_ptr),
+                                       C.c_void_p(potential_ptr or None), C.c_void_p(stream or None), C.byref(out)),
+           "gpe_observables_noalloc")
+    return {k: getattr(out, k) for k in ("norm", "energy", "mu", "kinetic", "potential", "interaction")}
 
 
 @dataclass
