@@ -254,8 +254,14 @@ def run_ours(args):
     conds = build_batch()
     insts = [c.inst for c in conds]
     verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
+    tile, zchunk, tuned = args.tile, args.zchunk, None
+    if tile < 0:
+        # untimed: pick the kernel variant and z-chunk for this batch (cached per device)
+        from vaikkari_gb300.autotune import autotune
+        tuned = autotune(insts, precision=Precision.FP32, potential=Potential.TRAP, device=local)
+        tile, zchunk = tuned["tile"], tuned["zchunk"]
     st = Stepper(insts, lattice=Lattice.BCC2, precision=Precision.FP32, kernel=Kernel.FUSED,
-                 potential=Potential.TRAP, graph_steps=100, tile=args.tile, zchunk=args.zchunk, device=local)
+                 potential=Potential.TRAP, graph_steps=100, tile=tile, zchunk=zchunk, device=local)
     evens, odds = prepare_fields(st, conds, np.float32)
 
     # Warm-up: W steps, plus one replay of the 100-step graph so that the
@@ -341,7 +347,8 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batch64_bcc2_fp32_trap_realtime", "instances": len(insts),
                        "vertices": verts, "sizes": sorted({i.nx for i in insts}), "dt": 1e-4,
-                       "graph_steps": 100, "kernel": "fused", "tile": args.tile,
+                       "graph_steps": 100, "kernel": "fused", "variant": tile, "zchunk": zchunk,
+                       "autotuned": tuned is not None,
                        "parallelism": f"replicas{ws}" if ws > 1 else "single",
                        "l2": f"inputs larger than L2 (fields {2 * 8 * verts / 1e6:.0f} MB vs {L2_BYTES / 1e6:.0f} MB)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -425,7 +432,7 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--tile", type=int, default=-1, help="kernel variant; -1 = autotune")
     ap.add_argument("--zchunk", type=int, default=0)
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--fp64-steps", type=int, default=200)

@@ -183,6 +183,18 @@ gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out
 gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64_t *steps_done,
                               int32_t *converged, double *mu_out);
 
+/* Runs gpe_step(h, steps) between two CUDA events recorded on the handle's
+ * stream and returns the elapsed device time in milliseconds (the profiling
+ * hook the autotuner and benchmarks use; the reference times with clock(),
+ * GPUGrossPitaevskii_BCC.cu:421,488). */
+gpe_status gpe_time_steps(gpe_handle h, int64_t steps, float *ms);
+
+/* Number of fused-kernel variants (tile shape, pipeline depth, register cap)
+ * that gpe_config.tile may select, and the tile shape of one of them. */
+int32_t gpe_variant_count(void);
+gpe_status gpe_variant_describe(int32_t variant, int32_t *tile_x, int32_t *tile_y, int32_t *stages,
+                                int32_t *min_blocks);
+
 /* Kernel launches the handle has issued (for accounting). */
 int64_t gpe_launch_count(gpe_handle h);
 

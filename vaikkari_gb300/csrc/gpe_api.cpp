@@ -847,6 +847,46 @@ gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64
     return GPE_OK;
 }
 
+gpe_status gpe_time_steps(gpe_handle h, int64_t steps, float *ms)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (!ms || steps < 0) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_time_steps: bad arguments");
+    cudaEvent_t a = nullptr, b = nullptr;
+    GPE_CUDA_TRY(cudaEventCreate(&a));
+    cudaError_t e = cudaEventCreate(&b);
+    if (e != cudaSuccess) {
+        cudaEventDestroy(a);
+        return cuda_fail(e, "cudaEventCreate");
+    }
+    e = cudaEventRecord(a, h->stream);
+    if (e == cudaSuccess) st = gpe_step(h, steps);
+    if (e == cudaSuccess && st == GPE_OK) e = cudaEventRecord(b, h->stream);
+    if (e == cudaSuccess && st == GPE_OK) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess && st == GPE_OK) e = cudaEventElapsedTime(ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (st != GPE_OK) return st;
+    if (e != cudaSuccess) return cuda_fail(e, "gpe_time_steps");
+    return sync_and_check(h);
+}
+
+int32_t gpe_variant_count(void) { return fused_tile_count(); }
+
+gpe_status gpe_variant_describe(int32_t variant, int32_t *tile_x, int32_t *tile_y, int32_t *stages,
+                                int32_t *min_blocks)
+{
+    if (variant < 0 || variant >= fused_tile_count())
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_variant_describe: no such variant");
+    int tx, ty, stg, mb;
+    fused_variant(variant, &tx, &ty, &stg, &mb);
+    if (tile_x) *tile_x = tx;
+    if (tile_y) *tile_y = ty;
+    if (stages) *stages = stg;
+    if (min_blocks) *min_blocks = mb;
+    return GPE_OK;
+}
+
 int64_t gpe_launch_count(gpe_handle h) { return h ? h->launches : 0; }
 
 void *gpe_stream(gpe_handle h) { return h ? (void *)h->stream : nullptr; }

@@ -435,6 +435,15 @@ void fused_tile_shape(int tile, int *tx, int *ty)
     *ty = kVariants[tile].ty;
 }
 
+void fused_variant(int tile, int *tx, int *ty, int *stages, int *minb)
+{
+    if (tile < 0 || tile >= fused_tile_count()) tile = 0;
+    *tx = kVariants[tile].tx;
+    *ty = kVariants[tile].ty;
+    *stages = kVariants[tile].stages;
+    *minb = kVariants[tile].minb;
+}
+
 int fused_box_bytes(int precision, int tile)
 {
     int tx, ty;

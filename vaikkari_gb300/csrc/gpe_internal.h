@@ -67,6 +67,7 @@ struct FusedLaunch {
 cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s);
 int fused_tile_count();
 void fused_tile_shape(int tile, int *tx, int *ty);
+void fused_variant(int tile, int *tx, int *ty, int *stages, int *minb);
 // Bytes of one TMA box (tile plus halo, both slots) of the fused kernel.
 int fused_box_bytes(int precision, int tile);
 // Encodes the fused kernel's two 4-D tensor maps (halo box, interior box) of

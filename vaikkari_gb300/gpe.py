@@ -140,6 +140,11 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_launch_count.argtypes = [C.c_void_p]
     lib.gpe_stream.restype = C.c_void_p
     lib.gpe_stream.argtypes = [C.c_void_p]
+    lib.gpe_time_steps.restype = st
+    lib.gpe_time_steps.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]
+    lib.gpe_variant_count.restype = C.c_int32
+    lib.gpe_variant_describe.restype = st
+    lib.gpe_variant_describe.argtypes = [C.c_int32] + [C.POINTER(C.c_int32)] * 4
     lib.gpe_observables_noalloc.restype = st
     lib.gpe_observables_noalloc.argtypes = [C.c_int32, C.c_int32, C.POINTER(_Instance), C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.POINTER(_Observables)]
@@ -185,6 +190,17 @@ def observables_noalloc(lattice: Lattice, precision: Precision, inst: "Instance"
                                        C.c_void_p(potential_ptr or None), C.c_void_p(stream or None), C.byref(out)),
            "gpe_observables_noalloc")
     return {k: getattr(out, k) for k in ("norm", "energy", "mu", "kinetic", "potential", "interaction")}
+
+
+def variants() -> List[dict]:
+    """The fused kernel's variants (gpe_config.tile values)."""
+    lib = load_library()
+    out = []
+    for v in range(lib.gpe_variant_count()):
+        t = [C.c_int32() for _ in range(4)]
+        _check(lib.gpe_variant_describe(v, *[C.byref(x) for x in t]), "gpe_variant_describe")
+        out.append({"tile": v, "tx": t[0].value, "ty": t[1].value, "stages": t[2].value, "min_blocks": t[3].value})
+    return out
 
 
 @dataclass
@@ -314,6 +330,13 @@ class Stepper:
         _check(self.lib.gpe_imaginary_time(self.h, int(max_steps), float(tol), C.byref(steps), C.byref(conv), mu),
                "gpe_imaginary_time")
         return steps.value, bool(conv.value), list(mu)
+
+    def time_steps(self, steps: int) -> float:
+        """Device milliseconds of `steps` steps, timed with CUDA events on the
+        library's stream (gpe_time_steps)."""
+        ms = C.c_float()
+        _check(self.lib.gpe_time_steps(self.h, int(steps), C.byref(ms)), "gpe_time_steps")
+        return float(ms.value)
 
     def launch_count(self) -> int:
         return int(self.lib.gpe_launch_count(self.h))
