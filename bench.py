@@ -426,6 +426,169 @@ def fp64_plain_rate(conds, insts, device, steps):
             "note": "each instance advanced alone (one launch per instance per half-step)"}
 
 
+# ---------------------------------------------------------------------------
+# The other configurations: parity and accuracy cases (not the headline line).
+
+def _stepper(conds, prec, kernel, mode, tile=0, graph_steps=100, device=0):
+    from vaikkari_gb300.gpe import Lattice, Potential, Stepper
+    return Stepper([c.inst for c in conds], lattice=Lattice.BCC2, precision=prec, kernel=kernel, mode=mode,
+                   potential=Potential.TRAP, graph_steps=graph_steps, tile=tile, device=device)
+
+
+def _rel_l2(a, b):
+    num = sum(float(np.sum((x.astype(np.float64) - y.astype(np.float64)) ** 2)) for x, y in zip(a, b))
+    den = sum(float(np.sum(y.astype(np.float64) ** 2)) for y in b)
+    return math.sqrt(num / den)
+
+
+def _rel_l2_phase(a, b):
+    """Relative L2 after aligning the global phase of a to b (ground states are
+    defined up to a constant phase)."""
+    num = den = 0.0
+    for x, y in zip(a, b):
+        xc = x[..., 0].astype(np.float64) + 1j * x[..., 1].astype(np.float64)
+        yc = y[..., 0].astype(np.float64) + 1j * y[..., 1].astype(np.float64)
+        ov = np.vdot(xc, yc)
+        xc = xc * (ov / abs(ov) if abs(ov) > 0 else 1.0)
+        num += float(np.sum(np.abs(xc - yc) ** 2))
+        den += float(np.sum(np.abs(yc) ** 2))
+    return math.sqrt(num / den)
+
+
+def _download(st, n):
+    return [st.download(i, odd=False)[0] for i in range(n)]
+
+
+def _cpu_config_rate(conds, steps):
+    """FP64 oracle port, all host threads, `steps` leapfrog steps of every condensate."""
+    e64 = [np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1)) for c in conds]
+    v, n, el, nv = cpu_sample(conds, e64, [a.copy() for a in e64], 0.0, os.cpu_count() or 1)
+    return {"value": v, "unit": METRIC, "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"{n} leapfrog step(s), {nv} vertices, FP64 oracle port, {el:.2f} s"}
+
+
+def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1):
+    """FP32 fused against FP64 fused of the same scheme at each checkpoint, plus
+    throughput of the FP32 fused and FP64 plain paths."""
+    from vaikkari_gb300.gpe import Kernel, Mode, Precision
+    insts = [c.inst for c in conds]
+    verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
+    if tile < 0:
+        from vaikkari_gb300.autotune import autotune
+        tile = autotune(insts)["tile"]
+    fp64_last = fp64_steps or checkpoints[-1]
+    runs = {}
+    for prec, dt_, last in ((Precision.FP64, np.float64, fp64_last), (Precision.FP32, np.float32, checkpoints[-1])):
+        st = _stepper(conds, prec, Kernel.FUSED, Mode.REAL, tile=tile)
+        prepare_fields(st, conds, dt_)
+        o0 = st.observables(0)
+        done, cps = 0, {}
+        for cp in checkpoints:
+            if cp > last:
+                break
+            st.step(cp - done)
+            done = cp
+            cps[cp] = (st.observables(0), _download(st, len(insts)))
+        runs[prec] = (o0, cps)
+        st.close()
+    acc = []
+    o64_0 = runs[Precision.FP64][0]
+    for cp, (o32, f32) in runs[Precision.FP32][1].items():
+        row = {"step": cp,
+               "norm_fp32": [o["norm"] for o in o32], "energy_fp32": [o["energy"] for o in o32],
+               "norm_drift_fp32_vs_initial": max(abs(a["norm"] - b["norm"]) / b["norm"] for a, b in zip(o32, o64_0))}
+        if cp in runs[Precision.FP64][1]:
+            o64, f64 = runs[Precision.FP64][1][cp]
+            row["rel_l2_fp32_vs_fp64"] = _rel_l2(f32, f64)
+            row["norm_drift_fp32_vs_fp64"] = max(abs(a["norm"] - b["norm"]) / b["norm"] for a, b in zip(o32, o64))
+            row["energy_drift_fp32_vs_fp64"] = max(abs(a["energy"] - b["energy"]) / abs(b["energy"])
+                                                   for a, b in zip(o32, o64))
+            row["norm_drift_fp64_vs_initial"] = max(abs(a["norm"] - b["norm"]) / b["norm"] for a, b in zip(o64, o64_0))
+            row["energy_fp64"] = [o["energy"] for o in o64]
+        acc.append(row)
+    # throughput: FP32 fused and FP64 plain, device time of 200 steps after warm-up
+    rates = {}
+    for key, prec, kern in (("fp32_fused", Precision.FP32, Kernel.FUSED), ("fp64_fused", Precision.FP64, Kernel.FUSED),
+                            ("fp64_plain", Precision.FP64, Kernel.PLAIN)):
+        st = _stepper(conds, prec, kern, Mode.REAL, tile=tile)
+        prepare_fields(st, conds, np.float64 if prec == Precision.FP64 else np.float32)
+        st.time_steps(103)
+        ms = min(st.time_steps(200) for _ in range(2))
+        rates[key] = verts * 200 / (ms * 1e-3)
+        st.close()
+    cpu_steps = 2 if verts > 1e7 else (20 if verts > 1e6 else 200)
+    return {"metric": METRIC, "value": rates["fp32_fused"], "unit": METRIC, "dtype": "f32",
+            "config": {"workload": name, "instances": len(insts), "vertices": verts, "dt": insts[0].dt,
+                       "variant": tile},
+            "rates": rates, "accuracy": acc, "cpu_baseline": _cpu_config_rate(conds, cpu_steps)}
+
+
+def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1):
+    from vaikkari_gb300.gpe import Kernel, Mode, Precision
+    insts = [c.inst for c in conds]
+    verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
+    if tile < 0:
+        tile = 0
+    res = {}
+    steps64 = None
+    for prec in (Precision.FP64, Precision.FP32):
+        st = _stepper(conds, prec, Kernel.FUSED, Mode.IMAGINARY, tile=tile)
+        for i, c in enumerate(conds):
+            st.upload(i, c.psi)
+        t0 = time.perf_counter()
+        # FP64 runs to the criterion.  The FP32 field stops changing once the
+        # per-step update drops below its rounding, which freezes mu and trips a
+        # 1e-9 criterion spuriously, so FP32 runs the same number of steps.
+        lim, crit = (max_steps, tol) if prec == Precision.FP64 else (steps64, 0.0)
+        steps, conv, mu = st.imaginary_time(lim, crit)
+        st.synchronize()
+        wall = time.perf_counter() - t0
+        obs = st.observables(0)
+        fields = _download(st, len(insts))
+        if prec == Precision.FP64:
+            steps64 = steps
+        st.close()
+        res[prec] = {"steps": steps, "converged": conv, "mu": mu, "energy": [o["energy"] for o in obs],
+                     "mu_obs": [o["mu"] for o in obs], "fields": fields, "wall_s": wall}
+    r64, r32 = res[Precision.FP64], res[Precision.FP32]
+    acc = {"steps_fp64": r64["steps"], "converged_fp64": r64["converged"], "steps_fp32": r32["steps"],
+           "converged_fp32": r32["converged"], "mu_fp64": r64["mu_obs"], "mu_fp32": r32["mu_obs"],
+           "rel_mu_fp32_vs_fp64": max(abs(a - b) / abs(b) for a, b in zip(r32["mu_obs"], r64["mu_obs"])),
+           "rel_energy_fp32_vs_fp64": max(abs(a - b) / abs(b) for a, b in zip(r32["energy"], r64["energy"])),
+           "rel_l2_fp32_vs_fp64": _rel_l2_phase(r32["fields"], r64["fields"])}
+    # throughput of the fused imaginary-time step (FP32), device time
+    st = _stepper(conds, Precision.FP32, Kernel.FUSED, Mode.IMAGINARY, tile=tile)
+    for i, c in enumerate(conds):
+        st.upload(i, c.psi)
+    st.time_steps(100)
+    ms = min(st.time_steps(1000) for _ in range(2))
+    st.close()
+    return {"metric": METRIC, "value": verts * 1000 / (ms * 1e-3), "unit": METRIC, "dtype": "f32",
+            "config": {"workload": name, "instances": len(insts), "vertices": verts, "dt": insts[0].dt,
+                       "tol": tol, "mode": "imaginary"},
+            "accuracy": acc, "cpu_baseline": None}
+
+
+def run_workload(args):
+    from vaikkari_gb300 import workloads
+    name = args.workload
+    if name == "config1":
+        line = run_config_realtime("config1_bcc2_32_realtime_1000", [workloads.config1()], [1000], tile=args.tile)
+    elif name == "config2":
+        line = run_config_imaginary("config2_bcc2_128_imaginary", [workloads.config2()], tile=args.tile)
+    elif name == "config3":
+        line = run_config_realtime("config3_bcc2_192_vortex_ring", [workloads.config3()], [1000, 5000, 10000],
+                                   tile=args.tile)
+    elif name == "config5":
+        line = run_config_realtime("config5_bcc2_512_realtime", [workloads.config5()], [200, 2000], fp64_steps=200,
+                                   tile=args.tile)
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    line["n_gpus"] = 1
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -439,11 +602,15 @@ def main():
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--workload", default="batch64",
+                    help="batch64 (the headline) or config1/config2/config3/config5 (accuracy cases)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "batch64":
+        return run_workload(args)
     return run_ours(args)
 
 
