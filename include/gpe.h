@@ -202,6 +202,66 @@ int64_t gpe_launch_count(gpe_handle h);
  * work or record CUDA events against the library's launches. */
 void *gpe_stream(gpe_handle h);
 
+/* ---- The reference's solver call, end to end ---------------------------------
+ * A vortex state file (the reference's VortexState binary format,
+ * koodit/GrossPitaevskii/VortexState.cpp:49-96) and integrateInTime's own
+ * set-up (GPUGrossPitaevskii_BCC.cu:222-348: grid from the domain and block_scale,
+ * psi sampled at the circumcentres, potentialV3, dt from the stability bound,
+ * MT19937 noise, odd field rotated by half a step) reproduced bit for bit on the
+ * host, then stepped on the GPU with the TETRA12 lattice. */
+typedef struct gpe_vortex_ *gpe_vortex;
+
+typedef struct gpe_vortex_info {
+    uint32_t kappa, rsize, zsize, pad_;
+    double g, mu, rplug, rstep, zstep;
+    double function_max;   /* searchFunctionMax (VortexState.cpp:240-248)            */
+    double max_r, max_z;   /* searchMaxR/MaxZ at eps = eps_fraction * function_max    */
+    double curvature;      /* integrateCurvature (:313-340)                           */
+    double block_scale;    /* 2 pi / (20 sqrt(curvature)), main() :539               */
+} gpe_vortex_info;
+
+typedef struct gpe_integrate_desc {
+    double block_scale;
+    double minp[3], maxp[3];  /* domain, e.g. (-maxr,-maxr,-maxz) .. (maxr,maxr,maxz)      */
+    double iteration_period;  /* time per iteration (1.0 in the reference)              */
+    uint32_t number_of_iterations;
+    uint32_t seed;            /* noise stream seed (54363 in the reference)             */
+    double ratio;             /* potentialV3's RATIO (0.1 in the reference)             */
+    double noise;             /* noise amplitude (0.01 in the reference)                */
+    int32_t precision;        /* GPE_FP64 reproduces the reference; GPE_FP32 is faster   */
+    int32_t device;
+} gpe_integrate_desc;
+
+typedef struct gpe_integrate_result {
+    uint32_t xsize, ysize, zsize, steps_per_iteration;
+    uint64_t values;          /* 12 * xsize * ysize * zsize                             */
+    double p0[3];             /* position of block (0,0,0)                              */
+    double maxpot, dt, lapfac_dt, lapfac0_dt, g_dt;
+    double odd_phase[2];
+    double device_ms;         /* device time of all steps (gpe_integrate_in_time)       */
+} gpe_integrate_result;
+
+/* VortexState::load (VortexState.cpp:49-72). */
+gpe_status gpe_vortex_load(const char *path, gpe_vortex *out);
+void gpe_vortex_free(gpe_vortex v);
+/* The diagnostics main() prints (GPUGrossPitaevskii_BCC.cu:503-548); main()
+ * uses eps_fraction = 1e-5. */
+gpe_status gpe_vortex_describe(gpe_vortex v, double eps_fraction, gpe_vortex_info *out);
+/* VortexState::getPsi at p[3] (VortexState.cpp:204-212); out = (re, im). */
+gpe_status gpe_vortex_psi(gpe_vortex v, const double *p, double *out);
+/* The host set-up of integrateInTime (GPUGrossPitaevskii_BCC.cu:222-348).  Fills
+ * `res`; when non-null, even/odd (complex, block order, 2*values doubles) and
+ * potential (V unscaled, values doubles). */
+gpe_status gpe_integrate_setup(gpe_vortex v, const gpe_integrate_desc *d, gpe_integrate_result *res,
+                               double *even, double *odd, double *potential);
+/* integrateInTime (GPUGrossPitaevskii_BCC.cu:218-499): set-up, then
+ * number_of_iterations iterations of steps_per_iteration leapfrog steps on the
+ * GPU.  per_iteration (may be NULL) receives number_of_iterations+1 observables
+ * of the even field, before each iteration and after the last; even_out/odd_out
+ * (may be NULL) the final fields. */
+gpe_status gpe_integrate_in_time(gpe_vortex v, const gpe_integrate_desc *d, gpe_integrate_result *res,
+                                 gpe_observables *per_iteration, double *even_out, double *odd_out);
+
 /* Observables without allocating.  No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc - programs whose device memory is all
  * handed out by their own pool, or latency-critical code where an allocation

@@ -258,14 +258,31 @@ static void run_setup(const char *state_path, double block_scale, const char *ou
     std::printf("  \"layout\": \"float64; even[z][y][x][slot][re,im], then odd (same), then pot*dt[z][y][x][slot]\"\n}\n");
 }
 
+// A small vortex state made by the reference's own axisymmetric relaxation
+// (VortexState::setRange + iterateSolution, VortexState.cpp:42-47,109-196; the
+// potential is the reference's potentialRZ, GPUGrossPitaevskii_BCC.cu:28-31).
+extern ddouble potentialRZ(const ddouble r, const ddouble z);
+static void make_state(const char *out, uint kappa, double g, double rstep, uint iters)
+{
+    VortexState state;
+    state.setKappa(kappa);
+    state.setG(g);
+    state.setRange(0.0, 15.0, 35.0, rstep, rstep);
+    state.iterateSolution(potentialRZ, iters, 1e-29);
+    if (!state.save(out)) { std::fprintf(stderr, "cannot write %s\n", out); std::exit(2); }
+    std::printf("{\"kappa\": %u, \"g\": %.17g, \"mu\": %.17g, \"rstep\": %.17g, \"iterations\": %u}\n", kappa, g,
+                state.getMu(), rstep, iters);
+}
+
 int main(int argc, char **argv)
 {
-    if (argc < 2) { std::fprintf(stderr, "usage: %s tables|mesh|vortex STATE|setup STATE BS OUT\n", argv[0]); return 2; }
+    if (argc < 2) { std::fprintf(stderr, "usage: %s tables|mesh|vortex STATE|setup STATE BS OUT|makestate OUT\n", argv[0]); return 2; }
     const std::string cmd = argv[1];
     if (cmd == "tables") print_tables();
     else if (cmd == "mesh") print_mesh();
     else if (cmd == "vortex" && argc >= 3) print_vortex(argv[2]);
     else if (cmd == "setup" && argc >= 5) run_setup(argv[2], std::atof(argv[3]), argv[4]);
+    else if (cmd == "makestate" && argc >= 3) make_state(argv[2], 20, 5000.0, 0.25, 3000);
     else { std::fprintf(stderr, "bad arguments\n"); return 2; }
     return 0;
 }

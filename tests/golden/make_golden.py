@@ -15,6 +15,8 @@ Outputs (committed):
   ref_setup_bs2.json/.bin  integrateInTime host set-up (GPUGrossPitaevskii_BCC.cu:222-348)
                            at block_scale 2.0 on state.dat
   ref_state_header.json  the binary header fields of state.dat (VortexState.cpp:49-72)
+  ref_state_small.dat    a coarse vortex state made by the reference's iterateSolution
+  ref_vortex_small.json  its diagnostics; ref_setup_small.json/.bin the set-up on it
 """
 import argparse
 import json
@@ -30,7 +32,8 @@ ORACLE = os.path.join(ROOT, "oracle")
 
 def run(args):
     out = subprocess.run(args, check=True, capture_output=True, text=True).stdout
-    return json.loads(out)
+    start = out.find("{")   # the reference's solver prints progress lines before the JSON
+    return json.loads(out[start:])
 
 
 def main():
@@ -55,6 +58,13 @@ def main():
     dump("ref_vortex_state2.json", run([exe, "vortex", os.path.join(gp, "state2.dat")]))
     binp = os.path.join(HERE, "ref_setup_bs2.bin")
     dump("ref_setup_bs2.json", run([exe, "setup", os.path.join(gp, "state.dat"), "2.0", binp]))
+
+    # A small vortex state from the reference's own relaxation solver (kappa 20,
+    # g 5000, r/z step 0.25), its diagnostics, and the integrateInTime set-up on it.
+    small = os.path.join(HERE, "ref_state_small.dat")
+    dump("ref_state_small.json", run([exe, "makestate", small]))
+    dump("ref_vortex_small.json", run([exe, "vortex", small]))
+    dump("ref_setup_small.json", run([exe, "setup", small, "1.5", os.path.join(HERE, "ref_setup_small.bin")]))
 
     # Header of the state file, decoded with the field order of VortexState::load.
     with open(os.path.join(gp, "state.dat"), "rb") as f:

@@ -382,21 +382,37 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
         __syncthreads();
         if (!last) return;
         __threadfence();
-        for (int i = warp; i < a.num_instances; i += NWARPS) {
+        // Each instance's rows are summed by the whole CTA: thread t folds rows
+        // b+t, b+t+NTHREADS, ... (compensated), then warps and the CTA combine
+        // in a fixed order, so the result does not depend on timing.
+        __shared__ double fin[NWARPS][4];
+        for (int i = 0; i < a.num_instances; i++) {
             const int b = a.inst_item_begin[2 * i], e = a.inst_item_begin[2 * i + 1];
-            double acc[4];
-            for (int k = 0; k < 4; k++) {
-                double sk = 0.0, ck = 0.0;
-                for (int r = b + lane; r < e; r += 32) {
-                    const double yv = __ldcg(a.partials + 4ll * r + k) - ck;
-                    const double t = sk + yv;
-                    ck = (t - sk) - yv;
-                    sk = t;
+            double sk[4] = {0.0, 0.0, 0.0, 0.0}, ck[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int r = b + tid; r < e; r += S::NTHREADS) {
+                const double2 v01 = __ldcg((const double2 *)(a.partials + 4ll * r));
+                const double2 v23 = __ldcg((const double2 *)(a.partials + 4ll * r + 2));
+                const double vv[4] = {v01.x, v01.y, v23.x, v23.y};
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const double yv = vv[k] - ck[k];
+                    const double t = sk[k] + yv;
+                    ck[k] = (t - sk[k]) - yv;
+                    sk[k] = t;
                 }
-                for (int off = 16; off > 0; off >>= 1) sk += __shfl_xor_sync(0xffffffffu, sk, off);
-                acc[k] = sk;
             }
-            if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                for (int off = 16; off > 0; off >>= 1) sk[k] += __shfl_xor_sync(0xffffffffu, sk[k], off);
+            if (lane == 0)
+                for (int k = 0; k < 4; k++) fin[warp][k] = sk[k];
+            __syncthreads();
+            if (tid == 0) {
+                double acc[4];
+                for (int k = 0; k < 4; k++) {
+                    acc[k] = 0.0;
+                    for (int wi = 0; wi < NWARPS; wi++) acc[k] += fin[wi][k];
+                }
                 const InstDev &di = a.inst[i];
                 ImagScalars &sc = a.imag[i];
                 // acc: |p'|^2, Re(conj(p') dt H p'), |p'|^4, |next|^2 over values
@@ -411,6 +427,7 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
                 sc.steps += 1;
                 sc.sigma = 1.0 / sqrt(di.vol * acc[3]);
             }
+            __syncthreads();
         }
         if (tid == 0) *a.counter = 0u;
     }

@@ -101,6 +101,26 @@ class _Observables(C.Structure):
     ]
 
 
+class _VortexInfo(C.Structure):
+    _fields_ = [("kappa", C.c_uint32), ("rsize", C.c_uint32), ("zsize", C.c_uint32), ("pad_", C.c_uint32),
+                ("g", C.c_double), ("mu", C.c_double), ("rplug", C.c_double), ("rstep", C.c_double),
+                ("zstep", C.c_double), ("function_max", C.c_double), ("max_r", C.c_double), ("max_z", C.c_double),
+                ("curvature", C.c_double), ("block_scale", C.c_double)]
+
+
+class _IntegrateDesc(C.Structure):
+    _fields_ = [("block_scale", C.c_double), ("minp", C.c_double * 3), ("maxp", C.c_double * 3),
+                ("iteration_period", C.c_double), ("number_of_iterations", C.c_uint32), ("seed", C.c_uint32),
+                ("ratio", C.c_double), ("noise", C.c_double), ("precision", C.c_int32), ("device", C.c_int32)]
+
+
+class _IntegrateResult(C.Structure):
+    _fields_ = [("xsize", C.c_uint32), ("ysize", C.c_uint32), ("zsize", C.c_uint32),
+                ("steps_per_iteration", C.c_uint32), ("values", C.c_uint64), ("p0", C.c_double * 3),
+                ("maxpot", C.c_double), ("dt", C.c_double), ("lapfac_dt", C.c_double), ("lapfac0_dt", C.c_double),
+                ("g_dt", C.c_double), ("odd_phase", C.c_double * 2), ("device_ms", C.c_double)]
+
+
 _lib = None
 
 
@@ -145,6 +165,20 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_variant_count.restype = C.c_int32
     lib.gpe_variant_describe.restype = st
     lib.gpe_variant_describe.argtypes = [C.c_int32] + [C.POINTER(C.c_int32)] * 4
+    lib.gpe_vortex_load.restype = st
+    lib.gpe_vortex_load.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+    lib.gpe_vortex_free.restype = None
+    lib.gpe_vortex_free.argtypes = [C.c_void_p]
+    lib.gpe_vortex_describe.restype = st
+    lib.gpe_vortex_describe.argtypes = [C.c_void_p, C.c_double, C.POINTER(_VortexInfo)]
+    lib.gpe_vortex_psi.restype = st
+    lib.gpe_vortex_psi.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.gpe_integrate_setup.restype = st
+    lib.gpe_integrate_setup.argtypes = [C.c_void_p, C.POINTER(_IntegrateDesc), C.POINTER(_IntegrateResult),
+                                        C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.gpe_integrate_in_time.restype = st
+    lib.gpe_integrate_in_time.argtypes = [C.c_void_p, C.POINTER(_IntegrateDesc), C.POINTER(_IntegrateResult),
+                                          C.POINTER(_Observables), C.c_void_p, C.c_void_p]
     lib.gpe_observables_noalloc.restype = st
     lib.gpe_observables_noalloc.argtypes = [C.c_int32, C.c_int32, C.POINTER(_Instance), C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.POINTER(_Observables)]
@@ -359,6 +393,88 @@ class Stepper:
 
     def __exit__(self, *a):
         self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class VortexState:
+    """A vortex state file in the reference's VortexState format, and the
+    reference's solver call on it (integrateInTime, GPUGrossPitaevskii_BCC.cu:218)."""
+
+    def __init__(self, path: str):
+        self.lib = load_library()
+        h = C.c_void_p()
+        _check(self.lib.gpe_vortex_load(path.encode(), C.byref(h)), "gpe_vortex_load")
+        self.h = h
+
+    def describe(self, eps_fraction: float = 1e-5) -> dict:
+        info = _VortexInfo()
+        _check(self.lib.gpe_vortex_describe(self.h, eps_fraction, C.byref(info)), "gpe_vortex_describe")
+        return {k: getattr(info, k) for k, _ in _VortexInfo._fields_ if k != "pad_"}
+
+    def psi(self, p) -> complex:
+        pp = (C.c_double * 3)(*p)
+        out = (C.c_double * 2)()
+        _check(self.lib.gpe_vortex_psi(self.h, pp, out), "gpe_vortex_psi")
+        return complex(out[0], out[1])
+
+    @staticmethod
+    def _desc(block_scale, minp, maxp, iteration_period=1.0, number_of_iterations=1, seed=54363, ratio=0.1,
+              noise=0.01, precision=Precision.FP64, device=0):
+        d = _IntegrateDesc()
+        d.block_scale, d.iteration_period = block_scale, iteration_period
+        d.number_of_iterations, d.seed, d.ratio, d.noise = number_of_iterations, seed, ratio, noise
+        d.precision, d.device = int(precision), device
+        for k in range(3):
+            d.minp[k], d.maxp[k] = minp[k], maxp[k]
+        return d
+
+    @staticmethod
+    def _res(r: _IntegrateResult) -> dict:
+        out = {k: getattr(r, k) for k, _ in _IntegrateResult._fields_}
+        out["p0"] = list(r.p0)
+        out["odd_phase"] = list(r.odd_phase)
+        return out
+
+    def setup(self, block_scale, minp, maxp, **kw):
+        """integrateInTime's host set-up: (result, even, odd, V) with fields in
+        block order, shape (zsize, ysize, xsize, 12, 2)."""
+        d = self._desc(block_scale, minp, maxp, **kw)
+        r = _IntegrateResult()
+        _check(self.lib.gpe_integrate_setup(self.h, C.byref(d), C.byref(r), None, None, None), "gpe_integrate_setup")
+        shp = (r.zsize, r.ysize, r.xsize, 12)
+        even = np.empty(shp + (2,))
+        odd = np.empty(shp + (2,))
+        V = np.empty(shp)
+        _check(self.lib.gpe_integrate_setup(self.h, C.byref(d), C.byref(r), even.ctypes.data_as(C.c_void_p),
+                                            odd.ctypes.data_as(C.c_void_p), V.ctypes.data_as(C.c_void_p)),
+               "gpe_integrate_setup")
+        return self._res(r), even, odd, V
+
+    def integrate_in_time(self, block_scale, minp, maxp, iteration_period=1.0, number_of_iterations=1, **kw):
+        """The reference's solver call on the GPU.  Returns (result, observables
+        per iteration, final even, final odd)."""
+        d = self._desc(block_scale, minp, maxp, iteration_period, number_of_iterations, **kw)
+        r = _IntegrateResult()
+        _check(self.lib.gpe_integrate_setup(self.h, C.byref(d), C.byref(r), None, None, None), "gpe_integrate_setup")
+        shp = (r.zsize, r.ysize, r.xsize, 12, 2)
+        even = np.empty(shp)
+        odd = np.empty(shp)
+        obs = (_Observables * (number_of_iterations + 1))()
+        _check(self.lib.gpe_integrate_in_time(self.h, C.byref(d), C.byref(r), obs, even.ctypes.data_as(C.c_void_p),
+                                              odd.ctypes.data_as(C.c_void_p)), "gpe_integrate_in_time")
+        ob = [{k: getattr(o, k) for k in ("norm", "energy", "mu", "kinetic", "potential", "interaction")}
+              for o in obs]
+        return self._res(r), ob, even, odd
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gpe_vortex_free(self.h)
+            self.h = None
 
     def __del__(self):
         try:
