@@ -189,6 +189,14 @@ gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64
  * GPUGrossPitaevskii_BCC.cu:421,488). */
 gpe_status gpe_time_steps(gpe_handle h, int64_t steps, float *ms);
 
+/* Test hook for failure detection: when plane >= 0, the fused kernel's
+ * producer withholds that plane's copy in the first work item of every launch,
+ * so that the consumers' bounded wait (about one second) runs out; the launch
+ * returns early and the next gpe_synchronize/gpe_download/... reports
+ * GPE_ERR_TIMEOUT.  plane = -1 switches it off.  No counterpart in the reference
+ * (which has no device-side waits). */
+gpe_status gpe_debug_inject(gpe_handle h, int32_t plane);
+
 /* Number of fused-kernel variants (tile shape, pipeline depth, register cap)
  * that gpe_config.tile may select, and the tile shape of one of them. */
 int32_t gpe_variant_count(void);

@@ -1,0 +1,63 @@
+"""Failure detection without faulting the GPU.
+
+A bounded device wait that runs out (forced with the test hook that withholds
+one TMA copy) turns into GPE_ERR_TIMEOUT on the host and leaves the context
+usable; NaN in a field trips the observables watchdog; bad calls return codes.
+"""
+import numpy as np
+import pytest
+
+from helpers import grid_for, interleave, random_state, vdt_for
+from vaikkari_gb300.gpe import GpeError, Instance, Kernel, Lattice, Potential, Precision, Status, Stepper
+
+pytestmark = pytest.mark.gpu
+
+
+def _stepper(kernel=Kernel.FUSED):
+    inst = Instance(8, 8, 8, 0.4, 1e-3, 50.0, origin=(-1.6, -1.6, -1.6))
+    return Stepper([inst], lattice=Lattice.BCC2, precision=Precision.FP32, kernel=kernel, potential=Potential.TRAP,
+                   graph_steps=-1)
+
+
+def test_bounded_wait_timeout_is_reported_and_context_survives():
+    st = _stepper()
+    shp = st.shape(0)
+    e, o = random_state(shp, 1, 0.3), random_state(shp, 2, 0.3)
+    st.upload(0, e, o)
+    st.debug_inject(3)
+    st.step(1)
+    with pytest.raises(GpeError) as err:
+        st.synchronize()
+    assert err.value.status == Status.TIMEOUT
+    # the error word was cleared and the context still works: a clean run
+    # afterwards is bit-exact with the oracle
+    st.debug_inject(-1)
+    st.upload(0, e, o)
+    st.step(3)
+    ge, go = st.download(0)
+    g = grid_for(st, 0)
+    we, wo = interleave(e, np.float32), interleave(o, np.float32)
+    g.leapfrog_bcc2(we, wo, vdt_for(st, 0), 3)
+    st.close()
+    np.testing.assert_array_equal(ge, we)
+    np.testing.assert_array_equal(go, wo)
+
+
+def test_nan_in_field_trips_the_watchdog():
+    st = _stepper()
+    shp = st.shape(0)
+    e = random_state(shp, 3, 0.3)
+    e[2, 3, 4, 1] = complex(np.nan, 0.0)
+    st.upload(0, e, e)
+    with pytest.raises(GpeError) as err:
+        st.observables(0)
+    assert err.value.status == Status.NOT_FINITE
+    st.close()
+
+
+def test_debug_inject_needs_the_fused_kernel():
+    st = _stepper(Kernel.PLAIN)
+    with pytest.raises(GpeError) as err:
+        st.debug_inject(1)
+    assert err.value.status == Status.UNSUPPORTED
+    st.close()

@@ -35,7 +35,7 @@ def _worker(rank, world, port, out):
 
 def test_two_replicas_report_slowest_rank():
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.start_processes(_worker, args=(2, port, out), nprocs=2, join=True, start_method="spawn")
         res = dict(out)

@@ -84,6 +84,7 @@ struct gpe_handle_ {
     cudaStream_t stream = nullptr;
     std::map<GraphKey, cudaGraphExec_t> graphs;
     int parity = 0;      // imaginary time: which buffer holds psi
+    int inject = -1;     // test hook for the bounded waits (gpe_debug_inject)
     bool imag_ready = false;
     double tol = 0.0;
     long long launches = 0;
@@ -155,6 +156,7 @@ gpe_status enqueue_step_real(gpe_handle h)
             l.vpot = h->vpot;
             l.maps = h->maps;
             l.zcmax = h->zcmax;
+            l.inject_skip_plane = h->inject;
             l.src = half == 0 ? 0 : 1;
             l.err = h->err;
             l.num_instances = h->cfg.num_instances;
@@ -226,6 +228,7 @@ gpe_status enqueue_step_imag(gpe_handle h, int parity)
         l.vpot = h->vpot;
         l.maps = h->maps;
         l.zcmax = h->zcmax;
+        l.inject_skip_plane = h->inject;
         l.src = parity;
         l.err = h->err;
         l.imag = h->imag;
@@ -869,6 +872,18 @@ gpe_status gpe_time_steps(gpe_handle h, int64_t steps, float *ms)
     if (st != GPE_OK) return st;
     if (e != cudaSuccess) return cuda_fail(e, "gpe_time_steps");
     return sync_and_check(h);
+}
+
+gpe_status gpe_debug_inject(gpe_handle h, int32_t plane)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (!h->fused) return fail(GPE_ERR_UNSUPPORTED, "gpe_debug_inject: only the fused kernel has device waits");
+    h->inject = plane < 0 ? -1 : plane;
+    // launches already captured into graphs carry the old value
+    for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    return GPE_OK;
 }
 
 int32_t gpe_variant_count(void) { return fused_tile_count(); }

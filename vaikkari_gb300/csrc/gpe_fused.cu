@@ -66,6 +66,7 @@ struct FusedArgs {
     int num_instances;
     double tol;
     int *err;
+    int inject_skip_plane;  // test hook: plane the producer of work item 0 withholds (-1 = none)
 };
 
 template <typename T> struct Acc;
@@ -117,12 +118,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait: about a second at most (each try_wait suspends briefly).
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait: gives up after about one second of wall time.
+constexpr uint64_t kWaitLimitNs = 1000000000ull;
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
 {
-    for (int i = 0; i < (1 << 22); i++)
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (true) {
         if (mbar_try_wait(bar, parity)) return true;
-    return false;
+        if (global_ns() - t0 > kWaitLimitNs) return false;
+    }
 }
 
 __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
@@ -216,16 +228,21 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
             for (int k = 0; k < nplanes; k++) {
                 const int st = k % STAGES;
                 if (k >= STAGES) {
-                    bool ok = false;
-                    for (int i = 0; i < (1 << 22) && !ok; i++) {
+                    bool ok = mbar_try_wait(empty + 8 * st, ((k / STAGES) - 1) & 1);
+                    const uint64_t t0 = global_ns();
+                    while (!ok && !*(volatile int *)&abort_flag && global_ns() - t0 <= kWaitLimitNs)
                         ok = mbar_try_wait(empty + 8 * st, ((k / STAGES) - 1) & 1);
-                        if (!ok && *(volatile int *)&abort_flag) break;
-                    }
                     if (!ok) {
                         atomicExch(a.err, kErrTimeout);
                         abort_flag = 1;
                         break;
                     }
+                }
+                if (a.inject_skip_plane == k && it == 0) {
+                    // test hook (gpe_debug_inject): withhold this plane's copy so that
+                    // the consumers' bounded wait runs out
+                    issued = k;
+                    break;
                 }
                 const bool with_next = (MODE == 0) && (k >= 2);
                 mbar_arrive_expect_tx(full + 8 * st, S::HALO_BYTES + (with_next ? S::NEXT_BYTES : 0));
@@ -575,6 +592,7 @@ cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s)
     a.num_instances = l.num_instances;
     a.tol = l.tol;
     a.err = l.err;
+    a.inject_skip_plane = l.inject_skip_plane;
     if (l.precision == GPE_FP64) return fused_launch_tile<double>(l, a, s);
     return fused_launch_tile<float>(l, a, s);
 }

@@ -49,6 +49,7 @@ struct FusedLaunch {
     int zcmax;            // longest z-range of a work item
     int src;              // field index of prev (0 or 1)
     int *err;             // device error word (bounded-wait timeouts)
+    int inject_skip_plane;  // test hook, -1 = off
     const InstDev *inst;
     const WorkItem *items;
     int num_items;

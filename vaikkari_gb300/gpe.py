@@ -162,6 +162,8 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_stream.argtypes = [C.c_void_p]
     lib.gpe_time_steps.restype = st
     lib.gpe_time_steps.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]
+    lib.gpe_debug_inject.restype = st
+    lib.gpe_debug_inject.argtypes = [C.c_void_p, C.c_int32]
     lib.gpe_variant_count.restype = C.c_int32
     lib.gpe_variant_describe.restype = st
     lib.gpe_variant_describe.argtypes = [C.c_int32] + [C.POINTER(C.c_int32)] * 4
@@ -371,6 +373,10 @@ class Stepper:
         ms = C.c_float()
         _check(self.lib.gpe_time_steps(self.h, int(steps), C.byref(ms)), "gpe_time_steps")
         return float(ms.value)
+
+    def debug_inject(self, plane: int):
+        """Test hook: make the fused kernel's bounded wait run out (see gpe.h)."""
+        _check(self.lib.gpe_debug_inject(self.h, int(plane)), "gpe_debug_inject")
 
     def launch_count(self) -> int:
         return int(self.lib.gpe_launch_count(self.h))
