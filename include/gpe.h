@@ -270,6 +270,30 @@ gpe_status gpe_integrate_setup(gpe_vortex v, const gpe_integrate_desc *d, gpe_in
 gpe_status gpe_integrate_in_time(gpe_vortex v, const gpe_integrate_desc *d, gpe_integrate_result *res,
                                  gpe_observables *per_iteration, double *even_out, double *odd_out);
 
+/* ---- Field outputs (device-side downsampling) ----------------------------------
+ * The reference's debug outputs, compiled out there by default
+ * (GPUGrossPitaevskii_BCC.cu:18-19). */
+
+/* Density per block over the padded block grid, (nx+2)*(ny+2)*(nz+2) uint16 in
+ * x-fastest order with zero padding blocks: min(65535, trunc(unit * sum)).  With
+ * reference_sum != 0 the sum is the reference's (its loop adds the first value's
+ * |psi|^2 twelve times, GPUGrossPitaevskii_BCC.cu:456-459); otherwise it is the
+ * block's total density.  The reference's unit is 60000 / (12 fmax^2). */
+gpe_status gpe_volume_map(gpe_handle h, int32_t instance, int32_t field, double unit, int32_t reference_sum,
+                          uint16_t *out);
+/* One plane of blocks (padded index z_padded, value `slot`) as (nx+2)*(ny+2) RGB
+ * triples: 256 * gain * (Re psi, |psi|, Im psi), below 1 -> 0, above 255 -> 255
+ * (the reference draws slot 0 of plane zsize/2+1 with gain 5, :426-440). */
+gpe_status gpe_slice_rgb(gpe_handle h, int32_t instance, int32_t field, int32_t z_padded, int32_t slot, double gain,
+                         uint8_t *out);
+/* MetaImage header <path> and data <path>.raw, as saveVolumeMap writes them
+ * (GPUGrossPitaevskii_BCC.cu:38-67); spacing = block edge per axis. */
+gpe_status gpe_write_metaimage(const char *path, const uint16_t *vol, uint32_t dx, uint32_t dy, uint32_t dz,
+                               const double *spacing);
+/* 24-bit BMP as Picture::save writes it (jukan_koodit/Output/Picture.cpp:81-129);
+ * rgb = width*height triples, row 0 first. */
+gpe_status gpe_write_bmp(const char *path, const uint8_t *rgb, uint32_t width, uint32_t height);
+
 /* Observables without allocating.  No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc - programs whose device memory is all
  * handed out by their own pool, or latency-critical code where an allocation

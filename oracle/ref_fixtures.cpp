@@ -258,6 +258,62 @@ static void run_setup(const char *state_path, double block_scale, const char *ou
     std::printf("  \"layout\": \"float64; even[z][y][x][slot][re,im], then odd (same), then pot*dt[z][y][x][slot]\"\n}\n");
 }
 
+// The reference's two debug outputs for the even field of a set-up file written
+// by `setup` (block order, interior blocks): the BMP slice of SAVE_PICTURE
+// (GPUGrossPitaevskii_BCC.cu:424-441) and the MetaImage volume of SAVE_VOLUME
+// (:443-468), both on the padded host array the reference keeps, written by
+// the reference's own Picture::save and saveVolumeMap.  The per-pixel loops are
+// restated from those lines (they sit inside integrateInTime).
+#include "jukan_koodit/Output/Picture.hpp"
+bool saveVolumeMap(const std::string &path, const Buffer<ushort> &vol, const uint xsize, const uint ysize,
+                   const uint zsize, const Vector3 &h);
+static void run_outputs(const char *setup_bin, uint xsize, uint ysize, uint zsize, double block_scale, double fmax,
+                        const char *bmp, const char *mhd)
+{
+    const size_t n = size_t(xsize) * ysize * zsize * 12;
+    std::vector<double> even(2 * n);
+    FILE *f = std::fopen(setup_bin, "rb");
+    if (!f || std::fread(even.data(), sizeof(double), even.size(), f) != even.size()) { std::fprintf(stderr, "bad %s\n", setup_bin); std::exit(2); }
+    std::fclose(f);
+    const uint dxsize = xsize + 2, dysize = ysize + 2, dzsize = zsize + 2, bsize = 12;
+    // padded host array h_evenPsi[(k*dysize + j)*dxsize + i].values[l]
+    std::vector<double> h(size_t(dxsize) * dysize * dzsize * 24, 0.0);
+    for (uint k = 0; k < zsize; k++)
+        for (uint j = 0; j < ysize; j++)
+            for (uint i = 0; i < xsize; i++)
+                for (uint l = 0; l < 12; l++) {
+                    const size_t src = ((size_t(k) * ysize + j) * xsize + i) * 12 + l;
+                    const size_t dst = ((size_t(k + 1) * dysize + (j + 1)) * dxsize + (i + 1)) * 24 + 2 * l;
+                    h[dst] = even[2 * src];
+                    h[dst + 1] = even[2 * src + 1];
+                }
+    // picture (:426-440)
+    Picture pic(dxsize, dysize);
+    const uint kk = zsize / 2 + 1;
+    for (uint j = 0; j < dysize; j++)
+        for (uint i = 0; i < dxsize; i++) {
+            const size_t idx = size_t(kk) * dxsize * dysize + j * dxsize + i;
+            const double x = h[idx * 24], y = h[idx * 24 + 1];
+            const double norm = sqrt(x * x + y * y);
+            pic.setColor(i, j, 5.0 * Vector4(x, norm, y, 1.0));
+        }
+    pic.save(bmp, false);
+    // volume (:445-467), including the reference's sum over values[0]
+    const ddouble unit = 60000.0 / (bsize * fmax * fmax);
+    Buffer<ushort> vol(dxsize * dysize * dzsize);
+    for (uint k = 0; k < dzsize; k++)
+        for (uint j = 0; j < dysize; j++)
+            for (uint i = 0; i < dxsize; i++) {
+                const size_t idx = size_t(k) * dxsize * dysize + j * dxsize + i;
+                ddouble sum = 0.0;
+                for (uint l = 0; l < bsize; l++) sum += h[idx * 24] * h[idx * 24] + h[idx * 24 + 1] * h[idx * 24 + 1];
+                sum *= unit;
+                vol[idx] = (sum > 65535.0 ? 65535 : ushort(sum));
+            }
+    saveVolumeMap(mhd, vol, dxsize, dysize, dzsize, block_scale * BLOCK_WIDTH);
+    std::printf("{\"unit\": %.17g, \"slice_k\": %u, \"dims\": [%u, %u, %u]}\n", unit, kk, dxsize, dysize, dzsize);
+}
+
 // A small vortex state made by the reference's own axisymmetric relaxation
 // (VortexState::setRange + iterateSolution, VortexState.cpp:42-47,109-196; the
 // potential is the reference's potentialRZ, GPUGrossPitaevskii_BCC.cu:28-31).
@@ -283,6 +339,9 @@ int main(int argc, char **argv)
     else if (cmd == "vortex" && argc >= 3) print_vortex(argv[2]);
     else if (cmd == "setup" && argc >= 5) run_setup(argv[2], std::atof(argv[3]), argv[4]);
     else if (cmd == "makestate" && argc >= 3) make_state(argv[2], 20, 5000.0, 0.25, 3000);
+    else if (cmd == "outputs" && argc >= 10)
+        run_outputs(argv[2], std::atoi(argv[3]), std::atoi(argv[4]), std::atoi(argv[5]), std::atof(argv[6]),
+                    std::atof(argv[7]), argv[8], argv[9]);
     else { std::fprintf(stderr, "bad arguments\n"); return 2; }
     return 0;
 }

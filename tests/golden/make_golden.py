@@ -17,6 +17,8 @@ Outputs (committed):
   ref_state_header.json  the binary header fields of state.dat (VortexState.cpp:49-72)
   ref_state_small.dat    a coarse vortex state made by the reference's iterateSolution
   ref_vortex_small.json  its diagnostics; ref_setup_small.json/.bin the set-up on it
+  ref_slice_small.bmp, ref_volume_small.mhd/.raw, ref_outputs_small.json
+                         the reference's picture and volume outputs of that set-up
 """
 import argparse
 import json
@@ -65,6 +67,17 @@ def main():
     dump("ref_state_small.json", run([exe, "makestate", small]))
     dump("ref_vortex_small.json", run([exe, "vortex", small]))
     dump("ref_setup_small.json", run([exe, "setup", small, "1.5", os.path.join(HERE, "ref_setup_small.bin")]))
+
+    # The reference's BMP slice and MetaImage volume of the small set-up's even
+    # field, written by its own Picture::save / saveVolumeMap (relative paths, so
+    # that the .mhd names its .raw without a directory).
+    setup = json.load(open(os.path.join(HERE, "ref_setup_small.json")))
+    vortex = json.load(open(os.path.join(HERE, "ref_vortex_small.json")))
+    out = subprocess.run([exe, "outputs", "ref_setup_small.bin", str(setup["xsize"]), str(setup["ysize"]),
+                          str(setup["zsize"]), repr(setup["block_scale"]), repr(vortex["function_max"]),
+                          "ref_slice_small.bmp", "ref_volume_small.mhd"],
+                         check=True, capture_output=True, text=True, cwd=HERE).stdout
+    dump("ref_outputs_small.json", json.loads(out))
 
     # Header of the state file, decoded with the field order of VortexState::load.
     with open(os.path.join(gp, "state.dat"), "rb") as f:

@@ -500,7 +500,7 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
     GPE_CREATE_TRY(set_plain_table(h->lat));
 
     // Arena layout.
-    size_t off = 0, voff = 0, max_vals = 0;
+    size_t off = 0, voff = 0, max_vals = 0, out_bytes = 0;
     std::vector<std::vector<double>> traps(cfg->num_instances);
     for (int i = 0; i < cfg->num_instances; i++) {
         const gpe_instance &in = h->inst[i];
@@ -541,6 +541,9 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
         d.vol = h->lat.cell_volume * in.block_scale * in.block_scale * in.block_scale;
         h->idev_host.push_back(d);
         max_vals = std::max(max_vals, size_t(in.nx) * in.ny * in.nz * h->ns);
+        // the output kernels stage a padded block grid of uint16 / a padded plane of RGB
+        out_bytes = std::max(out_bytes, size_t(in.nx + 2) * (in.ny + 2) * (in.nz + 2) * 2);
+        out_bytes = std::max(out_bytes, size_t(in.nx + 2) * (in.ny + 2) * 3);
     }
     h->field_elems = off;
     h->v_elems = voff;
@@ -573,7 +576,7 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
             }
         }
     }
-    h->staging_bytes = std::max<size_t>(max_vals * cbytes, 64);
+    h->staging_bytes = std::max<size_t>(std::max(max_vals * cbytes, out_bytes), 64);
     GPE_CREATE_TRY(cudaMalloc(&h->staging, h->staging_bytes));
     GPE_CREATE_TRY(cudaMalloc(&h->imag, sizeof(ImagScalars) * cfg->num_instances));
     std::vector<ImagScalars> imag_init(cfg->num_instances);
@@ -884,6 +887,41 @@ gpe_status gpe_debug_inject(gpe_handle h, int32_t plane)
     for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
     return GPE_OK;
+}
+
+gpe_status gpe_volume_map(gpe_handle h, int32_t instance, int32_t field, double unit, int32_t reference_sum,
+                          uint16_t *out)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (instance < 0 || instance >= h->cfg.num_instances || (field != 0 && field != 1) || !out)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_volume_map: bad arguments");
+    const gpe_instance &in = h->inst[instance];
+    const long long total = (long long)(in.nx + 2) * (in.ny + 2) * (in.nz + 2);
+    const int src = (h->cfg.mode == GPE_IMAGINARY_TIME) ? (field == 0 ? h->parity : 1 - h->parity) : field;
+    GPE_CUDA_TRY(launch_volume(h->cfg.precision, h->idev, instance, h->buf[src], unit, reference_sum ? 1 : 0,
+                               (uint16_t *)h->staging, total, h->stream));
+    h->launches++;
+    GPE_CUDA_TRY(cudaMemcpyAsync(out, h->staging, size_t(total) * 2, cudaMemcpyDeviceToHost, h->stream));
+    return sync_and_check(h);
+}
+
+gpe_status gpe_slice_rgb(gpe_handle h, int32_t instance, int32_t field, int32_t z_padded, int32_t slot, double gain,
+                         uint8_t *out)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (instance < 0 || instance >= h->cfg.num_instances || (field != 0 && field != 1) || !out || slot < 0 ||
+        slot >= h->ns)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_slice_rgb: bad arguments");
+    const gpe_instance &in = h->inst[instance];
+    const int total = (in.nx + 2) * (in.ny + 2);
+    const int src = (h->cfg.mode == GPE_IMAGINARY_TIME) ? (field == 0 ? h->parity : 1 - h->parity) : field;
+    GPE_CUDA_TRY(launch_slice(h->cfg.precision, h->idev, instance, h->buf[src], z_padded, slot, gain,
+                              (uint8_t *)h->staging, total, h->stream));
+    h->launches++;
+    GPE_CUDA_TRY(cudaMemcpyAsync(out, h->staging, size_t(total) * 3, cudaMemcpyDeviceToHost, h->stream));
+    return sync_and_check(h);
 }
 
 int32_t gpe_variant_count(void) { return fused_tile_count(); }

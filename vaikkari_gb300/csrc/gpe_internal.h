@@ -103,6 +103,11 @@ cudaError_t launch_pack(int precision, const InstDev *inst, int inst_index, int 
 cudaError_t launch_unpack(int precision, const InstDev *inst, int inst_index, int nx, int ny, int nz,
                           int slots, const void *field, void *host_order, const ImagScalars *imag,
                           cudaStream_t s);
+// Field outputs (gpe_output.cu).
+cudaError_t launch_volume(int precision, const InstDev *inst, int ii, const void *field, double unit, int quirk,
+                          uint16_t *out, long long total, cudaStream_t s);
+cudaError_t launch_slice(int precision, const InstDev *inst, int ii, const void *field, int kpad, int slot,
+                         double gain, uint8_t *rgb, int total, cudaStream_t s);
 cudaError_t launch_scale_field(int precision, const InstDev *inst, int inst_index, int nx, int ny, int nz,
                                int slots, void *field, const ImagScalars *imag, cudaStream_t s);
 // Imaginary time: sigma = 1/sqrt(norm) from observables sums (no mu update).

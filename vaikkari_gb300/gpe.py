@@ -181,6 +181,15 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_integrate_in_time.restype = st
     lib.gpe_integrate_in_time.argtypes = [C.c_void_p, C.POINTER(_IntegrateDesc), C.POINTER(_IntegrateResult),
                                           C.POINTER(_Observables), C.c_void_p, C.c_void_p]
+    lib.gpe_volume_map.restype = st
+    lib.gpe_volume_map.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.c_int32, C.c_void_p]
+    lib.gpe_slice_rgb.restype = st
+    lib.gpe_slice_rgb.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_void_p]
+    lib.gpe_write_metaimage.restype = st
+    lib.gpe_write_metaimage.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                        C.POINTER(C.c_double)]
+    lib.gpe_write_bmp.restype = st
+    lib.gpe_write_bmp.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32]
     lib.gpe_observables_noalloc.restype = st
     lib.gpe_observables_noalloc.argtypes = [C.c_int32, C.c_int32, C.POINTER(_Instance), C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.POINTER(_Observables)]
@@ -237,6 +246,24 @@ def variants() -> List[dict]:
         _check(lib.gpe_variant_describe(v, *[C.byref(x) for x in t]), "gpe_variant_describe")
         out.append({"tile": v, "tx": t[0].value, "ty": t[1].value, "stages": t[2].value, "min_blocks": t[3].value})
     return out
+
+
+def write_metaimage(path: str, vol: np.ndarray, spacing) -> None:
+    """MetaImage header `path` and data `path`.raw (gpe_write_metaimage); vol
+    shape (dz, dy, dx) uint16."""
+    lib = load_library()
+    vol = np.ascontiguousarray(vol, dtype=np.uint16)
+    sp = (C.c_double * 3)(*spacing)
+    _check(lib.gpe_write_metaimage(path.encode(), vol.ctypes.data_as(C.c_void_p), vol.shape[2], vol.shape[1],
+                                   vol.shape[0], sp), "gpe_write_metaimage")
+
+
+def write_bmp(path: str, rgb: np.ndarray) -> None:
+    """24-bit BMP (gpe_write_bmp); rgb shape (height, width, 3) uint8, row 0 first."""
+    lib = load_library()
+    rgb = np.ascontiguousarray(rgb, dtype=np.uint8)
+    _check(lib.gpe_write_bmp(path.encode(), rgb.ctypes.data_as(C.c_void_p), rgb.shape[1], rgb.shape[0]),
+           "gpe_write_bmp")
 
 
 @dataclass
@@ -377,6 +404,23 @@ class Stepper:
     def debug_inject(self, plane: int):
         """Test hook: make the fused kernel's bounded wait run out (see gpe.h)."""
         _check(self.lib.gpe_debug_inject(self.h, int(plane)), "gpe_debug_inject")
+
+    def volume_map(self, i: int, unit: float, field_: int = 0, reference_sum: bool = False) -> np.ndarray:
+        """Per-block density volume over the padded block grid, uint16, shape
+        (nz+2, ny+2, nx+2) (gpe_volume_map)."""
+        inst = self.instances[i]
+        out = np.empty((inst.nz + 2, inst.ny + 2, inst.nx + 2), dtype=np.uint16)
+        _check(self.lib.gpe_volume_map(self.h, i, field_, float(unit), int(reference_sum),
+                                       out.ctypes.data_as(C.c_void_p)), "gpe_volume_map")
+        return out
+
+    def slice_rgb(self, i: int, z_padded: int, slot: int = 0, gain: float = 5.0, field_: int = 0) -> np.ndarray:
+        """RGB image of one block plane, shape (ny+2, nx+2, 3) (gpe_slice_rgb)."""
+        inst = self.instances[i]
+        out = np.empty((inst.ny + 2, inst.nx + 2, 3), dtype=np.uint8)
+        _check(self.lib.gpe_slice_rgb(self.h, i, field_, int(z_padded), int(slot), float(gain),
+                                      out.ctypes.data_as(C.c_void_p)), "gpe_slice_rgb")
+        return out
 
     def launch_count(self) -> int:
         return int(self.lib.gpe_launch_count(self.h))
