@@ -203,10 +203,166 @@ void oracle_half_step_bcc2_f64(const oracle_grid *g, const double *prev, double 
     BCC2_BODY(double, fma)
 }
 
+/* One value of the checked BCC2 path (both slots of block (x, y, z)). */
+static void bcc2_value_f64(const oracle_grid *g0, const double *prev, double *next, const double *vdt, int mode,
+                           double sigma, int x0, int y0, int z0)
+{
+    oracle_grid one = *g0;
+    /* run the checked body on a 1x1x1 window by offsetting the loops */
+#define T double
+#define FMA fma
+    const oracle_grid *g = g0;
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    const T L0 = (T)g->L0, gdt = (T)g->gdt;
+    const T Lc0 = (T)g->Lc[0], Lc1 = (T)g->Lc[1];
+    (void)one;
+    {
+        const int z = z0, y = y0, x = x0;
+        T vx[2][3][3][3], vy[2][3][3][3];
+        for (int s = 0; s < 2; s++)
+            for (int dz = -1; dz <= 1; dz++)
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dx = -1; dx <= 1; dx++) {
+                        const int xx = x + dx, yy = y + dy, zz = z + dz;
+                        T a = 0, b = 0;
+                        if (xx >= 0 && xx < nx && yy >= 0 && yy < ny && zz >= 0 && zz < nz) {
+                            const size_t o = IDX(g, xx, yy, zz, s);
+                            a = prev[2 * o];
+                            b = prev[2 * o + 1];
+                            if (mode == 1) {
+                                a = sigma * a;
+                                b = sigma * b;
+                            }
+                        }
+                        vx[s][dz + 1][dy + 1][dx + 1] = a;
+                        vy[s][dz + 1][dy + 1][dx + 1] = b;
+                    }
+        for (int s = 0; s < 2; s++) {
+            T sdx, sdy, sax, say;
+            const T(*X)[3][3] = vx[s];
+            const T(*Y)[3][3] = vy[s];
+            const T(*OX)[3][3] = vx[1 - s];
+            const T(*OY)[3][3] = vy[1 - s];
+            if (s == 0) {
+                const T b0x = (OX[0][0][0] + OX[0][0][1]) + (OX[0][1][0] + OX[0][1][1]);
+                const T b0y = (OY[0][0][0] + OY[0][0][1]) + (OY[0][1][0] + OY[0][1][1]);
+                const T b1x = (OX[1][0][0] + OX[1][0][1]) + (OX[1][1][0] + OX[1][1][1]);
+                const T b1y = (OY[1][0][0] + OY[1][0][1]) + (OY[1][1][0] + OY[1][1][1]);
+                sdx = b0x + b1x;
+                sdy = b0y + b1y;
+            } else {
+                const T b0x = (OX[1][1][1] + OX[1][1][2]) + (OX[1][2][1] + OX[1][2][2]);
+                const T b0y = (OY[1][1][1] + OY[1][1][2]) + (OY[1][2][1] + OY[1][2][2]);
+                const T b1x = (OX[2][1][1] + OX[2][1][2]) + (OX[2][2][1] + OX[2][2][2]);
+                const T b1y = (OY[2][1][1] + OY[2][1][2]) + (OY[2][2][1] + OY[2][2][2]);
+                sdx = b0x + b1x;
+                sdy = b0y + b1y;
+            }
+            sax = (X[0][1][1] + X[2][1][1]) + ((X[1][1][0] + X[1][1][2]) + (X[1][0][1] + X[1][2][1]));
+            say = (Y[0][1][1] + Y[2][1][1]) + ((Y[1][1][0] + Y[1][1][2]) + (Y[1][0][1] + Y[1][2][1]));
+            const T px = X[1][1][1], py = Y[1][1][1];
+            const size_t o = IDX(g, x, y, z, s);
+            const T nrm = FMA(px, px, py * py);
+            const T cc = FMA(gdt, nrm, L0 + vdt[o]);
+            T ax = Lc0 * sdx, ay = Lc0 * sdy;
+            ax = FMA(Lc1, sax, ax);
+            ay = FMA(Lc1, say, ay);
+            const T hx = FMA(cc, px, ax), hy = FMA(cc, py, ay);
+            if (mode == 0) {
+                next[2 * o] = next[2 * o] + hy;
+                next[2 * o + 1] = next[2 * o + 1] - hx;
+            } else {
+                next[2 * o] = px - hx;
+                next[2 * o + 1] = py - hy;
+            }
+        }
+    }
+#undef T
+#undef FMA
+}
+
 void oracle_half_step_bcc2_f32(const oracle_grid *g, const float *prev, float *next, const float *vdt, int mode,
                                float sigma)
 {
     BCC2_BODY(float, fmaf)
+}
+
+/*
+ * The same BCC2 half-step, fast: interior values (one block away from every
+ * face) read their 3x3x3 neighbourhood by direct offsets, boundary values take
+ * the checked path above.  Same rounded operations in the same order, so it is
+ * bit-identical to oracle_half_step_bcc2_f64 (tests check it); used to time the
+ * CPU baseline.
+ */
+static void bcc2_value_f64(const oracle_grid *g, const double *prev, double *next, const double *vdt, int mode,
+                           double sigma, int x, int y, int z);
+
+void oracle_half_step_bcc2_fast_f64(const oracle_grid *g, const double *prev, double *next, const double *vdt,
+                                    int mode, double sigma)
+{
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    const double L0 = g->L0, gdt = g->gdt, Lc0 = g->Lc[0], Lc1 = g->Lc[1];
+    const ptrdiff_t sx = 2, sy = (ptrdiff_t)nx * 2, sz = (ptrdiff_t)nx * ny * 2; /* in slot units */
+    int z;
+#pragma omp parallel for schedule(static) num_threads(oracle_get_threads())
+    for (z = 0; z < nz; z++) {
+        for (int y = 0; y < ny; y++) {
+            const int interior_zy = (z > 0 && z < nz - 1 && y > 0 && y < ny - 1);
+            for (int x = 0; x < nx; x++) {
+                if (!interior_zy || x == 0 || x == nx - 1 || mode != 0) {
+                    bcc2_value_f64(g, prev, next, vdt, mode, sigma, x, y, z);
+                    continue;
+                }
+                const ptrdiff_t c = (((ptrdiff_t)z * ny + y) * nx + x) * 2; /* slot-0 index */
+#define P(o, s) (prev + 2 * (c + (o) + (s)))
+                /* slot 0 (C): B boxes at z-1, z around (x-1..x, y-1..y) */
+                {
+                    const double *b00 = P(-sz - sy - sx, 1), *b01 = P(-sz - sy, 1), *b02 = P(-sz - sx, 1), *b03 = P(-sz, 1);
+                    const double *b10 = P(-sy - sx, 1), *b11 = P(-sy, 1), *b12 = P(-sx, 1), *b13 = P(0, 1);
+                    const double sdx = ((b00[0] + b01[0]) + (b02[0] + b03[0])) + ((b10[0] + b11[0]) + (b12[0] + b13[0]));
+                    const double sdy = ((b00[1] + b01[1]) + (b02[1] + b03[1])) + ((b10[1] + b11[1]) + (b12[1] + b13[1]));
+                    const double *zm = P(-sz, 0), *zp = P(sz, 0), *xm = P(-sx, 0), *xp = P(sx, 0), *ym = P(-sy, 0), *yp = P(sy, 0);
+                    const double sax = (zm[0] + zp[0]) + ((xm[0] + xp[0]) + (ym[0] + yp[0]));
+                    const double say = (zm[1] + zp[1]) + ((xm[1] + xp[1]) + (ym[1] + yp[1]));
+                    const double *p = P(0, 0);
+                    const double px = p[0], py = p[1];
+                    const double nrm = fma(px, px, py * py);
+                    const double cc = fma(gdt, nrm, L0 + vdt[c]);
+                    const double ax = fma(Lc1, sax, Lc0 * sdx), ay = fma(Lc1, say, Lc0 * sdy);
+                    const double hx = fma(cc, px, ax), hy = fma(cc, py, ay);
+                    next[2 * c] = next[2 * c] + hy;
+                    next[2 * c + 1] = next[2 * c + 1] - hx;
+                }
+                /* slot 1 (B): C boxes at z, z+1 around (x..x+1, y..y+1) */
+                {
+                    const double *c00 = P(0, 0), *c01 = P(sx, 0), *c02 = P(sy, 0), *c03 = P(sy + sx, 0);
+                    const double *c10 = P(sz, 0), *c11 = P(sz + sx, 0), *c12 = P(sz + sy, 0), *c13 = P(sz + sy + sx, 0);
+                    const double sdx = ((c00[0] + c01[0]) + (c02[0] + c03[0])) + ((c10[0] + c11[0]) + (c12[0] + c13[0]));
+                    const double sdy = ((c00[1] + c01[1]) + (c02[1] + c03[1])) + ((c10[1] + c11[1]) + (c12[1] + c13[1]));
+                    const double *zm = P(-sz, 1), *zp = P(sz, 1), *xm = P(-sx, 1), *xp = P(sx, 1), *ym = P(-sy, 1), *yp = P(sy, 1);
+                    const double sax = (zm[0] + zp[0]) + ((xm[0] + xp[0]) + (ym[0] + yp[0]));
+                    const double say = (zm[1] + zp[1]) + ((xm[1] + xp[1]) + (ym[1] + yp[1]));
+                    const double *p = P(0, 1);
+                    const double px = p[0], py = p[1];
+                    const double nrm = fma(px, px, py * py);
+                    const double cc = fma(gdt, nrm, L0 + vdt[c + 1]);
+                    const double ax = fma(Lc1, sax, Lc0 * sdx), ay = fma(Lc1, say, Lc0 * sdy);
+                    const double hx = fma(cc, px, ax), hy = fma(cc, py, ay);
+                    next[2 * (c + 1)] = next[2 * (c + 1)] + hy;
+                    next[2 * (c + 1) + 1] = next[2 * (c + 1) + 1] - hx;
+                }
+#undef P
+            }
+        }
+    }
+}
+
+void oracle_leapfrog_bcc2_fast_f64(const oracle_grid *g, double *even, double *odd, const double *vdt, long steps)
+{
+    for (long k = 0; k < steps; k++) {
+        oracle_half_step_bcc2_fast_f64(g, even, odd, vdt, 0, 1.0);
+        oracle_half_step_bcc2_fast_f64(g, odd, even, vdt, 0, 1.0);
+    }
 }
 
 void oracle_leapfrog_bcc2_f64(const oracle_grid *g, double *even, double *odd, const double *vdt, long steps)

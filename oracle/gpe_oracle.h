@@ -61,6 +61,12 @@ void oracle_half_step_bcc2_f32(const oracle_grid *g, const float *prev, float *n
 void oracle_leapfrog_bcc2_f64(const oracle_grid *g, double *even, double *odd, const double *vdt, long steps);
 void oracle_leapfrog_bcc2_f32(const oracle_grid *g, float *even, float *odd, const float *vdt, long steps);
 
+/* The BCC2 real-time half-step/leapfrog with direct indexing for interior values
+ * (bit-identical to the _bcc2_ functions); the timed CPU baseline. */
+void oracle_half_step_bcc2_fast_f64(const oracle_grid *g, const double *prev, double *next, const double *vdt,
+                                    int mode, double sigma);
+void oracle_leapfrog_bcc2_fast_f64(const oracle_grid *g, double *even, double *odd, const double *vdt, long steps);
+
 /* `steps` leapfrog steps (odd <- even, even <- odd). */
 void oracle_leapfrog_f64(const oracle_grid *g, double *even, double *odd, const double *vdt, long steps);
 void oracle_leapfrog_f32(const oracle_grid *g, float *even, float *odd, const float *vdt, long steps);

@@ -46,6 +46,7 @@ def load():
     lib.oracle_half_step_bcc2_f32.argtypes = [G, vp, vp, vp, C.c_int, C.c_float]
     lib.oracle_leapfrog_bcc2_f64.argtypes = [G, vp, vp, vp, C.c_long]
     lib.oracle_leapfrog_bcc2_f32.argtypes = [G, vp, vp, vp, C.c_long]
+    lib.oracle_leapfrog_bcc2_fast_f64.argtypes = [G, vp, vp, vp, C.c_long]
     lib.oracle_leapfrog_f64.argtypes = [G, vp, vp, vp, C.c_long]
     lib.oracle_leapfrog_f32.argtypes = [G, vp, vp, vp, C.c_long]
     lib.oracle_observables_f64.argtypes = [G, vp, vp, dp, dp, vp, vp]
@@ -126,6 +127,14 @@ class Grid:
             assert a.flags.c_contiguous
         fn = lib.oracle_leapfrog_bcc2_f64 if even.dtype == np.float64 else lib.oracle_leapfrog_bcc2_f32
         fn(C.byref(self._g), self._p(even), self._p(odd), self._p(vdt), int(steps))
+
+    def leapfrog_bcc2_fast(self, even, odd, vdt, steps):
+        """FP64, BCC2: the box-order leapfrog with direct interior indexing (bit-identical)."""
+        lib = load()
+        assert self.slots == 2 and even.dtype == np.float64
+        for a in (even, odd, vdt):
+            assert a.flags.c_contiguous
+        lib.oracle_leapfrog_bcc2_fast_f64(C.byref(self._g), self._p(even), self._p(odd), self._p(vdt), int(steps))
 
     def observables(self, psi, vdt, vol):
         lib = load()

@@ -107,3 +107,18 @@ def test_leapfrog_conserves_norm_approximately():
     n0 = g.observables(e, vdt, vol)["norm"]
     g.leapfrog(e, o, vdt, 200)
     assert abs(g.observables(e, vdt, vol)["norm"] - n0) / n0 < 1e-3
+
+
+@pytest.mark.parametrize("dims", [(1, 1, 1), (2, 3, 4), (9, 7, 11)])
+def test_bcc2_fast_path_bit_identical(dims):
+    """The timed CPU baseline (direct interior indexing) equals the checked path."""
+    g = _grid(Lattice.BCC2, dims)
+    shp = (dims[2], dims[1], dims[0], 2)
+    e = interleave(random_state(shp, 5, 0.3), np.float64)
+    o = interleave(random_state(shp, 6, 0.3), np.float64)
+    v = np.ascontiguousarray(np.random.default_rng(2).uniform(0, 0.01, shp))
+    e1, o1, e2, o2 = e.copy(), o.copy(), e.copy(), o.copy()
+    g.leapfrog_bcc2(e1, o1, v, 3)
+    g.leapfrog_bcc2_fast(e2, o2, v, 3)
+    np.testing.assert_array_equal(e1, e2)
+    np.testing.assert_array_equal(o1, o2)
