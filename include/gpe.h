@@ -189,6 +189,14 @@ gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64
  * GPUGrossPitaevskii_BCC.cu:421,488). */
 gpe_status gpe_time_steps(gpe_handle h, int64_t steps, float *ms);
 
+/* z-slab decomposition (the reference's multi-GPU strategy,
+ * GPUGrossPitaevskii_BCC_multi.cu:399-917, here on one GPU): instance `upper`
+ * continues instance `lower` along +z (same nx, ny and lattice; upper's origin z =
+ * lower's origin z + nz * block edge).  After every half-step the library copies
+ * the boundary planes of the field just written into the neighbour's padding
+ * planes, so the slabs evolve exactly as one undivided grid.  Real time only. */
+gpe_status gpe_link_z(gpe_handle h, int32_t lower, int32_t upper);
+
 /* Test hook for failure detection: when plane >= 0, the fused kernel's
  * producer withholds that plane's copy in the first work item of every launch,
  * so that the consumers' bounded wait (about one second) runs out; the launch

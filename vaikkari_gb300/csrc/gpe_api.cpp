@@ -85,6 +85,7 @@ struct gpe_handle_ {
     std::map<GraphKey, cudaGraphExec_t> graphs;
     int parity = 0;      // imaginary time: which buffer holds psi
     int inject = -1;     // test hook for the bounded waits (gpe_debug_inject)
+    std::vector<std::pair<int, int>> zlinks;  // (lower, upper): upper continues lower along +z
     bool imag_ready = false;
     double tol = 0.0;
     long long launches = 0;
@@ -135,6 +136,29 @@ gpe_status upload_raw(gpe_handle h, const void *src, size_t bytes)
     return GPE_OK;
 }
 
+// Halo exchange between z-linked instances for one field: the lower slab's top
+// interior plane goes to the upper slab's bottom padding plane and the upper
+// slab's bottom plane to the lower slab's top padding plane (the reference's
+// z-slab copies, GPUGrossPitaevskii_BCC_multi.cu:660-707).  Each plane is one
+// contiguous block of the padded layout.
+gpe_status enqueue_halo(gpe_handle h, int field)
+{
+    const size_t cb = 2 * h->esize;
+    for (auto &lk : h->zlinks) {
+        const InstDev &lo = h->idev_host[lk.first], &up = h->idev_host[lk.second];
+        char *f = (char *)h->buf[field];
+        const size_t bytes = size_t(lo.zstride) * cb;
+        // lower plane nz-1 (padded nz) -> upper padded plane 0
+        GPE_CUDA_TRY(cudaMemcpyAsync(f + size_t(up.base) * cb, f + size_t(lo.base + lo.nz * lo.zstride) * cb, bytes,
+                                     cudaMemcpyDeviceToDevice, h->stream));
+        // upper plane 0 (padded 1) -> lower padded plane nz+1
+        GPE_CUDA_TRY(cudaMemcpyAsync(f + size_t(lo.base + (lo.nz + 1) * lo.zstride) * cb,
+                                     f + size_t(up.base + up.zstride) * cb, bytes, cudaMemcpyDeviceToDevice,
+                                     h->stream));
+    }
+    return GPE_OK;
+}
+
 gpe_status enqueue_step_real(gpe_handle h)
 {
     // odd <- even, then even <- odd (GPUGrossPitaevskii_BCC.cu:475-481)
@@ -182,6 +206,8 @@ gpe_status enqueue_step_real(gpe_handle h)
                 h->launches++;
             }
         }
+        gpe_status st = enqueue_halo(h, half == 0 ? 1 : 0);
+        if (st != GPE_OK) return st;
     }
     return GPE_OK;
 }
@@ -763,6 +789,11 @@ gpe_status gpe_step(gpe_handle h, int64_t steps)
     if (st != GPE_OK) return st;
     if (steps < 0) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_step: negative step count");
     if (steps == 0) return GPE_OK;
+    if (!h->zlinks.empty()) {  // halos of both fields as uploaded
+        st = enqueue_halo(h, 0);
+        if (st == GPE_OK) st = enqueue_halo(h, 1);
+        if (st != GPE_OK) return st;
+    }
     if (h->cfg.mode == GPE_IMAGINARY_TIME) {
         st = imag_prepare(h);
         if (st != GPE_OK) return st;
@@ -922,6 +953,28 @@ gpe_status gpe_slice_rgb(gpe_handle h, int32_t instance, int32_t field, int32_t 
     h->launches++;
     GPE_CUDA_TRY(cudaMemcpyAsync(out, h->staging, size_t(total) * 3, cudaMemcpyDeviceToHost, h->stream));
     return sync_and_check(h);
+}
+
+gpe_status gpe_link_z(gpe_handle h, int32_t lower, int32_t upper)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (h->cfg.mode != GPE_REAL_TIME)
+        return fail(GPE_ERR_UNSUPPORTED, "gpe_link_z: slabs are supported in real time (imaginary time "
+                                         "normalises each instance on its own)");
+    const int n = h->cfg.num_instances;
+    if (lower < 0 || lower >= n || upper < 0 || upper >= n || lower == upper)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_link_z: bad instance indices");
+    const InstDev &lo = h->idev_host[lower], &up = h->idev_host[upper];
+    if (lo.nx != up.nx || lo.ny != up.ny || lo.px != up.px)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_link_z: linked slabs need the same nx and ny");
+    for (auto &lk : h->zlinks)
+        if (lk.first == lower || lk.second == upper)
+            return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_link_z: a slab has one neighbour per side");
+    h->zlinks.push_back({lower, upper});
+    for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);  // captured steps lack the new copies
+    h->graphs.clear();
+    return GPE_OK;
 }
 
 int32_t gpe_variant_count(void) { return fused_tile_count(); }

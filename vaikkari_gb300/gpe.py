@@ -162,6 +162,8 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_stream.argtypes = [C.c_void_p]
     lib.gpe_time_steps.restype = st
     lib.gpe_time_steps.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]
+    lib.gpe_link_z.restype = st
+    lib.gpe_link_z.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
     lib.gpe_debug_inject.restype = st
     lib.gpe_debug_inject.argtypes = [C.c_void_p, C.c_int32]
     lib.gpe_variant_count.restype = C.c_int32
@@ -400,6 +402,10 @@ class Stepper:
         ms = C.c_float()
         _check(self.lib.gpe_time_steps(self.h, int(steps), C.byref(ms)), "gpe_time_steps")
         return float(ms.value)
+
+    def link_z(self, lower: int, upper: int):
+        """Instance `upper` continues `lower` along +z; halos exchanged every half-step."""
+        _check(self.lib.gpe_link_z(self.h, int(lower), int(upper)), "gpe_link_z")
 
     def debug_inject(self, plane: int):
         """Test hook: make the fused kernel's bounded wait run out (see gpe.h)."""
