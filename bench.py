@@ -492,10 +492,11 @@ def _download(st, n):
     return [st.download(i, odd=False)[0] for i in range(n)]
 
 
-def _cpu_config_rate(conds, steps):
-    """FP64 oracle port, all host threads, `steps` leapfrog steps of every condensate."""
+def _cpu_config_rate(conds, budget_s=5.0):
+    """FP64 oracle port on all host threads: whole leapfrog steps of every
+    condensate for about `budget_s` seconds (at least one step)."""
     e64 = [np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1)) for c in conds]
-    v, n, el, nv = cpu_sample(conds, e64, [a.copy() for a in e64], 0.0, os.cpu_count() or 1)
+    v, n, el, nv = cpu_sample(conds, e64, [a.copy() for a in e64], budget_s, os.cpu_count() or 1)
     return {"value": v, "unit": METRIC, "cores": os.cpu_count() or 1, "kind": "port",
             "sample": f"{n} leapfrog step(s), {nv} vertices, FP64 oracle port, {el:.2f} s"}
 
@@ -549,11 +550,10 @@ def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1):
         ms = min(st.time_steps(200) for _ in range(2))
         rates[key] = verts * 200 / (ms * 1e-3)
         st.close()
-    cpu_steps = 2 if verts > 1e7 else (20 if verts > 1e6 else 200)
     return {"metric": METRIC, "value": rates["fp32_fused"], "unit": METRIC, "dtype": "f32",
             "config": {"workload": name, "instances": len(insts), "vertices": verts, "dt": insts[0].dt,
                        "variant": tile},
-            "rates": rates, "accuracy": acc, "cpu_baseline": _cpu_config_rate(conds, cpu_steps)}
+            "rates": rates, "accuracy": acc, "cpu_baseline": _cpu_config_rate(conds)}
 
 
 def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1):
@@ -602,9 +602,82 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1):
             "accuracy": acc, "cpu_baseline": None}
 
 
+def run_relax(args):
+    """main()'s vortex construction (GPUGrossPitaevskii_BCC.cu:509-531) on the GPU:
+    the coarse relaxation (0.2 grid, up to 10000 iterations), the fine one (0.03
+    grid resampled from it, 10000 iterations), and a batch of fine relaxations
+    over a range of g in one call.  The unit is one Gauss-Seidel point update
+    (with its share of the norm sums): (rsize - 1) * zsize per iteration."""
+    from vaikkari_gb300.gpe import VortexState, relax
+    unit = "point-updates/s"
+    t0 = time.perf_counter()
+    s0 = VortexState.create(20, 5000.0, 0.0, 15.0, 35.0, 0.2, 0.2)
+    r0 = s0.relax(10000)
+    d0 = s0.describe(1e-5)
+    fine_args = (d0["min_r"], d0["max_r"], d0["max_z"], 0.03, 0.03)
+    s = VortexState.create(20, 5000.0, *fine_args)
+    s.initialize(s0)
+    r1 = s.relax(10000)
+    wall = time.perf_counter() - t0
+    d = s.describe()
+    R0, Z0 = d0["rsize"], d0["zsize"]
+    R, Z = d["rsize"], d["zsize"]
+    fine_rate = (R - 1) * Z * r1["iterations"] / (r1["device_ms"] * 1e-3)
+    coarse_rate = (R0 - 1) * Z0 * r0["iterations"] / (r0["device_ms"] * 1e-3)
+    # a batch: the same fine grid for 19 values of g, one call
+    nb = max(1, args.relax_batch)
+    gs = np.linspace(4000.0, 6000.0, nb)
+    batch = []
+    for gv in gs:
+        v = VortexState.create(20, float(gv), *fine_args)
+        v.initialize(s0)
+        batch.append(v)
+    its = args.relax_batch_iters
+    rb = relax(batch, its, eps=0.0)
+    batch_rate = nb * (R - 1) * Z * its / (rb[0]["device_ms"] * 1e-3)
+    # CPU: the reference-order oracle on one thread (the reference's loop is serial)
+    cpu = None
+    if not args.skip_cpu:
+        import oracle.oracle as orc
+        path = _tmp_save(s0)
+        o0 = orc.Vortex.from_file(path)
+        os.remove(path)
+        o = orc.Vortex.from_range(20, 5000.0, *fine_args)
+        o.initialize(o0)
+        n, el = 0, 0.0
+        tc = time.perf_counter()
+        while el < args.cpu_budget and n < 10000:
+            o.iterate(100, eps=0.0)
+            n += 100
+            el = time.perf_counter() - tc
+        cpu = {"value": (R - 1) * Z * n / el, "unit": unit, "cores": 1, "kind": "port",
+               "sample": f"{n} iterations of the fine state ({R}x{Z}), FP64 oracle in the reference's order, "
+                         f"{el:.1f} s"}
+    line = {"metric": unit, "value": fine_rate, "unit": unit, "n_gpus": 1, "dtype": "f64", "data": "synthetic",
+            "higher_is_better": True,
+            "config": {"workload": "vortex_relaxation_main", "kappa": 20, "g": 5000.0, "coarse": [R0, Z0],
+                       "fine": [R, Z], "ratio": 0.1},
+            "coarse": {"iterations": r0["iterations"], "device_ms": r0["device_ms"], "rate": coarse_rate},
+            "fine": {"iterations": r1["iterations"], "device_ms": r1["device_ms"], "mu": d["mu"]},
+            "batch": {"states": nb, "iterations": its, "device_ms": rb[0]["device_ms"], "rate": batch_rate},
+            "construction_wall_s": wall, "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _tmp_save(v):
+    import tempfile
+    fd, path = tempfile.mkstemp(suffix=".dat")
+    os.close(fd)
+    v.save(path)
+    return path
+
+
 def run_workload(args):
     from vaikkari_gb300 import workloads
     name = args.workload
+    if name == "relax":
+        return run_relax(args)
     if name == "config1":
         line = run_config_realtime("config1_bcc2_32_realtime_1000", [workloads.config1()], [1000], tile=args.tile)
     elif name == "config2":
@@ -636,7 +709,10 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--workload", default="batch64",
-                    help="batch64 (the headline) or config1/config2/config3/config5 (accuracy cases)")
+                    help="batch64 (the headline), config1/config2/config3/config5 (accuracy cases) or relax "
+                         "(the vortex relaxation)")
+    ap.add_argument("--relax-batch", type=int, default=19)
+    ap.add_argument("--relax-batch-iters", type=int, default=2000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

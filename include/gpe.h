@@ -234,6 +234,7 @@ typedef struct gpe_vortex_info {
     double max_r, max_z;   /* searchMaxR/MaxZ at eps = eps_fraction * function_max    */
     double curvature;      /* integrateCurvature (:313-340)                           */
     double block_scale;    /* 2 pi / (20 sqrt(curvature)), main() :539               */
+    double min_r;          /* searchMinR at the same eps (VortexState.cpp:250-257)    */
 } gpe_vortex_info;
 
 typedef struct gpe_integrate_desc {
@@ -277,6 +278,56 @@ gpe_status gpe_integrate_setup(gpe_vortex v, const gpe_integrate_desc *d, gpe_in
  * (may be NULL) the final fields. */
 gpe_status gpe_integrate_in_time(gpe_vortex v, const gpe_integrate_desc *d, gpe_integrate_result *res,
                                  gpe_observables *per_iteration, double *even_out, double *odd_out);
+
+/* ---- The vortex relaxation (VortexState.cpp:98-185) on the GPU -----------------
+ * main() (GPUGrossPitaevskii_BCC.cu:509-531) builds its vortex state by relaxing a
+ * coarse profile, then a fine one resampled from it.  These calls reproduce each
+ * step; gpe_vortex_relax runs iterateSolution's sweeps on the GPU. */
+
+/* setKappa, setG and setRange with setDimensions' initial state
+ * (VortexState.cpp:12-47): rsize = (rmax-rmin)/rstep rounded, zsize likewise.
+ * A range that rounds to zero rows or columns is refused (the reference divides
+ * by that zero and continues with NaN values). */
+gpe_status gpe_vortex_create(uint32_t kappa, double g, double rmin, double rmax, double zmax, double rstep,
+                             double zstep, gpe_vortex *out);
+/* initialize(src) (VortexState.cpp:98-107): src's mu and its f resampled
+ * (bilinear, getFunction) onto dst's grid. */
+gpe_status gpe_vortex_initialize(gpe_vortex dst, gpe_vortex src);
+/* VortexState::save (VortexState.cpp:74-96). */
+gpe_status gpe_vortex_save(gpe_vortex v, const char *path);
+/* The values f(r_i, z_j), rsize*zsize doubles row-major (row i at r_i). */
+gpe_status gpe_vortex_values(gpe_vortex v, double *f);
+
+typedef struct gpe_relax_desc {
+    uint32_t maxiters;          /* iteration limit (10000 in main())                     */
+    uint32_t graph_iterations;  /* iterations per CUDA graph launch; 0 = 100             */
+    double eps;                 /* stop after an iteration whose diff < eps (1e-29)      */
+    double ratio;               /* potentialRZ's RATIO (0.1 in the reference)           */
+    int32_t device;
+    int32_t pad_;
+} gpe_relax_desc;
+
+typedef struct gpe_relax_result {
+    uint32_t iterations;        /* iterations run: k + 1 at the break, else maxiters   */
+    uint32_t pad_;
+    double diff;                /* the last iteration's diff                           */
+    double mu;                  /* the state's mu afterwards                           */
+    double device_ms;           /* device time of the whole call (all states)          */
+} gpe_relax_result;
+
+/* iterateSolution(potentialRZ, maxiters, eps) (VortexState.cpp:109-185) for
+ * `count` independent states at once; each state's f and mu are updated in place
+ * and results[k] (may be NULL) describes state k.  The sweep is the reference's
+ * Gauss-Seidel order exactly; the per-iteration sums are formed per row in chunks
+ * of 32 columns, so values agree with the reference to rounding (with a CPU
+ * restatement of that order bit for bit).  Needs rsize >= 2.  Error
+ * GPE_ERR_TIMEOUT if a sweep's bounded wait on the row above ran out. */
+gpe_status gpe_vortex_relax(gpe_vortex *states, int32_t count, const gpe_relax_desc *d, gpe_relax_result *results);
+
+/* Test hook: the relaxation sweep's division (from a correctly rounded
+ * reciprocal, two Markstein corrections) and __ddiv_rn on the same n pairs; host
+ * arrays, out ours[n] and ref[n]. */
+gpe_status gpe_debug_divide(const double *a, const double *b, double *ours, double *ref, int64_t n, int32_t device);
 
 /* ---- Field outputs (device-side downsampling) ----------------------------------
  * The reference's debug outputs, compiled out there by default

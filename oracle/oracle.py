@@ -36,7 +36,8 @@ def load():
         cc = os.environ.get("CC", "gcc")
         os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
         subprocess.run([cc, "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-                        "-fno-fast-math", os.path.join(HERE, "gpe_oracle.c"), "-o", LIB_PATH, "-lm"], check=True)
+                        "-fno-fast-math", os.path.join(HERE, "gpe_oracle.c"), os.path.join(HERE, "vortex_oracle.c"),
+                        "-o", LIB_PATH, "-lm"], check=True)
     lib = C.CDLL(LIB_PATH)
     vp, dp = C.c_void_p, C.c_double
     G = C.POINTER(_Grid)
@@ -53,6 +54,16 @@ def load():
     lib.oracle_observables_f32.argtypes = [G, vp, vp, dp, dp, vp, vp]
     lib.oracle_imaginary_f64.argtypes = [G, vp, vp, vp, dp, dp, vp, dp, C.c_long, dp, vp]
     lib.oracle_imaginary_f64.restype = C.c_long
+    ui, ul = C.c_uint, C.c_long
+    lib.oracle_vortex_initial.argtypes = [ui, dp, dp, ui, dp, vp]
+    lib.oracle_vortex_resample.argtypes = [vp, ui, ui, dp, dp, dp, vp, ui, ui, dp, dp, dp]
+    lib.oracle_vortex_iterate.argtypes = [vp, ui, ui, dp, dp, dp, ui, dp, dp, C.POINTER(dp), ul, dp, C.c_int,
+                                          C.c_int, C.POINTER(dp)]
+    lib.oracle_vortex_iterate.restype = ul
+    lib.oracle_vortex_function_max.argtypes = [vp, C.c_size_t]
+    lib.oracle_vortex_function_max.restype = dp
+    lib.oracle_vortex_min_r.argtypes = [vp, ui, ui, dp, dp, dp]
+    lib.oracle_vortex_min_r.restype = dp
     lib.oracle_set_threads.argtypes = [C.c_int]
     lib.oracle_get_threads.restype = C.c_int
     _lib = lib
@@ -152,3 +163,69 @@ class Grid:
         conv = lib.oracle_imaginary_f64(C.byref(self._g), self._p(psi), self._p(work), self._p(vdt), self.dt,
                                         self.g, self._p(self._w), vol, int(steps), tol, self._p(mu))
         return int(conv), mu[: int(steps)]
+
+
+class Vortex:
+    """The axisymmetric vortex state f(r, z) of VortexState.cpp: rsize x zsize
+    values, row i at r = rplug + i*rstep, column j at z = j*zstep."""
+
+    def __init__(self, kappa, g, rsize, zsize, rplug, rstep, zstep, mu=1.0, f=None):
+        self.kappa, self.g = int(kappa), float(g)
+        self.rsize, self.zsize = int(rsize), int(zsize)
+        self.rplug, self.rstep, self.zstep, self.mu = float(rplug), float(rstep), float(zstep), float(mu)
+        self.f = np.zeros(self.rsize * self.zsize) if f is None else np.ascontiguousarray(f, dtype=np.float64)
+
+    @classmethod
+    def from_range(cls, kappa, g, rmin, rmax, zmax, rstep, zstep):
+        """setKappa/setG/setRange with setDimensions' initial state (VortexState.cpp:12-47)."""
+        rsize0 = int((rmax - rmin) / rstep + 0.5)
+        zsize0 = int(zmax / zstep + 0.5)
+        if rsize0 == 0 or zsize0 == 0:
+            raise ValueError("range shorter than half a step")
+        rs = max((rmax - rmin) / rsize0, 1e-13)
+        zs = max(zmax / zsize0, 1e-13)
+        rsize, zsize = max(rsize0, 1), max(zsize0, 1)
+        v = cls(kappa, g, rsize, zsize, max(rmin, 0.0), rs, zs, 1.0)
+        load().oracle_vortex_initial(rsize, rs, v.rplug, zsize, zs, v.f.ctypes.data_as(C.c_void_p))
+        return v
+
+    @classmethod
+    def from_file(cls, path):
+        """The binary format of VortexState::load (VortexState.cpp:49-72)."""
+        import struct
+        raw = open(path, "rb").read()
+        kappa, g, rsize, zsize, rplug, rstep, zstep, mu = struct.unpack_from("<IdIIdddd", raw, 0)
+        f = np.frombuffer(raw, dtype="<f8", count=rsize * zsize, offset=struct.calcsize("<IdIIdddd"))
+        return cls(kappa, g, rsize, zsize, rplug, rstep, zstep, mu, f.copy())
+
+    def initialize(self, src):
+        """initialize(state) (VortexState.cpp:98-107): mu and a bilinear resampling of src."""
+        self.mu = src.mu
+        load().oracle_vortex_resample(src.f.ctypes.data_as(C.c_void_p), src.rsize, src.zsize, src.rplug, src.rstep,
+                                      src.zstep, self.f.ctypes.data_as(C.c_void_p), self.rsize, self.zsize,
+                                      self.rplug, self.rstep, self.zstep)
+
+    def iterate(self, maxiters, eps=1e-29, ratio=0.1, order=0, chunk=16):
+        """iterateSolution (VortexState.cpp:109-185) with potentialRZ; returns (iterations, last diff)."""
+        mu = C.c_double(self.mu)
+        diff = C.c_double(0.0)
+        its = load().oracle_vortex_iterate(self.f.ctypes.data_as(C.c_void_p), self.rsize, self.zsize, self.rplug,
+                                           self.rstep, self.zstep, self.kappa, self.g, ratio, C.byref(mu),
+                                           int(maxiters), eps, int(order), int(chunk), C.byref(diff))
+        self.mu = mu.value
+        return int(its), diff.value
+
+    def function_max(self):
+        return load().oracle_vortex_function_max(self.f.ctypes.data_as(C.c_void_p), self.f.size)
+
+    def min_r(self, eps):
+        return load().oracle_vortex_min_r(self.f.ctypes.data_as(C.c_void_p), self.rsize, self.zsize, self.rplug,
+                                          self.rstep, eps)
+
+    def max_r(self, eps):
+        idx = np.nonzero(self.f > eps)[0]
+        return self.rplug + (int(idx[-1]) // self.zsize) * self.rstep if idx.size else 0.0
+
+    def max_z(self, eps):
+        cols = np.nonzero((self.f.reshape(self.rsize, self.zsize) > eps).any(axis=0))[0]
+        return int(cols[-1]) * self.zstep if cols.size else 0.0

@@ -19,6 +19,9 @@ Outputs (committed):
   ref_vortex_small.json  its diagnostics; ref_setup_small.json/.bin the set-up on it
   ref_slice_small.bmp, ref_volume_small.mhd/.raw, ref_outputs_small.json
                          the reference's picture and volume outputs of that set-up
+  ref_state_main.json    digest of the reference's shipped state.dat (main()'s two-stage
+                         relaxation, GPUGrossPitaevskii_BCC.cu:509-531): header, SHA-256 of
+                         the values, and a seeded sample of values
 """
 import argparse
 import json
@@ -78,6 +81,22 @@ def main():
                           "ref_slice_small.bmp", "ref_volume_small.mhd"],
                          check=True, capture_output=True, text=True, cwd=HERE).stdout
     dump("ref_outputs_small.json", json.loads(out))
+
+    # The shipped state.dat is main()'s relaxation output: its digest and a sample.
+    import hashlib
+    import numpy as np
+    with open(os.path.join(gp, "state.dat"), "rb") as f:
+        raw = f.read()
+    hdr = struct.calcsize("<IdIIdddd")
+    kappa, g, rsize, zsize, rplug, rstep, zstep, mu = struct.unpack_from("<IdIIdddd", raw, 0)
+    vals = np.frombuffer(raw, dtype="<f8", count=rsize * zsize, offset=hdr)
+    idx = np.sort(np.random.default_rng(7).choice(rsize * zsize, 512, replace=False))
+    dump("ref_state_main.json", {
+        "source": "koodit/GrossPitaevskii/state.dat (main(), GPUGrossPitaevskii_BCC.cu:509-531)",
+        "kappa": kappa, "g": g, "rsize": rsize, "zsize": zsize, "rplug": rplug, "rstep": rstep, "zstep": zstep,
+        "mu": mu, "values_sha256": hashlib.sha256(vals.tobytes()).hexdigest(),
+        "function_max": float(vals.max()),
+        "sample_index": [int(i) for i in idx], "sample_value": [float(vals[i]) for i in idx]})
 
     # Header of the state file, decoded with the field order of VortexState::load.
     with open(os.path.join(gp, "state.dat"), "rb") as f:

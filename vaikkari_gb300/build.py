@@ -24,7 +24,7 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "libgpe_oracle.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["gpe_lattice.cpp", "gpe_api.cpp", "gpe_vortex.cpp", "gpe_plain.cu", "gpe_fused.cu", "gpe_output.cu", "gpe_noalloc.cu"]
+SOURCES = ["gpe_lattice.cpp", "gpe_api.cpp", "gpe_vortex.cpp", "gpe_plain.cu", "gpe_fused.cu", "gpe_output.cu", "gpe_noalloc.cu", "gpe_relax.cu"]
 
 
 def nvcc():
@@ -79,9 +79,9 @@ def build_lib(verbose=False):
 def build_oracle(verbose=False):
     os.makedirs(os.path.dirname(ORACLE_LIB), exist_ok=True)
     cc = os.environ.get("CC", "gcc")
-    src = os.path.join(ORACLE_DIR, "gpe_oracle.c")
+    srcs = [os.path.join(ORACLE_DIR, n) for n in ("gpe_oracle.c", "vortex_oracle.c")]
     tmp = ORACLE_LIB + ".tmp"
-    _run([cc, "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", src,
+    _run([cc, "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", *srcs,
           "-o", tmp, "-lm"], verbose)
     os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB

@@ -10,6 +10,14 @@
 #include "../../include/gpe.h"
 #include "gpe_device.cuh"
 
+// An axisymmetric vortex state f(r, z) (the reference's VortexState): rsize rows
+// at r = rplug + i*rstep, each of zsize values at z = j*zstep, row-major.
+struct gpe_vortex_ {
+    uint32_t kappa = 0, rsize = 0, zsize = 0;
+    double g = 0, rplug = 0, rstep = 0, zstep = 0, mu = 0;
+    std::vector<double> f;
+};
+
 namespace gpe {
 
 // Lattice tables from the BCC geometry (gpe_lattice.cpp).

@@ -105,7 +105,17 @@ class _VortexInfo(C.Structure):
     _fields_ = [("kappa", C.c_uint32), ("rsize", C.c_uint32), ("zsize", C.c_uint32), ("pad_", C.c_uint32),
                 ("g", C.c_double), ("mu", C.c_double), ("rplug", C.c_double), ("rstep", C.c_double),
                 ("zstep", C.c_double), ("function_max", C.c_double), ("max_r", C.c_double), ("max_z", C.c_double),
-                ("curvature", C.c_double), ("block_scale", C.c_double)]
+                ("curvature", C.c_double), ("block_scale", C.c_double), ("min_r", C.c_double)]
+
+
+class _RelaxDesc(C.Structure):
+    _fields_ = [("maxiters", C.c_uint32), ("graph_iterations", C.c_uint32), ("eps", C.c_double),
+                ("ratio", C.c_double), ("device", C.c_int32), ("pad_", C.c_int32)]
+
+
+class _RelaxResult(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("pad_", C.c_uint32), ("diff", C.c_double), ("mu", C.c_double),
+                ("device_ms", C.c_double)]
 
 
 class _IntegrateDesc(C.Structure):
@@ -175,6 +185,20 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_vortex_free.argtypes = [C.c_void_p]
     lib.gpe_vortex_describe.restype = st
     lib.gpe_vortex_describe.argtypes = [C.c_void_p, C.c_double, C.POINTER(_VortexInfo)]
+    lib.gpe_vortex_create.restype = st
+    lib.gpe_vortex_create.argtypes = [C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                      C.c_double, C.POINTER(C.c_void_p)]
+    lib.gpe_vortex_initialize.restype = st
+    lib.gpe_vortex_initialize.argtypes = [C.c_void_p, C.c_void_p]
+    lib.gpe_vortex_save.restype = st
+    lib.gpe_vortex_save.argtypes = [C.c_void_p, C.c_char_p]
+    lib.gpe_vortex_values.restype = st
+    lib.gpe_vortex_values.argtypes = [C.c_void_p, C.c_void_p]
+    lib.gpe_vortex_relax.restype = st
+    lib.gpe_vortex_relax.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(_RelaxDesc),
+                                     C.POINTER(_RelaxResult)]
+    lib.gpe_debug_divide.restype = st
+    lib.gpe_debug_divide.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32]
     lib.gpe_vortex_psi.restype = st
     lib.gpe_vortex_psi.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.gpe_integrate_setup.restype = st
@@ -461,11 +485,40 @@ class VortexState:
     """A vortex state file in the reference's VortexState format, and the
     reference's solver call on it (integrateInTime, GPUGrossPitaevskii_BCC.cu:218)."""
 
-    def __init__(self, path: str):
+    def __init__(self, path: str = None, _handle=None):
         self.lib = load_library()
+        if _handle is not None:
+            self.h = _handle
+            return
         h = C.c_void_p()
         _check(self.lib.gpe_vortex_load(path.encode(), C.byref(h)), "gpe_vortex_load")
         self.h = h
+
+    @classmethod
+    def create(cls, kappa: int, g: float, rmin: float, rmax: float, zmax: float, rstep: float, zstep: float):
+        """setKappa/setG/setRange with the initial profile (VortexState.cpp:12-47)."""
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.gpe_vortex_create(int(kappa), g, rmin, rmax, zmax, rstep, zstep, C.byref(h)), "gpe_vortex_create")
+        return cls(_handle=h)
+
+    def initialize(self, src: "VortexState"):
+        """initialize(src) (VortexState.cpp:98-107)."""
+        _check(self.lib.gpe_vortex_initialize(self.h, src.h), "gpe_vortex_initialize")
+
+    def save(self, path: str):
+        _check(self.lib.gpe_vortex_save(self.h, path.encode()), "gpe_vortex_save")
+
+    def values(self) -> np.ndarray:
+        """f as an array (rsize, zsize)."""
+        d = self.describe()
+        f = np.empty((d["rsize"], d["zsize"]))
+        _check(self.lib.gpe_vortex_values(self.h, f.ctypes.data_as(C.c_void_p)), "gpe_vortex_values")
+        return f
+
+    def relax(self, maxiters: int = 10000, eps: float = 1e-29, **kw) -> dict:
+        """iterateSolution(potentialRZ, maxiters, eps) on the GPU (VortexState.cpp:109-185)."""
+        return relax([self], maxiters, eps, **kw)[0]
 
     def describe(self, eps_fraction: float = 1e-5) -> dict:
         info = _VortexInfo()
@@ -537,3 +590,31 @@ class VortexState:
             self.close()
         except Exception:
             pass
+
+
+def relax(states: List["VortexState"], maxiters: int = 10000, eps: float = 1e-29, ratio: float = 0.1,
+          graph_iterations: int = 0, device: int = 0) -> List[dict]:
+    """iterateSolution for several independent vortex states in one GPU call
+    (gpe_vortex_relax); every state is updated in place."""
+    lib = load_library()
+    d = _RelaxDesc()
+    d.maxiters, d.graph_iterations, d.eps, d.ratio, d.device = int(maxiters), int(graph_iterations), eps, ratio, \
+        int(device)
+    n = len(states)
+    hs = (C.c_void_p * n)(*[s.h.value if isinstance(s.h, C.c_void_p) else s.h for s in states])
+    res = (_RelaxResult * n)()
+    _check(lib.gpe_vortex_relax(hs, n, C.byref(d), res), "gpe_vortex_relax")
+    return [{"iterations": r.iterations, "diff": r.diff, "mu": r.mu, "device_ms": r.device_ms} for r in res]
+
+
+def debug_divide(a: np.ndarray, b: np.ndarray, device: int = 0):
+    """The relaxation sweep's division and __ddiv_rn on the GPU (test hook)."""
+    lib = load_library()
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    assert a.shape == b.shape
+    ours, ref = np.empty_like(a), np.empty_like(a)
+    _check(lib.gpe_debug_divide(a.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p),
+                                ours.ctypes.data_as(C.c_void_p), ref.ctypes.data_as(C.c_void_p), a.size, device),
+           "gpe_debug_divide")
+    return ours, ref
