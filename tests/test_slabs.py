@@ -176,3 +176,14 @@ def test_link_z_rejects_bad_links():
     with pytest.raises(GpeError):
         im.link_z(0, 1)
     im.close()
+
+
+def test_halo_slots_are_the_references_packing():
+    """The slots a slab boundary exchanges are those the stencil reads across z:
+    for TETRA12 {2, 6} from above and {0, 9, 10, 11} from below, the reference's
+    packed halo (GPUGrossPitaevskii_BCC_MPI.cu:220-221); for BCC2 both slots."""
+    from vaikkari_gb300.gpe import Lattice, lattice_info
+    for lat, above, below in ((Lattice.TETRA12, [2, 6], [0, 9, 10, 11]), (Lattice.BCC2, [0, 1], [0, 1])):
+        e = lattice_info(lat)["entry"]
+        assert sorted({int(x[3]) for row in e for x in row if x[2] > 0}) == above
+        assert sorted({int(x[3]) for row in e for x in row if x[2] < 0}) == below

@@ -86,6 +86,7 @@ struct gpe_handle_ {
     int parity = 0;      // imaginary time: which buffer holds psi
     int inject = -1;     // test hook for the bounded waits (gpe_debug_inject)
     std::vector<std::pair<int, int>> zlinks;  // (lower, upper): upper continues lower along +z
+    uint32_t slots_from_above = 0, slots_from_below = 0;  // slots the stencil reads at z+1 / z-1
     bool imag_ready = false;
     double tol = 0.0;
     long long launches = 0;
@@ -136,25 +137,42 @@ gpe_status upload_raw(gpe_handle h, const void *src, size_t bytes)
     return GPE_OK;
 }
 
-// Halo exchange between z-linked instances for one field: the lower slab's top
-// interior plane goes to the upper slab's bottom padding plane and the upper
-// slab's bottom plane to the lower slab's top padding plane (the reference's
-// z-slab copies, GPUGrossPitaevskii_BCC_multi.cu:660-707).  Each plane is one
-// contiguous block of the padded layout.
-gpe_status enqueue_halo(gpe_handle h, int field)
+// Copies the slots in `mask` of one block plane: each slot's values are one
+// contiguous run of the padded layout, and neighbouring slots merge.
+gpe_status copy_plane_slots(gpe_handle h, char *f, long long dst_plane, long long src_plane, long long slot_len,
+                            uint32_t mask)
 {
     const size_t cb = 2 * h->esize;
+    for (int s = 0; s < h->ns;) {
+        if (!(mask >> s & 1u)) {
+            s++;
+            continue;
+        }
+        int e = s;
+        while (e < h->ns && (mask >> e & 1u)) e++;
+        GPE_CUDA_TRY(cudaMemcpyAsync(f + size_t(dst_plane + s * slot_len) * cb, f + size_t(src_plane + s * slot_len) * cb,
+                                     size_t(e - s) * size_t(slot_len) * cb, cudaMemcpyDeviceToDevice, h->stream));
+        s = e;
+    }
+    return GPE_OK;
+}
+
+// Halo exchange between z-linked instances for one field (the reference's
+// z-slab copies, GPUGrossPitaevskii_BCC_multi.cu:660-707 and the slot packing of
+// GPUGrossPitaevskii_BCC_MPI.cu:220-271): the lower slab's top interior plane
+// feeds the upper slab's bottom padding plane and the upper slab's bottom plane
+// the lower slab's top padding plane, each with only the slots the stencil reads
+// across that face (TETRA12: 4 and 2 of 12; BCC2: both).
+gpe_status enqueue_halo(gpe_handle h, int field)
+{
     for (auto &lk : h->zlinks) {
         const InstDev &lo = h->idev_host[lk.first], &up = h->idev_host[lk.second];
         char *f = (char *)h->buf[field];
-        const size_t bytes = size_t(lo.zstride) * cb;
-        // lower plane nz-1 (padded nz) -> upper padded plane 0
-        GPE_CUDA_TRY(cudaMemcpyAsync(f + size_t(up.base) * cb, f + size_t(lo.base + lo.nz * lo.zstride) * cb, bytes,
-                                     cudaMemcpyDeviceToDevice, h->stream));
-        // upper plane 0 (padded 1) -> lower padded plane nz+1
-        GPE_CUDA_TRY(cudaMemcpyAsync(f + size_t(lo.base + (lo.nz + 1) * lo.zstride) * cb,
-                                     f + size_t(up.base + up.zstride) * cb, bytes, cudaMemcpyDeviceToDevice,
-                                     h->stream));
+        gpe_status st = copy_plane_slots(h, f, up.base, lo.base + lo.nz * lo.zstride, lo.plane, h->slots_from_below);
+        if (st != GPE_OK) return st;
+        st = copy_plane_slots(h, f, lo.base + (lo.nz + 1) * lo.zstride, up.base + up.zstride, lo.plane,
+                              h->slots_from_above);
+        if (st != GPE_OK) return st;
     }
     return GPE_OK;
 }
@@ -972,6 +990,13 @@ gpe_status gpe_link_z(gpe_handle h, int32_t lower, int32_t upper)
         if (lk.first == lower || lk.second == upper)
             return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_link_z: a slab has one neighbour per side");
     h->zlinks.push_back({lower, upper});
+    h->slots_from_above = h->slots_from_below = 0;
+    for (int s = 0; s < h->lat.slots; s++)
+        for (int k = 0; k < h->lat.neighbours; k++) {
+            const int dz = h->lat.entry[s][k][2], sl = h->lat.entry[s][k][3];
+            if (dz > 0) h->slots_from_above |= 1u << sl;
+            if (dz < 0) h->slots_from_below |= 1u << sl;
+        }
     for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);  // captured steps lack the new copies
     h->graphs.clear();
     return GPE_OK;
