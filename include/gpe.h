@@ -210,6 +210,10 @@ gpe_status gpe_debug_inject(gpe_handle h, int32_t plane);
 int32_t gpe_variant_count(void);
 gpe_status gpe_variant_describe(int32_t variant, int32_t *tile_x, int32_t *tile_y, int32_t *stages,
                                 int32_t *min_blocks);
+/* Half-steps one launch of a variant advances: 1, or 2 for the variants that
+ * do a whole leapfrog step per pass over HBM (BCC2, real time only; they keep a
+ * second set of fields and refuse gpe_link_z).  0 for no such variant. */
+int32_t gpe_variant_half_steps(int32_t variant);
 
 /* Kernel launches the handle has issued (for accounting). */
 int64_t gpe_launch_count(gpe_handle h);

@@ -80,6 +80,39 @@ def test_fused_tiles_batch_trap_bit_exact(tile, prec):
     _run_real(Lattice.BCC2, prec, Kernel.FUSED, Potential.TRAP, SIZES, steps=4, tile=tile)
 
 
+def _two_step_tiles():
+    from vaikkari_gb300.gpe import variants
+    return [v["tile"] for v in variants() if v["half_steps"] == 2]
+
+
+@pytest.mark.parametrize("potential", [Potential.TRAP, Potential.ARRAY])
+@pytest.mark.parametrize("prec", [Precision.FP64, Precision.FP32])
+def test_two_step_variants_bit_exact(prec, potential):
+    """The variants that do both half-steps per launch (a second set of fields,
+    O' and E' from one pass) equal the one-half-step kernel's order bit for
+    bit: a batch of ragged sizes, odd and even step counts, and CUDA graphs of
+    an odd number of steps (the sets alternate inside a graph)."""
+    tiles = _two_step_tiles()
+    assert len(tiles) >= 1
+    for tile in tiles:
+        n = _run_real(Lattice.BCC2, prec, Kernel.FUSED, potential, SIZES, steps=3, tile=tile)
+        assert n <= 3 + 2 * len(SIZES) * 2 + 8   # one launch per step (plus packing)
+        _run_real(Lattice.BCC2, prec, Kernel.FUSED, potential, SIZES, steps=4, tile=tile, seed=5)
+    _run_real(Lattice.BCC2, prec, Kernel.FUSED, potential, SIZES, steps=23, tile=tiles[0], graph_steps=7, seed=9)
+
+
+def test_two_step_variant_refuses_imaginary_time_and_slabs():
+    from vaikkari_gb300.gpe import GpeError
+    tile = _two_step_tiles()[0]
+    inst = Instance(8, 8, 8, 0.3, 1e-3, 10.0)
+    with pytest.raises(GpeError):
+        Stepper([inst], lattice=Lattice.BCC2, kernel=Kernel.FUSED, mode=Mode.IMAGINARY, tile=tile)
+    st = Stepper([inst, inst], lattice=Lattice.BCC2, kernel=Kernel.FUSED, tile=tile)
+    with pytest.raises(GpeError):
+        st.link_z(0, 1)
+    st.close()
+
+
 @pytest.mark.parametrize("lattice", [Lattice.TETRA12, Lattice.BCC2])
 def test_trap_potential_plain_bit_exact(lattice):
     _run_real(lattice, Precision.FP32, Kernel.PLAIN, Potential.TRAP, SIZES[:3], steps=2)

@@ -63,7 +63,10 @@ struct gpe_handle_ {
     std::vector<InstDev> idev_host;
     InstDev *idev = nullptr;
     size_t field_elems = 0, v_elems = 0;
-    void *buf[2] = {nullptr, nullptr};  // even, odd (or psi and its ping-pong partner)
+    // even, odd (or psi and its ping-pong partner); the two-step variants add a
+    // second set (2, 3) and alternate between the sets every step
+    void *buf[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool two_step = false;
     void *vpot = nullptr;
     bool fused = false;
     int tile = 0, tx = 32, ty = 8, zchunk = 0, zcmax = 1;
@@ -83,7 +86,7 @@ struct gpe_handle_ {
     size_t staging_bytes = 0;
     cudaStream_t stream = nullptr;
     std::map<GraphKey, cudaGraphExec_t> graphs;
-    int parity = 0;      // imaginary time: which buffer holds psi
+    int parity = 0;      // imaginary time: which buffer holds psi; two-step: which set holds the fields
     int inject = -1;     // test hook for the bounded waits (gpe_debug_inject)
     std::vector<std::pair<int, int>> zlinks;  // (lower, upper): upper continues lower along +z
     uint32_t slots_from_above = 0, slots_from_below = 0;  // slots the stencil reads at z+1 / z-1
@@ -95,6 +98,13 @@ struct gpe_handle_ {
 namespace {
 
 size_t round_up(size_t v, size_t m) { return (v + m - 1) / m * m; }
+
+// The buffer that holds field f (0 even / psi, 1 odd / its partner) now.
+void *field_buf(const gpe_handle_ *h, int f)
+{
+    if (h->cfg.mode == GPE_IMAGINARY_TIME) return h->buf[f == 0 ? h->parity : 1 - h->parity];
+    return h->buf[(h->two_step ? 2 * h->parity : 0) + f];
+}
 
 gpe_status check_handle(gpe_handle h)
 {
@@ -167,7 +177,7 @@ gpe_status enqueue_halo(gpe_handle h, int field)
 {
     for (auto &lk : h->zlinks) {
         const InstDev &lo = h->idev_host[lk.first], &up = h->idev_host[lk.second];
-        char *f = (char *)h->buf[field];
+        char *f = (char *)field_buf(h, field);
         gpe_status st = copy_plane_slots(h, f, up.base, lo.base + lo.nz * lo.zstride, lo.plane, h->slots_from_below);
         if (st != GPE_OK) return st;
         st = copy_plane_slots(h, f, lo.base + (lo.nz + 1) * lo.zstride, up.base + up.zstride, lo.plane,
@@ -179,10 +189,35 @@ gpe_status enqueue_halo(gpe_handle h, int field)
 
 gpe_status enqueue_step_real(gpe_handle h)
 {
+    if (h->two_step) {
+        // both half-steps in one launch, from set `parity` into the other set
+        FusedLaunch l{};
+        l.precision = h->cfg.precision;
+        l.mode = GPE_REAL_TIME;
+        l.potential = h->cfg.potential;
+        l.tile = h->tile;
+        l.inst = h->idev;
+        l.items = h->items_dev;
+        l.num_items = int(h->items.size());
+        l.grid = h->grid;
+        l.vpot = h->vpot;
+        l.maps = h->maps;
+        l.zcmax = h->zcmax;
+        l.inject_skip_plane = h->inject;
+        l.src = h->parity;
+        l.out_e = h->buf[2 * (1 - h->parity)];
+        l.out_o = h->buf[2 * (1 - h->parity) + 1];
+        l.err = h->err;
+        l.num_instances = h->cfg.num_instances;
+        GPE_CUDA_TRY(launch_twostep(l, h->stream));
+        h->launches++;
+        h->parity = 1 - h->parity;
+        return GPE_OK;
+    }
     // odd <- even, then even <- odd (GPUGrossPitaevskii_BCC.cu:475-481)
     for (int half = 0; half < 2; half++) {
-        void *prev = h->buf[half == 0 ? 0 : 1];
-        void *next = h->buf[half == 0 ? 1 : 0];
+        void *prev = field_buf(h, half == 0 ? 0 : 1);
+        void *next = field_buf(h, half == 0 ? 1 : 0);
         if (h->fused) {
             FusedLaunch l{};
             l.precision = h->cfg.precision;
@@ -389,10 +424,10 @@ gpe_status run_steps(gpe_handle h, long long steps)
         GPE_CUDA_TRY(cudaGraphLaunch(it->second, h->stream));
         // account for the launches inside the graph and the parity it leaves
         const long long per_step = (h->cfg.mode == GPE_REAL_TIME)
-                                       ? (h->fused ? 2 : 2ll * h->cfg.num_instances)
+                                       ? (h->two_step ? 1 : (h->fused ? 2 : 2ll * h->cfg.num_instances))
                                        : (h->fused ? 1 : 4ll * h->cfg.num_instances);
         h->launches += per_step * G;
-        if (h->cfg.mode == GPE_IMAGINARY_TIME && (G % 2) == 1) h->parity = 1 - h->parity;
+        if ((h->cfg.mode == GPE_IMAGINARY_TIME || h->two_step) && (G % 2) == 1) h->parity = 1 - h->parity;
         done += G;
     }
     return enqueue_steps(h, steps - done);
@@ -403,8 +438,7 @@ void free_handle(gpe_handle h)
     if (!h) return;
     for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);
     cudaFree(h->idev);
-    cudaFree(h->buf[0]);
-    cudaFree(h->buf[1]);
+    for (void *b : h->buf) cudaFree(b);
     cudaFree(h->vpot);
     cudaFree(h->items_dev);
     cudaFree(h->item_begin_dev);
@@ -639,6 +673,18 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
     if (h->fused) {
         h->tile = cfg->tile > 0 && cfg->tile < fused_tile_count() ? cfg->tile : 0;
         fused_tile_shape(h->tile, &h->tx, &h->ty);
+        if (fused_half_steps(h->tile) == 2) {
+            if (cfg->mode != GPE_REAL_TIME) {
+                free_handle(h);
+                return fail(GPE_ERR_UNSUPPORTED, "gpe_create: this kernel variant advances whole real-time steps; "
+                                                 "imaginary time needs a half-step variant");
+            }
+            h->two_step = true;
+            for (int b = 2; b < 4; b++) {
+                GPE_CREATE_TRY(cudaMalloc(&h->buf[b], cbytes * h->field_elems));
+                GPE_CREATE_TRY(cudaMemsetAsync(h->buf[b], 0, cbytes * h->field_elems, h->stream));
+            }
+        }
         // Instances in decreasing size; each instance's items contiguous,
         // x fastest, then y, then z-chunk.
         std::vector<int> order(cfg->num_instances);
@@ -686,11 +732,15 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
             ranges[2 * i] = first[i];
             ranges[2 * i + 1] = first[i] + int(per[i].size());
         }
-        // TMA halo maps, one per instance and field.
+        // TMA maps: per instance and field (halo box, interior box); for the
+        // two-step variants per instance and buffer set (E box, O box).
         std::vector<CUtensorMap> maps(4 * cfg->num_instances);
         for (int i = 0; i < cfg->num_instances; i++)
             for (int f = 0; f < 2; f++) {
-                gpe_status ms = make_halo_map(&maps[4 * i + 2 * f], cfg->precision, h->idev_host[i], h->buf[f], h->tile);
+                gpe_status ms = h->two_step ? make_twostep_maps(&maps[4 * i + 2 * f], cfg->precision, h->idev_host[i],
+                                                                h->buf[2 * f], h->buf[2 * f + 1], h->tile)
+                                            : make_halo_map(&maps[4 * i + 2 * f], cfg->precision, h->idev_host[i],
+                                                            h->buf[f], h->tile);
                 if (ms != GPE_OK) {
                     free_handle(h);
                     return ms;
@@ -752,15 +802,12 @@ gpe_status gpe_upload(gpe_handle h, int32_t instance, const void *even, const vo
     const gpe_instance &in = h->inst[instance];
     const size_t vals = size_t(in.nx) * in.ny * in.nz * h->ns;
     const int prec = h->cfg.precision;
-    int target0 = 0;
-    if (h->cfg.mode == GPE_IMAGINARY_TIME) target0 = h->parity;
     const void *srcs[2] = {even, odd};
     for (int f = 0; f < 2; f++) {
         if (!srcs[f]) continue;
-        const int target = (f == 0) ? target0 : 1 - target0;
         st = upload_raw(h, srcs[f], vals * 2 * h->esize);
         if (st != GPE_OK) return st;
-        GPE_CUDA_TRY(launch_pack(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->staging, h->buf[target], 1,
+        GPE_CUDA_TRY(launch_pack(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->staging, field_buf(h, f), 1,
                                  1.0, h->stream));
         h->launches++;
         GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -787,12 +834,10 @@ gpe_status gpe_download(gpe_handle h, int32_t instance, void *even, void *odd)
     if (st != GPE_OK) return st;
     const gpe_instance &in = h->inst[instance];
     const size_t vals = size_t(in.nx) * in.ny * in.nz * h->ns;
-    int src0 = (h->cfg.mode == GPE_IMAGINARY_TIME) ? h->parity : 0;
     void *dsts[2] = {even, odd};
     for (int f = 0; f < 2; f++) {
         if (!dsts[f]) continue;
-        const int src = (f == 0) ? src0 : 1 - src0;
-        GPE_CUDA_TRY(launch_unpack(h->cfg.precision, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->buf[src],
+        GPE_CUDA_TRY(launch_unpack(h->cfg.precision, h->idev, instance, in.nx, in.ny, in.nz, h->ns, field_buf(h, f),
                                    h->staging, nullptr, h->stream));
         h->launches++;
         GPE_CUDA_TRY(cudaMemcpyAsync(dsts[f], h->staging, vals * 2 * h->esize, cudaMemcpyDeviceToHost, h->stream));
@@ -837,9 +882,8 @@ gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
     if (!out || (field != 0 && field != 1)) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_observables_get: bad arguments");
-    const int src = (h->cfg.mode == GPE_IMAGINARY_TIME) ? (field == 0 ? h->parity : 1 - h->parity) : field;
     for (int i = 0; i < h->cfg.num_instances; i++) {
-        st = enqueue_observables(h, h->buf[src], i, h->obs_sums + 6 * i);
+        st = enqueue_observables(h, field_buf(h, field), i, h->obs_sums + 6 * i);
         if (st != GPE_OK) return st;
     }
     std::vector<double> sums(6 * h->cfg.num_instances);
@@ -947,8 +991,7 @@ gpe_status gpe_volume_map(gpe_handle h, int32_t instance, int32_t field, double 
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_volume_map: bad arguments");
     const gpe_instance &in = h->inst[instance];
     const long long total = (long long)(in.nx + 2) * (in.ny + 2) * (in.nz + 2);
-    const int src = (h->cfg.mode == GPE_IMAGINARY_TIME) ? (field == 0 ? h->parity : 1 - h->parity) : field;
-    GPE_CUDA_TRY(launch_volume(h->cfg.precision, h->idev, instance, h->buf[src], unit, reference_sum ? 1 : 0,
+    GPE_CUDA_TRY(launch_volume(h->cfg.precision, h->idev, instance, field_buf(h, field), unit, reference_sum ? 1 : 0,
                                (uint16_t *)h->staging, total, h->stream));
     h->launches++;
     GPE_CUDA_TRY(cudaMemcpyAsync(out, h->staging, size_t(total) * 2, cudaMemcpyDeviceToHost, h->stream));
@@ -965,8 +1008,7 @@ gpe_status gpe_slice_rgb(gpe_handle h, int32_t instance, int32_t field, int32_t 
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_slice_rgb: bad arguments");
     const gpe_instance &in = h->inst[instance];
     const int total = (in.nx + 2) * (in.ny + 2);
-    const int src = (h->cfg.mode == GPE_IMAGINARY_TIME) ? (field == 0 ? h->parity : 1 - h->parity) : field;
-    GPE_CUDA_TRY(launch_slice(h->cfg.precision, h->idev, instance, h->buf[src], z_padded, slot, gain,
+    GPE_CUDA_TRY(launch_slice(h->cfg.precision, h->idev, instance, field_buf(h, field), z_padded, slot, gain,
                               (uint8_t *)h->staging, total, h->stream));
     h->launches++;
     GPE_CUDA_TRY(cudaMemcpyAsync(out, h->staging, size_t(total) * 3, cudaMemcpyDeviceToHost, h->stream));
@@ -980,6 +1022,9 @@ gpe_status gpe_link_z(gpe_handle h, int32_t lower, int32_t upper)
     if (h->cfg.mode != GPE_REAL_TIME)
         return fail(GPE_ERR_UNSUPPORTED, "gpe_link_z: slabs are supported in real time (imaginary time "
                                          "normalises each instance on its own)");
+    if (h->two_step)
+        return fail(GPE_ERR_UNSUPPORTED, "gpe_link_z: slabs exchange halos between half-steps; use a kernel "
+                                         "variant that advances a half-step per launch");
     const int n = h->cfg.num_instances;
     if (lower < 0 || lower >= n || upper < 0 || upper >= n || lower == upper)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_link_z: bad instance indices");
@@ -1003,6 +1048,11 @@ gpe_status gpe_link_z(gpe_handle h, int32_t lower, int32_t upper)
 }
 
 int32_t gpe_variant_count(void) { return fused_tile_count(); }
+
+int32_t gpe_variant_half_steps(int32_t variant)
+{
+    return (variant >= 0 && variant < fused_tile_count()) ? fused_half_steps(variant) : 0;
+}
 
 gpe_status gpe_variant_describe(int32_t variant, int32_t *tile_x, int32_t *tile_y, int32_t *stages,
                                 int32_t *min_blocks)

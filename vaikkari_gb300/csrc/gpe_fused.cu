@@ -450,6 +450,371 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
     }
 }
 
+// ---- Both half-steps of a leapfrog step in one pass --------------------------
+// Reads the even field E and odd field O of one buffer set and writes
+// O' = O - i H(E) and E' = E - i H(O') into the other set, so each step moves
+// 32 instead of 48 bytes per vertex (FP32).  Per work item (tile TX x TY of
+// one instance, planes z0..z1-1) the consumer threads cover the tile plus a
+// one-block ring, (TX+2) x (TY+2) columns:
+//   phase A  every thread computes O'(p) of its column from the E stencil (E box:
+//            tile plus a 2-block ring) and O(p) (O box: tile plus a 1-block
+//            ring), exactly as the one-half-step kernel does, and leaves O'(p)
+//            in a shared plane buffer; O' is zero outside the instance;
+//   phase B  after a barrier of the consumer warps the tile's threads compute
+//            E'(p-1) from the O' stencil in that buffer and their own E(p-1)
+//            carried from phase A.
+// Planes z0-1 and z1 of O' are computed again here (the neighbouring items
+// compute them too) so that no CTA waits for another.  The sums follow the
+// same order as the one-half-step kernel, so the result is bit-identical to two
+// of its launches.
+// Packed FP32 pairs (add / mul / fma .rn.f32x2, sm_100 and later): each lane is
+// the IEEE operation of that lane, so a complex sum, or a complex times a real
+// factor, rounds exactly as the two scalar operations do, in one instruction.
+__device__ __forceinline__ float2 f2_add(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "add.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "mul.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, c, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "mov.b64 c, {%6, %7};\n\tfma.rn.f32x2 d, a, b, c;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
+}
+
+// Complex sums and dt*H psi (gpe_device.cuh's hpsi, two classes) with the same
+// rounded operations, packed for FP32.
+template <typename T> struct Ops;
+template <> struct Ops<double> {
+    static __device__ __forceinline__ double2 add(double2 a, double2 b) { return c_add<double>(a, b); }
+    static __device__ __forceinline__ void hpsi(double2 p, const double2 *S, const double *L, double L0, double vdt,
+                                                double gdt, double &hx, double &hy, double &nrm)
+    {
+        gpe::hpsi<double, 2>(p, S, L, L0, vdt, gdt, hx, hy, nrm);
+    }
+};
+template <> struct Ops<float> {
+    static __device__ __forceinline__ float2 add(float2 a, float2 b) { return f2_add(a, b); }
+    static __device__ __forceinline__ void hpsi(float2 p, const float2 *S, const float *L, float L0, float vdt,
+                                                float gdt, float &hx, float &hy, float &nrm)
+    {
+        nrm = d_fma(p.x, p.x, d_mul(p.y, p.y));
+        const float c = d_fma(gdt, nrm, d_add(L0, vdt));
+        float2 a = f2_mul(make_float2(L[0], L[0]), S[0]);
+        a = f2_fma(make_float2(L[1], L[1]), S[1], a);
+        const float2 h = f2_fma(make_float2(c, c), p, a);
+        hx = h.x;
+        hy = h.y;
+    }
+};
+
+template <typename T, int TX, int TY>
+struct TwoStepShape {
+    using T2 = typename Cplx<T>::type;
+    static constexpr int EX = TX + 2, EY = TY + 2;  // thread box
+    static constexpr int NT = ((EX * EY + 31) / 32) * 32;
+    static constexpr int NTHREADS = NT + 32;
+    static constexpr int BW = TX + 4;  // box columns x0-2 .. x0+TX+1
+    static constexpr int EH = TY + 4;  // E box rows y0-2 .. y0+TY+1
+    static constexpr int OH = TY + 2;  // O box rows y0-1 .. y0+TY
+    static constexpr int E_BYTES = 2 * BW * EH * (int)sizeof(T2);
+    static constexpr int O_BYTES = 2 * BW * OH * (int)sizeof(T2);
+    static constexpr int O_OFF = ((E_BYTES + 127) / 128) * 128;
+    static constexpr int STAGE_BYTES = ((O_OFF + O_BYTES + 127) / 128) * 128;
+    static constexpr int NEW_SLOT = EX * EY;
+    static constexpr int NEW_BYTES = ((2 * NEW_SLOT * (int)sizeof(T2) + 127) / 128) * 128;
+    static constexpr int XE = (int)sizeof(T2) / 8;
+};
+
+template <typename T, int TX, int TY, int STAGES>
+int twostep_smem_bytes(int zcmax)
+{
+    using S = TwoStepShape<T, TX, TY>;
+    return STAGES * S::STAGE_BYTES + 2 * S::NEW_BYTES + 128 + 16 * STAGES + 2 * (zcmax + 2) * (int)sizeof(T) + 16;
+}
+
+struct TwoStepArgs {
+    const InstDev *__restrict__ inst;
+    const WorkItem *__restrict__ items;
+    const CUtensorMap *maps;  // [instance][set][E box, O box]
+    int set;                  // buffer set read (0 or 1)
+    int zcmax;
+    void *out_e, *out_o;      // field arenas of the other set
+    const void *vpot;
+    int *err;
+    int inject_skip_plane;
+};
+
+// Barrier of threads 0..n-1 on barrier id, returning whether any of them passed v.
+__device__ __forceinline__ bool bar_any(int id, int n, bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred q, p;\n\t"
+        "setp.ne.u32 q, %1, 0;\n\t"
+        "bar.red.or.pred p, %2, %3, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"(v ? 1u : 0u), "r"(id), "r"(n)
+        : "memory");
+    return r != 0;
+}
+
+template <typename T, int TX, int TY, int POT, int STAGES, int MINB>
+__global__ void __launch_bounds__(TwoStepShape<T, TX, TY>::NTHREADS, MinBlocks<T, MINB>::value)
+    twostep_bcc2_kernel(const TwoStepArgs a)
+{
+    using S = TwoStepShape<T, TX, TY>;
+    using T2 = typename S::T2;
+    constexpr int NT = S::NT;
+    constexpr int NWARPS = S::NTHREADS / 32;
+    extern __shared__ unsigned char dyn_smem[];
+    const uint32_t raw = smem_u32(dyn_smem);
+    const uint32_t base = (raw + 127u) & ~127u;
+    unsigned char *const gbase = dyn_smem + (base - raw);
+    T2 *const newbuf = (T2 *)(gbase + STAGES * S::STAGE_BYTES);  // two O' planes
+    const uint32_t full = base + STAGES * S::STAGE_BYTES + 2 * S::NEW_BYTES;
+    const uint32_t empty = full + 8 * STAGES;
+    T *const ztab = (T *)(gbase + STAGES * S::STAGE_BYTES + 2 * S::NEW_BYTES + 16 * STAGES);
+    __shared__ int abort_flag;
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int it = blockIdx.x;
+    const WorkItem w = a.items[it];
+    const InstDev &d = a.inst[w.inst];
+    const int zl = w.z1 - w.z0;
+    const int nplanes = zl + 4;  // E planes z0-2 .. z1+1
+    const int nz = d.nz;
+
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int st = 0; st < STAGES; st++) {
+            mbar_init(full + 8 * st, 1);
+            mbar_init(empty + 8 * st, NT / 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (POT == GPE_POTENTIAL_TRAP) {
+        // z-term of the trap for planes z0-1 .. z1 (clamped into the instance), both slots
+        const T *tz = (const T *)a.vpot + d.vbase + 2ll * d.nx + 2ll * d.ny;
+        const int zn = zl + 2;
+        for (int i = tid; i < 2 * zn; i += S::NTHREADS) {
+            const int sl = i / zn;
+            const int z = min(max(w.z0 - 1 + (i - sl * zn), 0), nz - 1);
+            ztab[i] = tz[sl * nz + z];
+        }
+    }
+    __syncthreads();
+
+    if (warp == NWARPS - 1) {
+        // ---- producer warp: E(q) and O(q-1) for q = z0-2 .. z1+1 -------------
+        if (lane == 0) {
+            const CUtensorMap *emap = a.maps + 4 * w.inst + 2 * a.set;
+            const CUtensorMap *omap = emap + 1;
+            int issued = 0;
+            for (int k = 0; k < nplanes; k++) {
+                const int st = k % STAGES;
+                if (k >= STAGES) {
+                    bool ok = mbar_try_wait(empty + 8 * st, ((k / STAGES) - 1) & 1);
+                    const uint64_t t0 = global_ns();
+                    while (!ok && !*(volatile int *)&abort_flag && global_ns() - t0 <= kWaitLimitNs)
+                        ok = mbar_try_wait(empty + 8 * st, ((k / STAGES) - 1) & 1);
+                    if (!ok) {
+                        atomicExch(a.err, kErrTimeout);
+                        abort_flag = 1;
+                        break;
+                    }
+                }
+                if (a.inject_skip_plane == k && it == 0) {
+                    issued = k;
+                    break;
+                }
+                const bool with_o = k >= 2;
+                mbar_arrive_expect_tx(full + 8 * st, S::E_BYTES + (with_o ? S::O_BYTES : 0));
+                // padded coordinates: x0-2 -> x0; E rows from y0-2 -> y0-1, O rows from
+                // y0-1 -> y0; plane q = z0-2+k -> z0-1+k
+                tma_load_4d(base + st * S::STAGE_BYTES, emap, w.x0 * S::XE, w.y0 - 1, 0, w.z0 - 1 + k,
+                            full + 8 * st);
+                if (with_o)
+                    tma_load_4d(base + st * S::STAGE_BYTES + S::O_OFF, omap, w.x0 * S::XE, w.y0, 0, w.z0 - 2 + k,
+                                full + 8 * st);
+                issued = k + 1;
+            }
+            if (abort_flag) {
+                for (int k = (issued > STAGES ? issued - STAGES : 0); k < issued; k++)
+                    mbar_wait_bounded(full + 8 * (k % STAGES), (k / STAGES) & 1);
+            }
+        }
+    } else {
+        // ---- consumer warps ----------------------------------------------
+        const bool in_box = tid < S::EX * S::EY;
+        const int ex = in_box ? tid % S::EX : 0, ey = in_box ? tid / S::EX : 0;
+        const int x = w.x0 - 1 + ex, y = w.y0 - 1 + ey;
+        const bool inside = in_box && x >= 0 && x < d.nx && y >= 0 && y < d.ny;
+        const bool tile = inside && ex >= 1 && ex <= TX && ey >= 1 && ey <= TY;
+        const long long zstride = d.zstride, plane = d.plane;
+        const long long col = inside ? field_index(d, 0, x, y, 0) : 0;
+        const long long voff = d.vbase - d.base;
+        const T Lw[2] = {T(d.Lc[0]), T(d.Lc[1])};
+        const T L0 = T(d.L0), gdt = T(d.gdt);
+        T2 *__restrict__ oute = (T2 *)a.out_e;
+        T2 *__restrict__ outo = (T2 *)a.out_o;
+        const T *__restrict__ vpot = (const T *)a.vpot;
+        T vxy0 = T(0), vxy1 = T(0);
+        if (POT == GPE_POTENTIAL_TRAP && inside) {
+            const T *tx_ = vpot + d.vbase;
+            const T *ty_ = tx_ + 2ll * d.nx;
+            vxy0 = d_add(tx_[x], ty_[y]);
+            vxy1 = d_add(tx_[d.nx + x], ty_[d.ny + y]);
+        }
+        auto vdt_at = [&](int slot, int z) -> T {  // V*dt at (x, y, z), z in z0-1 .. z1
+            if (POT == GPE_POTENTIAL_TRAP) return d_add(slot ? vxy1 : vxy0, ztab[slot * (zl + 2) + z - (w.z0 - 1)]);
+            return vpot[col + z * zstride + slot * plane + voff];
+        };
+
+        const T2 zero2 = {T(0), T(0)};
+        // phase A carries: E at this column (see the one-half-step kernel)
+        T2 cm = zero2, cc = zero2, bm = zero2, bc = zero2, axyC = zero2, axyB = zero2, bBp = zero2, sd0 = zero2,
+           bCc = zero2;
+        // phase B carries: O' at this column
+        T2 pcm = zero2, pcc = zero2, pbm = zero2, pbc = zero2, paxyC = zero2, paxyB = zero2, pbBp = zero2,
+           psd0 = zero2, pbCc = zero2;
+        const int lx = ex + 1, ly = ey + 1;  // E box position of the column
+        for (int k = 0; k < nplanes; k++) {
+            const int st = k % STAGES;
+            // A thread whose wait runs out still reaches the consumers' barrier
+            // below, where all of them learn of it and stop together.
+            const bool got = mbar_wait_bounded(full + 8 * st, (k / STAGES) & 1);
+            if (!got) {
+                atomicExch(a.err, kErrTimeout);
+                abort_flag = 1;
+            }
+            const unsigned char *sb = gbase + st * S::STAGE_BYTES;
+            const T2 *Ep = (const T2 *)sb;
+            const T2 *EB = Ep + S::BW * S::EH;
+            auto at = [&](const T2 *P, int dx, int dy) -> T2 { return P[(ly + dy) * S::BW + lx + dx]; };
+            const T2 qC = at(Ep, 0, 0), qCxm = at(Ep, -1, 0), qCxp = at(Ep, 1, 0), qCym = at(Ep, 0, -1),
+                     qCyp = at(Ep, 0, 1), qCpp = at(Ep, 1, 1);
+            const T2 qB = at(EB, 0, 0), qBxm = at(EB, -1, 0), qBxp = at(EB, 1, 0), qBym = at(EB, 0, -1),
+                     qByp = at(EB, 0, 1), qBmm = at(EB, -1, -1);
+            T2 o0 = zero2, o1 = zero2;  // O(p) at the column, p = q-1
+            if (k >= 2) {
+                const T2 *Op = (const T2 *)(sb + S::O_OFF);
+                o0 = Op[ey * S::BW + lx];
+                o1 = Op[S::BW * S::OH + ey * S::BW + lx];
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(empty + 8 * st);
+
+            // ---- phase A: O'(p), p = z0-3+k, from E planes p-1, p, p+1
+            const T2 bBq = Ops<T>::add(Ops<T>::add(qBmm, qBym), Ops<T>::add(qBxm, qB));
+            const T2 bCq = Ops<T>::add(Ops<T>::add(qC, qCxp), Ops<T>::add(qCyp, qCpp));
+            const T2 axyCq = Ops<T>::add(Ops<T>::add(qCxm, qCxp), Ops<T>::add(qCym, qCyp));
+            const T2 axyBq = Ops<T>::add(Ops<T>::add(qBxm, qBxp), Ops<T>::add(qBym, qByp));
+            const T2 sd0q = Ops<T>::add(bBp, bBq);
+            const int p = w.z0 - 3 + k;
+            T2 n0 = zero2, n1 = zero2;  // O'(p) of the column; zero outside the instance
+            if (k >= 2 && inside && p >= 0 && p < nz) {
+                T2 S2[2];
+                T hx, hy, nrm;
+                S2[0] = sd0;
+                S2[1] = Ops<T>::add(Ops<T>::add(cm, qC), axyC);
+                Ops<T>::hpsi(cc, S2, Lw, L0, vdt_at(0, p), gdt, hx, hy, nrm);
+                n0 = integrate<T, 0>(o0, cc, hx, hy);
+                S2[0] = Ops<T>::add(bCc, bCq);
+                S2[1] = Ops<T>::add(Ops<T>::add(bm, qB), axyB);
+                Ops<T>::hpsi(bc, S2, Lw, L0, vdt_at(1, p), gdt, hx, hy, nrm);
+                n1 = integrate<T, 0>(o1, bc, hx, hy);
+                if (got && tile && p >= w.z0 && p < w.z1) {
+                    const long long i0 = col + p * zstride;
+                    outo[i0] = n0;
+                    outo[i0 + plane] = n1;
+                }
+            }
+            const T2 eown0 = cm, eown1 = bm;  // E(p-1) of the column, the target of phase B
+            cm = cc;
+            cc = qC;
+            bm = bc;
+            bc = qB;
+            axyC = axyCq;
+            axyB = axyBq;
+            bBp = bBq;
+            sd0 = sd0q;
+            bCc = bCq;
+
+            // ---- hand O'(p) to the tile
+            T2 *nb = newbuf + (k & 1) * (S::NEW_BYTES / (int)sizeof(T2));
+            if (in_box) {
+                nb[ey * S::EX + ex] = n0;
+                nb[S::NEW_SLOT + ey * S::EX + ex] = n1;
+            }
+            if (bar_any(1, NT, !got)) break;  // consumer warps only
+
+            // ---- phase B: E'(p-1) from O' planes p-2, p-1, p (read: plane p)
+            if (k >= 2 && ex >= 1 && ex <= TX && ey >= 1 && ey <= TY && in_box) {
+                auto nat = [&](int sl, int dx, int dy) -> T2 {
+                    return nb[sl * S::NEW_SLOT + (ey + dy) * S::EX + ex + dx];
+                };
+                const T2 rC = nat(0, 0, 0), rCxm = nat(0, -1, 0), rCxp = nat(0, 1, 0), rCym = nat(0, 0, -1),
+                         rCyp = nat(0, 0, 1), rCpp = nat(0, 1, 1);
+                const T2 rB = nat(1, 0, 0), rBxm = nat(1, -1, 0), rBxp = nat(1, 1, 0), rBym = nat(1, 0, -1),
+                         rByp = nat(1, 0, 1), rBmm = nat(1, -1, -1);
+                const T2 pbBq = Ops<T>::add(Ops<T>::add(rBmm, rBym), Ops<T>::add(rBxm, rB));
+                const T2 pbCq = Ops<T>::add(Ops<T>::add(rC, rCxp), Ops<T>::add(rCyp, rCpp));
+                const T2 paxyCq = Ops<T>::add(Ops<T>::add(rCxm, rCxp), Ops<T>::add(rCym, rCyp));
+                const T2 paxyBq = Ops<T>::add(Ops<T>::add(rBxm, rBxp), Ops<T>::add(rBym, rByp));
+                const T2 psd0q = Ops<T>::add(pbBp, pbBq);
+                const int pz = p - 1;
+                if (k >= 4 && inside) {  // pz in z0 .. z1-1
+                    T2 S2[2];
+                    T hx, hy, nrm;
+                    S2[0] = psd0;
+                    S2[1] = Ops<T>::add(Ops<T>::add(pcm, rC), paxyC);
+                    Ops<T>::hpsi(pcc, S2, Lw, L0, vdt_at(0, pz), gdt, hx, hy, nrm);
+                    const T2 e0 = integrate<T, 0>(eown0, pcc, hx, hy);
+                    S2[0] = Ops<T>::add(pbCc, pbCq);
+                    S2[1] = Ops<T>::add(Ops<T>::add(pbm, rB), paxyB);
+                    Ops<T>::hpsi(pbc, S2, Lw, L0, vdt_at(1, pz), gdt, hx, hy, nrm);
+                    const T2 e1 = integrate<T, 0>(eown1, pbc, hx, hy);
+                    const long long i0 = col + pz * zstride;
+                    oute[i0] = e0;
+                    oute[i0 + plane] = e1;
+                }
+                pcm = pcc;
+                pcc = rC;
+                pbm = pbc;
+                pbc = rB;
+                paxyC = paxyCq;
+                paxyB = paxyBq;
+                pbBp = pbBq;
+                psd0 = psd0q;
+                pbCc = pbCq;
+            }
+        }
+    }
+}
+
+
+
 // Kernel variants: tile (TX, TY), pipeline depth (STAGES planes) and the
 // minimum resident CTAs per SM asked of the register allocator (MINB).  Index 0
 // is the default; the autotuner picks among them per workload.
@@ -461,21 +826,37 @@ static const Variant kVariants[] = {
     {16, 8, 6, 6}, {32, 2, 8, 8}, {16, 16, 4, 3}, {32, 8, 4, 2}, {64, 4, 6, 2}, {32, 16, 4, 1},
 };
 
-int fused_tile_count() { return int(sizeof(kVariants) / sizeof(kVariants[0])); }
+// Variants that advance a whole leapfrog step per launch (twostep_bcc2_kernel):
+// output tile (TX, TY), pipeline depth, resident CTAs asked for.  Their indices
+// follow the one-half-step variants.
+static const Variant kTwoVariants[] = {
+    {32, 12, 6, 1}, {32, 4, 4, 2}, {32, 6, 3, 2}, {32, 12, 8, 1}, {32, 8, 3, 1}, {32, 10, 6, 1},
+    {32, 10, 3, 1}, {32, 12, 3, 1},
+};
+constexpr int kOneCount = int(sizeof(kVariants) / sizeof(kVariants[0]));
+constexpr int kTwoCount = int(sizeof(kTwoVariants) / sizeof(kTwoVariants[0]));
+
+static const Variant &variant_of(int tile)
+{
+    if (tile < 0 || tile >= kOneCount + kTwoCount) tile = 0;
+    return tile < kOneCount ? kVariants[tile] : kTwoVariants[tile - kOneCount];
+}
+
+int fused_tile_count() { return kOneCount + kTwoCount; }
+int fused_half_steps(int tile) { return (tile >= kOneCount && tile < kOneCount + kTwoCount) ? 2 : 1; }
 void fused_tile_shape(int tile, int *tx, int *ty)
 {
-    if (tile < 0 || tile >= fused_tile_count()) tile = 0;
-    *tx = kVariants[tile].tx;
-    *ty = kVariants[tile].ty;
+    *tx = variant_of(tile).tx;
+    *ty = variant_of(tile).ty;
 }
 
 void fused_variant(int tile, int *tx, int *ty, int *stages, int *minb)
 {
-    if (tile < 0 || tile >= fused_tile_count()) tile = 0;
-    *tx = kVariants[tile].tx;
-    *ty = kVariants[tile].ty;
-    *stages = kVariants[tile].stages;
-    *minb = kVariants[tile].minb;
+    const Variant &v = variant_of(tile);
+    *tx = v.tx;
+    *ty = v.ty;
+    *stages = v.stages;
+    *minb = v.minb;
 }
 
 int fused_box_bytes(int precision, int tile)
@@ -526,6 +907,103 @@ gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *f
             return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     }
     return GPE_OK;
+}
+
+// The two-step kernel's maps of one buffer set of one instance: out_map[0] the
+// E box (tile plus 2 columns either side, 2 rows either side), out_map[1] the O
+// box (tile plus 2 columns, 1 row either side); both slots, one plane.
+gpe_status make_twostep_maps(void *out_map, int precision, const InstDev &d, void *even_arena, void *odd_arena,
+                             int tile)
+{
+    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+        return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    Encode encode = (Encode)fn;
+    int tx, ty;
+    fused_tile_shape(tile, &tx, &ty);
+    const int csize = precision == GPE_FP64 ? 16 : 8;
+    const int xe = csize / 8;
+    const cuuint64_t dims[4] = {(cuuint64_t)d.px * xe, (cuuint64_t)d.py, 2, (cuuint64_t)d.nz + 2};
+    const cuuint64_t strides[3] = {(cuuint64_t)d.px * csize, (cuuint64_t)d.plane * csize,
+                                   (cuuint64_t)d.zstride * csize};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    void *arenas[2] = {even_arena, odd_arena};
+    const cuuint32_t boxes[2][4] = {{(cuuint32_t)(tx + 4) * xe, (cuuint32_t)(ty + 4), 2, 1},
+                                    {(cuuint32_t)(tx + 4) * xe, (cuuint32_t)(ty + 2), 2, 1}};
+    for (int b = 0; b < 2; b++) {
+        void *gaddr = (char *)arenas[b] + (size_t)d.base * csize;
+        CUresult r = encode((CUtensorMap *)out_map + b, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, gaddr, dims, strides,
+                            boxes[b], estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    }
+    return GPE_OK;
+}
+
+// FP64 stages are twice as large: half as many (at least 2) fit the same memory.
+template <typename T, int ST> struct TwoStages {
+    static constexpr int value = sizeof(T) == 8 ? (ST / 2 > 2 ? ST / 2 : 2) : ST;
+};
+
+template <typename T, int TX, int TY, int ST0, int MB, int POT>
+static cudaError_t launch_two(const TwoStepArgs &a, int grid, cudaStream_t s)
+{
+    constexpr int ST = TwoStages<T, ST0>::value;
+    const int bytes = twostep_smem_bytes<T, TX, TY, ST>(a.zcmax);
+    auto kern = twostep_bcc2_kernel<T, TX, TY, POT, ST, MB>;
+    static int allowed = 48 * 1024;
+    if (bytes > allowed) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        allowed = bytes;
+    }
+    kern<<<grid, TwoStepShape<T, TX, TY>::NTHREADS, bytes, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T, int TX, int TY, int ST, int MB>
+static cudaError_t launch_two_pot(const FusedLaunch &l, const TwoStepArgs &a, cudaStream_t s)
+{
+    if (l.potential == GPE_POTENTIAL_ARRAY) return launch_two<T, TX, TY, ST, MB, 0>(a, l.grid, s);
+    return launch_two<T, TX, TY, ST, MB, 1>(a, l.grid, s);
+}
+
+template <typename T>
+static cudaError_t launch_two_tile(const FusedLaunch &l, const TwoStepArgs &a, cudaStream_t s)
+{
+    switch (l.tile - kOneCount) {  // must list kTwoVariants in order
+    case 1: return launch_two_pot<T, 32, 4, 4, 2>(l, a, s);
+    case 2: return launch_two_pot<T, 32, 6, 3, 2>(l, a, s);
+    case 3: return launch_two_pot<T, 32, 12, 8, 1>(l, a, s);
+    case 4: return launch_two_pot<T, 32, 8, 3, 1>(l, a, s);
+    case 5: return launch_two_pot<T, 32, 10, 6, 1>(l, a, s);
+    case 6: return launch_two_pot<T, 32, 10, 3, 1>(l, a, s);
+    case 7: return launch_two_pot<T, 32, 12, 3, 1>(l, a, s);
+    default: return launch_two_pot<T, 32, 12, 6, 1>(l, a, s);
+    }
+}
+
+cudaError_t launch_twostep(const FusedLaunch &l, cudaStream_t s)
+{
+    TwoStepArgs a;
+    a.inst = l.inst;
+    a.items = l.items;
+    a.maps = (const CUtensorMap *)l.maps;
+    a.set = l.src;
+    a.zcmax = l.zcmax;
+    a.out_e = l.out_e;
+    a.out_o = l.out_o;
+    a.vpot = l.vpot;
+    a.err = l.err;
+    a.inject_skip_plane = l.inject_skip_plane;
+    if (l.precision == GPE_FP64) return launch_two_tile<double>(l, a, s);
+    return launch_two_tile<float>(l, a, s);
 }
 
 template <typename T, int TX, int TY, int ST, int MB, int MODE, int POT>

@@ -72,8 +72,15 @@ struct FusedLaunch {
     double tol;
     long long step;       // host-side step index (for convergence bookkeeping)
     const long long *step_dev;  // device step counter (graphs)
+    void *out_e, *out_o;  // two-step variants: the other buffer set (src = the set read)
 };
 cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s);
+// A whole leapfrog step (both half-steps) per launch: reads set l.src through
+// l.maps ([instance][set][E box, O box]), writes l.out_e / l.out_o.
+cudaError_t launch_twostep(const FusedLaunch &l, cudaStream_t s);
+int fused_half_steps(int tile);  // 2 for the two-step variants, else 1
+gpe_status make_twostep_maps(void *out_map, int precision, const InstDev &d, void *even_arena, void *odd_arena,
+                             int tile);
 int fused_tile_count();
 void fused_tile_shape(int tile, int *tx, int *ty);
 void fused_variant(int tile, int *tx, int *ty, int *stages, int *minb);
