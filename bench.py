@@ -665,6 +665,46 @@ def run_relax(args):
     return 0
 
 
+def run_production(args):
+    """The reference's main() at production size (GPUGrossPitaevskii_BCC.cu:501-555),
+    kappa 20, g 5000, on the GPU: both relaxations, the set-up of integrateInTime at
+    main()'s block scale, and `--production-iters` iterations of the solver call in
+    FP64 (the reference's arithmetic) and FP32.  The unit is one value update (one
+    of the 12 values of a block, one leapfrog step)."""
+    from vaikkari_gb300.gpe import Precision, VortexState
+    unit = "value-updates/s"
+    t0 = time.perf_counter()
+    s0 = VortexState.create(20, 5000.0, 0.0, 15.0, 35.0, 0.2, 0.2)
+    r0 = s0.relax(10000)
+    d0 = s0.describe(1e-5)
+    s = VortexState.create(20, 5000.0, d0["min_r"], d0["max_r"], d0["max_z"], 0.03, 0.03)
+    s.initialize(s0)
+    r1 = s.relax(10000)
+    relax_s = time.perf_counter() - t0
+    d = s.describe(1e-5)
+    bs, mr, mz = d["block_scale"], d["max_r"], d["max_z"]
+    lo, hi = (-mr, -mr, -mz), (mr, mr, mz)
+    t1 = time.perf_counter()
+    res, _, _, _ = s.setup(bs, lo, hi)
+    setup_s = time.perf_counter() - t1
+    its = max(1, args.production_iters)
+    rates = {}
+    for name, prec in (("fp64", Precision.FP64), ("fp32", Precision.FP32)):
+        r, obs, _, _ = s.integrate_in_time(bs, lo, hi, 1.0, its, precision=prec)
+        rates[name] = {"value": res["values"] * its * res["steps_per_iteration"] / (r["device_ms"] * 1e-3),
+                       "device_ms": r["device_ms"], "energy": [o["energy"] for o in obs]}
+    line = {"metric": unit, "value": rates["fp64"]["value"], "unit": unit, "n_gpus": 1, "dtype": "f64",
+            "data": "synthetic", "higher_is_better": True,
+            "config": {"workload": "production_main", "kappa": 20, "g": 5000.0, "block_scale": bs,
+                       "blocks": [res["xsize"], res["ysize"], res["zsize"]], "values": res["values"],
+                       "steps_per_iteration": res["steps_per_iteration"], "iterations_timed": its},
+            "relax": {"seconds": relax_s, "device_ms": [r0["device_ms"], r1["device_ms"]],
+                      "iterations": [r0["iterations"], r1["iterations"]]},
+            "setup_seconds": setup_s, "fp64": rates["fp64"], "fp32": rates["fp32"]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def _tmp_save(v):
     import tempfile
     fd, path = tempfile.mkstemp(suffix=".dat")
@@ -678,6 +718,8 @@ def run_workload(args):
     name = args.workload
     if name == "relax":
         return run_relax(args)
+    if name == "production":
+        return run_production(args)
     if name == "config1":
         line = run_config_realtime("config1_bcc2_32_realtime_1000", [workloads.config1()], [1000], tile=args.tile)
     elif name == "config2":
@@ -709,8 +751,9 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--workload", default="batch64",
-                    help="batch64 (the headline), config1/config2/config3/config5 (accuracy cases) or relax "
-                         "(the vortex relaxation)")
+                    help="batch64 (the headline), config1/config2/config3/config5 (accuracy cases), relax "
+                         "(the vortex relaxation) or production (main() at production size)")
+    ap.add_argument("--production-iters", type=int, default=2)
     ap.add_argument("--relax-batch", type=int, default=19)
     ap.add_argument("--relax-batch-iters", type=int, default=2000)
     args = ap.parse_args()
