@@ -176,6 +176,65 @@ template <typename T, int MINB> struct MinBlocks {
     static constexpr int value = sizeof(T) == 8 ? (MINB + 1) / 2 : MINB;
 };
 
+// Packed FP32 pairs (add / mul / fma .rn.f32x2, sm_100 and later): each lane is
+// the IEEE operation of that lane, so a complex sum, or a complex times a real
+// factor, rounds exactly as the two scalar operations do, in one instruction.
+__device__ __forceinline__ float2 f2_add(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "add.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "mul.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, c, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "mov.b64 c, {%6, %7};\n\tfma.rn.f32x2 d, a, b, c;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
+}
+
+// Complex sums and dt*H psi (gpe_device.cuh's hpsi, two classes) with the same
+// rounded operations, packed for FP32.
+template <typename T> struct Ops;
+template <> struct Ops<double> {
+    static __device__ __forceinline__ double2 add(double2 a, double2 b) { return c_add<double>(a, b); }
+    static __device__ __forceinline__ void hpsi(double2 p, const double2 *S, const double *L, double L0, double vdt,
+                                                double gdt, double &hx, double &hy, double &nrm)
+    {
+        gpe::hpsi<double, 2>(p, S, L, L0, vdt, gdt, hx, hy, nrm);
+    }
+};
+template <> struct Ops<float> {
+    static __device__ __forceinline__ float2 add(float2 a, float2 b) { return f2_add(a, b); }
+    static __device__ __forceinline__ void hpsi(float2 p, const float2 *S, const float *L, float L0, float vdt,
+                                                float gdt, float &hx, float &hy, float &nrm)
+    {
+        nrm = d_fma(p.x, p.x, d_mul(p.y, p.y));
+        const float c = d_fma(gdt, nrm, d_add(L0, vdt));
+        float2 a = f2_mul(make_float2(L[0], L[0]), S[0]);
+        a = f2_fma(make_float2(L[1], L[1]), S[1], a);
+        const float2 h = f2_fma(make_float2(c, c), p, a);
+        hx = h.x;
+        hy = h.y;
+    }
+};
+
 template <typename T, int TX, int TY, int MODE, int POT, int STAGES, int MINB>
 __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_bcc2_kernel(const FusedArgs a)
 {
@@ -317,11 +376,11 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
             if (lane == 0) mbar_arrive(empty + 8 * st);  // this warp is done with stage st
 
             // sums of plane q = z0-1+k
-            const T2 bBq = c_add<T>(c_add<T>(qBmm, qBym), c_add<T>(qBxm, qB));
-            const T2 bCq = c_add<T>(c_add<T>(qC, qCxp), c_add<T>(qCyp, qCpp));
-            const T2 axyCq = c_add<T>(c_add<T>(qCxm, qCxp), c_add<T>(qCym, qCyp));
-            const T2 axyBq = c_add<T>(c_add<T>(qBxm, qBxp), c_add<T>(qBym, qByp));
-            const T2 sd0q = c_add<T>(bBp, bBq);  // Sd of slot 0 at plane q
+            const T2 bBq = Ops<T>::add(Ops<T>::add(qBmm, qBym), Ops<T>::add(qBxm, qB));
+            const T2 bCq = Ops<T>::add(Ops<T>::add(qC, qCxp), Ops<T>::add(qCyp, qCpp));
+            const T2 axyCq = Ops<T>::add(Ops<T>::add(qCxm, qCxp), Ops<T>::add(qCym, qCyp));
+            const T2 axyBq = Ops<T>::add(Ops<T>::add(qBxm, qBxp), Ops<T>::add(qBym, qByp));
+            const T2 sd0q = Ops<T>::add(bBp, bBq);  // Sd of slot 0 at plane q
 
             if (k >= 2 && valid) {
                 const int z = w.z0 + k - 2;  // output plane (q - 1)
@@ -338,8 +397,8 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
                 }
                 // slot 0 (cube corner)
                 S2[0] = sd0;
-                S2[1] = c_add<T>(c_add<T>(cm, qC), axyC);
-                hpsi<T, 2>(cc, S2, Lw, L0, v0, gdt, hx, hy, nrm);
+                S2[1] = Ops<T>::add(Ops<T>::add(cm, qC), axyC);
+                Ops<T>::hpsi(cc, S2, Lw, L0, v0, gdt, hx, hy, nrm);
                 const T2 o0 = integrate<T, MODE>(n0, cc, hx, hy);
                 if (MODE == 1) {
                     s0.add(nrm);
@@ -348,9 +407,9 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
                     s3.add(d_fma(o0.x, o0.x, d_mul(o0.y, o0.y)));
                 }
                 // slot 1 (cube centre)
-                S2[0] = c_add<T>(bCc, bCq);
-                S2[1] = c_add<T>(c_add<T>(bm, qB), axyB);
-                hpsi<T, 2>(bc, S2, Lw, L0, v1, gdt, hx, hy, nrm);
+                S2[0] = Ops<T>::add(bCc, bCq);
+                S2[1] = Ops<T>::add(Ops<T>::add(bm, qB), axyB);
+                Ops<T>::hpsi(bc, S2, Lw, L0, v1, gdt, hx, hy, nrm);
                 const T2 o1 = integrate<T, MODE>(n1, bc, hx, hy);
                 if (MODE == 1) {
                     s0.add(nrm);
@@ -467,65 +526,6 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
 // compute them too) so that no CTA waits for another.  The sums follow the
 // same order as the one-half-step kernel, so the result is bit-identical to two
 // of its launches.
-// Packed FP32 pairs (add / mul / fma .rn.f32x2, sm_100 and later): each lane is
-// the IEEE operation of that lane, so a complex sum, or a complex times a real
-// factor, rounds exactly as the two scalar operations do, in one instruction.
-__device__ __forceinline__ float2 f2_add(float2 a, float2 b)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
-        "add.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-
-__device__ __forceinline__ float2 f2_mul(float2 a, float2 b)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
-        "mul.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-
-__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 a, b, c, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
-        "mov.b64 c, {%6, %7};\n\tfma.rn.f32x2 d, a, b, c;\n\tmov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-    return r;
-}
-
-// Complex sums and dt*H psi (gpe_device.cuh's hpsi, two classes) with the same
-// rounded operations, packed for FP32.
-template <typename T> struct Ops;
-template <> struct Ops<double> {
-    static __device__ __forceinline__ double2 add(double2 a, double2 b) { return c_add<double>(a, b); }
-    static __device__ __forceinline__ void hpsi(double2 p, const double2 *S, const double *L, double L0, double vdt,
-                                                double gdt, double &hx, double &hy, double &nrm)
-    {
-        gpe::hpsi<double, 2>(p, S, L, L0, vdt, gdt, hx, hy, nrm);
-    }
-};
-template <> struct Ops<float> {
-    static __device__ __forceinline__ float2 add(float2 a, float2 b) { return f2_add(a, b); }
-    static __device__ __forceinline__ void hpsi(float2 p, const float2 *S, const float *L, float L0, float vdt,
-                                                float gdt, float &hx, float &hy, float &nrm)
-    {
-        nrm = d_fma(p.x, p.x, d_mul(p.y, p.y));
-        const float c = d_fma(gdt, nrm, d_add(L0, vdt));
-        float2 a = f2_mul(make_float2(L[0], L[0]), S[0]);
-        a = f2_fma(make_float2(L[1], L[1]), S[1], a);
-        const float2 h = f2_fma(make_float2(c, c), p, a);
-        hx = h.x;
-        hy = h.y;
-    }
-};
-
 template <typename T, int TX, int TY>
 struct TwoStepShape {
     using T2 = typename Cplx<T>::type;
