@@ -462,10 +462,10 @@ def fp64_plain_rate(conds, insts, device, steps):
 # ---------------------------------------------------------------------------
 # The other configurations: parity and accuracy cases (not the headline line).
 
-def _stepper(conds, prec, kernel, mode, tile=0, graph_steps=100, device=0):
+def _stepper(conds, prec, kernel, mode, tile=0, graph_steps=100, device=0, zchunk=0):
     from vaikkari_gb300.gpe import Lattice, Potential, Stepper
     return Stepper([c.inst for c in conds], lattice=Lattice.BCC2, precision=prec, kernel=kernel, mode=mode,
-                   potential=Potential.TRAP, graph_steps=graph_steps, tile=tile, device=device)
+                   potential=Potential.TRAP, graph_steps=graph_steps, tile=tile, device=device, zchunk=zchunk)
 
 
 def _rel_l2(a, b):
@@ -560,12 +560,15 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1):
     from vaikkari_gb300.gpe import Kernel, Mode, Precision
     insts = [c.inst for c in conds]
     verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
+    zchunk = 0
     if tile < 0:
-        tile = 0
+        from vaikkari_gb300.autotune import autotune
+        best = autotune(insts, mode=Mode.IMAGINARY, zchunks=(0, 16, 32, 64))
+        tile, zchunk = best["tile"], best["zchunk"]
     res = {}
     steps64 = None
     for prec in (Precision.FP64, Precision.FP32):
-        st = _stepper(conds, prec, Kernel.FUSED, Mode.IMAGINARY, tile=tile)
+        st = _stepper(conds, prec, Kernel.FUSED, Mode.IMAGINARY, tile=tile, zchunk=zchunk)
         for i, c in enumerate(conds):
             st.upload(i, c.psi)
         t0 = time.perf_counter()
@@ -590,7 +593,7 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1):
            "rel_energy_fp32_vs_fp64": max(abs(a - b) / abs(b) for a, b in zip(r32["energy"], r64["energy"])),
            "rel_l2_fp32_vs_fp64": _rel_l2_phase(r32["fields"], r64["fields"])}
     # throughput of the fused imaginary-time step (FP32), device time
-    st = _stepper(conds, Precision.FP32, Kernel.FUSED, Mode.IMAGINARY, tile=tile)
+    st = _stepper(conds, Precision.FP32, Kernel.FUSED, Mode.IMAGINARY, tile=tile, zchunk=zchunk)
     for i, c in enumerate(conds):
         st.upload(i, c.psi)
     st.time_steps(100)
@@ -598,7 +601,7 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1):
     st.close()
     return {"metric": METRIC, "value": verts * 1000 / (ms * 1e-3), "unit": METRIC, "dtype": "f32",
             "config": {"workload": name, "instances": len(insts), "vertices": verts, "dt": insts[0].dt,
-                       "tol": tol, "mode": "imaginary"},
+                       "tol": tol, "mode": "imaginary", "variant": tile, "zchunk": zchunk},
             "accuracy": acc, "cpu_baseline": None}
 
 

@@ -19,7 +19,7 @@ from typing import List, Optional, Sequence
 
 import numpy as np
 
-from .gpe import Instance, Kernel, Lattice, Potential, Precision, Stepper, variants
+from .gpe import Instance, Kernel, Lattice, Mode, Potential, Precision, Stepper, variants
 
 CACHE = os.environ.get("GPE_AUTOTUNE_CACHE",
                        os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tune", "cache.json"))
@@ -34,10 +34,13 @@ def _device_name(device: int) -> str:
         return "unknown"
 
 
-def signature(instances: Sequence[Instance], lattice, precision, potential, device_name: str) -> str:
+def signature(instances: Sequence[Instance], lattice, precision, potential, device_name: str, mode=Mode.REAL) -> str:
     dims = sorted((i.nx, i.ny, i.nz) for i in instances)
-    key = json.dumps({"dims": dims, "lattice": int(lattice), "precision": int(precision),
-                      "potential": int(potential), "device": device_name})
+    fields = {"dims": dims, "lattice": int(lattice), "precision": int(precision), "potential": int(potential),
+              "device": device_name}
+    if mode != Mode.REAL:
+        fields["mode"] = int(mode)
+    key = json.dumps(fields)
     return hashlib.sha1(key.encode()).hexdigest()
 
 
@@ -58,10 +61,11 @@ def _store(db):
 
 
 def measure(instances: List[Instance], tile: int, zchunk: int, fields=None, lattice=Lattice.BCC2,
-            precision=Precision.FP32, potential=Potential.TRAP, steps: int = 200, device: int = 0) -> float:
+            precision=Precision.FP32, potential=Potential.TRAP, steps: int = 200, device: int = 0,
+            mode=Mode.REAL) -> float:
     """Vertex-updates per second of one candidate (best of three timed runs)."""
     st = Stepper(instances, lattice=lattice, precision=precision, kernel=Kernel.FUSED, potential=potential,
-                 graph_steps=100, tile=tile, zchunk=zchunk, device=device)
+                 graph_steps=100, tile=tile, zchunk=zchunk, device=device, mode=mode)
     try:
         for i in range(len(instances)):
             if fields is not None:
@@ -71,7 +75,7 @@ def measure(instances: List[Instance], tile: int, zchunk: int, fields=None, latt
                 shp = st.shape(i)
                 e = o = np.full(shp + (2,), 1e-3, dtype=st.dtype)
                 v = np.zeros(shp, dtype=st.dtype) if potential == Potential.ARRAY else None
-            st.upload(i, e, o, v)
+            st.upload(i, e, None if mode != Mode.REAL else o, v)
         st.time_steps(103)      # warm-up, graph instantiation
         best = min(st.time_steps(steps) for _ in range(3))
         vals = st.total_values()
@@ -82,17 +86,20 @@ def measure(instances: List[Instance], tile: int, zchunk: int, fields=None, latt
 
 def autotune(instances: List[Instance], fields=None, lattice=Lattice.BCC2, precision=Precision.FP32,
              potential=Potential.TRAP, device: int = 0, steps: int = 200, cache: bool = True,
-             zchunks: Sequence[int] = (0, 16, 32), verbose: bool = False) -> dict:
+             zchunks: Sequence[int] = (0, 16, 32), verbose: bool = False, mode=Mode.REAL) -> dict:
     """Best (tile, zchunk) for this batch.  Every variant is timed with the
-    automatic z-chunk, then the three fastest with each z-chunk in `zchunks`."""
+    automatic z-chunk, then the three fastest with each z-chunk in `zchunks`.
+    Imaginary time skips the variants that advance whole real-time steps."""
     name = _device_name(device)
-    sig = signature(instances, lattice, precision, potential, name)
+    sig = signature(instances, lattice, precision, potential, name, mode)
     db = _load() if cache else {}
     if sig in db:
         return db[sig]
     results = []
     for v in variants():
-        r = measure(instances, v["tile"], 0, fields, lattice, precision, potential, steps, device)
+        if mode != Mode.REAL and v["half_steps"] != 1:
+            continue
+        r = measure(instances, v["tile"], 0, fields, lattice, precision, potential, steps, device, mode)
         results.append({"tile": v["tile"], "zchunk": 0, "vups": r})
         if verbose:
             print("autotune", v, f"{r:.4g}", flush=True)
@@ -101,7 +108,7 @@ def autotune(instances: List[Instance], fields=None, lattice=Lattice.BCC2, preci
         for zc in zchunks:
             if zc == 0:
                 continue
-            r = measure(instances, t["tile"], zc, fields, lattice, precision, potential, steps, device)
+            r = measure(instances, t["tile"], zc, fields, lattice, precision, potential, steps, device, mode)
             results.append({"tile": t["tile"], "zchunk": zc, "vups": r})
             if verbose:
                 print("autotune", t["tile"], zc, f"{r:.4g}", flush=True)

@@ -695,8 +695,10 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
         });
         int zc = cfg->zchunk;
         if (zc <= 0) {
-            // Aim for >= ~4 waves of 152 SMs x 8 CTAs while keeping chunks >= 8 planes.
-            const long long target = 152ll * 8 * 4;
+            // Real time: aim for >= ~4 waves of 152 SMs x 8 CTAs while keeping chunks
+            // >= 8 planes.  Imaginary time pays a reduction per item and a final
+            // fold over all items every step, so it aims for about two items per SM.
+            const long long target = cfg->mode == GPE_IMAGINARY_TIME ? 152ll * 2 : 152ll * 8 * 4;
             long long maxnz = 1;
             for (auto &in : h->inst) maxnz = std::max<long long>(maxnz, in.nz);
             zc = int(maxnz);
