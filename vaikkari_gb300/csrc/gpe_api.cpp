@@ -77,7 +77,7 @@ struct gpe_handle_ {
     ImagScalars *imag = nullptr;
     double *partials = nullptr;       // fused imaginary-time rows
     unsigned int *counter = nullptr;
-    void *maps = nullptr;             // fused: CUtensorMap[num_instances][2]
+    void *maps = nullptr;             // fused: CUtensorMap[num_instances][2][2] (fields or buffer sets)
     int *err = nullptr;               // device error word of the bounded waits
     double *obs_partials = nullptr;   // observables CTA rows
     double *obs_sums = nullptr;       // per instance, 6 sums

@@ -859,14 +859,6 @@ void fused_variant(int tile, int *tx, int *ty, int *stages, int *minb)
     *minb = v.minb;
 }
 
-int fused_box_bytes(int precision, int tile)
-{
-    int tx, ty;
-    fused_tile_shape(tile, &tx, &ty);
-    const int c = precision == GPE_FP64 ? 16 : 8;
-    return (tx + 4) * (ty + 2) * 2 * c;
-}
-
 // The two 4-D tensor maps of one field of one instance (out_map[0], out_map[1]):
 // dimensions (x in 8-byte elements, y, slot, z) over the padded layout; boxes =
 // tile plus a 2-column / 1-row halo (previous-field loads) and the interior tile

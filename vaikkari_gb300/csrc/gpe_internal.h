@@ -84,8 +84,6 @@ gpe_status make_twostep_maps(void *out_map, int precision, const InstDev &d, voi
 int fused_tile_count();
 void fused_tile_shape(int tile, int *tx, int *ty);
 void fused_variant(int tile, int *tx, int *ty, int *stages, int *minb);
-// Bytes of one TMA box (tile plus halo, both slots) of the fused kernel.
-int fused_box_bytes(int precision, int tile);
 // Encodes the fused kernel's two 4-D tensor maps (halo box, interior box) of
 // one field of one instance into out_map[0..1].
 gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *field_arena, int tile);
