@@ -176,6 +176,28 @@ template <typename T, int MINB> struct MinBlocks {
     static constexpr int value = sizeof(T) == 8 ? (MINB + 1) / 2 : MINB;
 };
 
+// Programmatic dependent launch (sm_90 and later).
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Launch with programmatic stream serialisation: the kernel may begin while the
+// previous kernel on the stream drains, and waits for it in grid_dependency_wait.
+template <typename Kern, typename Args>
+static cudaError_t launch_pdl(Kern kern, int grid, int threads, int bytes, cudaStream_t s, const Args &a)
+{
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.gridDim = dim3(unsigned(grid));
+    cfg.blockDim = dim3(unsigned(threads));
+    cfg.dynamicSmemBytes = size_t(bytes);
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, a);
+}
+
 // Packed FP32 pairs (add / mul / fma .rn.f32x2, sm_100 and later): each lane is
 // the IEEE operation of that lane, so a complex sum, or a complex times a real
 // factor, rounds exactly as the two scalar operations do, in one instruction.
@@ -276,6 +298,9 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
             ztab[i] = tz[sl * nz + z];
         }
     }
+    // Programmatic dependent launch: this grid may start while the previous one
+    // drains; nothing it wrote (fields, imaginary-time scalars) is read before here.
+    grid_dependency_wait();
     __syncthreads();
 
     if (warp == NWARPS - 1) {
@@ -448,6 +473,7 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
         }
     }
 
+    launch_dependents();  // the next grid may be scheduled; it waits for this one to finish
     if (MODE == 1) {
         // Last CTA to finish reduces every instance's rows (fixed order).
         __shared__ bool last;
@@ -623,6 +649,7 @@ __global__ void __launch_bounds__(TwoStepShape<T, TX, TY>::NTHREADS, MinBlocks<T
             ztab[i] = tz[sl * nz + z];
         }
     }
+    grid_dependency_wait();
     __syncthreads();
 
     if (warp == NWARPS - 1) {
@@ -811,6 +838,7 @@ __global__ void __launch_bounds__(TwoStepShape<T, TX, TY>::NTHREADS, MinBlocks<T
             }
         }
     }
+    launch_dependents();
 }
 
 
@@ -955,8 +983,7 @@ static cudaError_t launch_two(const TwoStepArgs &a, int grid, cudaStream_t s)
         if (e != cudaSuccess) return e;
         allowed = bytes;
     }
-    kern<<<grid, TwoStepShape<T, TX, TY>::NTHREADS, bytes, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(kern, grid, TwoStepShape<T, TX, TY>::NTHREADS, bytes, s, a);
 }
 
 template <typename T, int TX, int TY, int ST, int MB>
@@ -1009,6 +1036,10 @@ static cudaError_t launch_one(const FusedArgs &a, int grid, cudaStream_t s)
         if (e != cudaSuccess) return e;
         allowed = bytes;
     }
+    // Real time: programmatic dependent launch.  Imaginary time ends every grid with
+    // a serial fold in one CTA; there an early-scheduled next grid only holds SM
+    // slots, so it launches plainly (the griddepcontrol instructions are then no-ops).
+    if (MODE == 0) return launch_pdl(kern, grid, FusedShape<T, TX, TY>::NTHREADS, bytes, s, a);
     kern<<<grid, FusedShape<T, TX, TY>::NTHREADS, bytes, s>>>(a);
     return cudaGetLastError();
 }
