@@ -602,7 +602,38 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1):
     return {"metric": METRIC, "value": verts * 1000 / (ms * 1e-3), "unit": METRIC, "dtype": "f32",
             "config": {"workload": name, "instances": len(insts), "vertices": verts, "dt": insts[0].dt,
                        "tol": tol, "mode": "imaginary", "variant": tile, "zchunk": zchunk},
-            "accuracy": acc, "cpu_baseline": None}
+            "accuracy": acc, "cpu_baseline": _cpu_imag_rate(conds)}
+
+
+def _cpu_imag_rate(conds, budget_s=5.0):
+    """FP64 oracle imaginary-time steps (observables, then the normalised Euler
+    step, all host threads for the step) of every condensate for about
+    `budget_s` seconds."""
+    import oracle.oracle as orc
+    from vaikkari_gb300.gpe import Lattice, lattice_info, value_positions
+    from vaikkari_gb300.workloads import harmonic
+    info = lattice_info(Lattice.BCC2)
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    jobs = []
+    for c in conds:
+        inst = c.inst
+        g = orc.Grid(inst.nx, inst.ny, inst.nz, info["entry"], info["class_weight"], inst.block_scale, inst.dt,
+                     inst.g)
+        vdt = np.ascontiguousarray(harmonic(value_positions(inst, info), inst.trap) * inst.dt)
+        psi = np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1), dtype=np.float64)
+        jobs.append((g, psi, vdt, info["cell_volume"] * inst.block_scale ** 3))
+    verts = sum(c.inst.nx * c.inst.ny * c.inst.nz * 2 for c in conds)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        for g, psi, vdt, vol in jobs:
+            g.imaginary(psi, vdt, vol, 2, 0.0)
+        steps += 2
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 1000:
+            break
+    return {"value": verts * steps / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{steps} imaginary-time step(s), {verts} vertices, FP64 oracle port, {el:.2f} s"}
 
 
 def run_relax(args):
