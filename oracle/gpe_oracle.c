@@ -81,12 +81,15 @@ int oracle_get_threads(void)
                     }                                                                               \
                     const T nrm = FMA(px, px, py * py);                                             \
                     const T cc = FMA(gdt, nrm, L0 + vdt[o]);                                        \
-                    T ax = Lc0 * sx[0], ay = Lc0 * sy[0];                                           \
-                    if (ncls > 1) {                                                                 \
-                        ax = FMA(Lc1, sx[1], ax);                                                   \
-                        ay = FMA(Lc1, sy[1], ay);                                                   \
+                    T hx, hy;                                                                       \
+                    if (ncls == 1) { /* one class: fma(L, S, c*p), the reference kernel's rounding */ \
+                        hx = FMA(Lc0, sx[0], cc * px);                                              \
+                        hy = FMA(Lc0, sy[0], cc * py);                                              \
+                    } else {                                                                        \
+                        const T ax = FMA(Lc1, sx[1], Lc0 * sx[0]), ay = FMA(Lc1, sy[1], Lc0 * sy[0]); \
+                        hx = FMA(cc, px, ax);                                                       \
+                        hy = FMA(cc, py, ay);                                                       \
                     }                                                                               \
-                    const T hx = FMA(cc, px, ax), hy = FMA(cc, py, ay);                             \
                     if (mode == 0) {                                                                \
                         next[2 * o] = next[2 * o] + hy;                                             \
                         next[2 * o + 1] = next[2 * o + 1] - hx;                                     \

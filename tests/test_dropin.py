@@ -60,7 +60,7 @@ def test_integrate_setup_equals_reference():
 def test_integrate_in_time_matches_reference_kernel():
     """Two iterations (2 x steps_per_iteration leapfrog steps) of the drop-in on
     the GPU against the reference's own update kernel (built for sm_103a) from the
-    same set-up, and the CPU oracle."""
+    same set-up, and the CPU oracle: all three bit for bit."""
     import refkernel
     ref = golden("ref_setup_small.json")
     st = _state()
@@ -76,9 +76,8 @@ def test_integrate_in_time_matches_reference_kernel():
         rk.upload(even0, odd0, V * res["dt"])
         rk.step(steps, ref["block_scale"], res["dt"], _state().describe()["g"])
         re, ro = rk.download()
-        scale = np.abs(re).max()
-        assert np.abs(even - re).max() <= 1e-12 * scale
-        assert np.abs(odd - ro).max() <= 1e-12 * scale
+        np.testing.assert_array_equal(even, re)
+        np.testing.assert_array_equal(odd, ro)
     # the oracle, with the geometry-derived table as the library uses it
     import oracle.oracle as orc
     from vaikkari_gb300.gpe import Lattice, lattice_info

@@ -99,14 +99,23 @@ __device__ __forceinline__ typename Cplx<T>::type c_scale(T s, typename Cplx<T>:
 // with one weight per class:
 //     nrm = fma(p.x, p.x, p.y*p.y)
 //     c   = fma(gdt, nrm, L0 + Vdt)
-//     a   = L[0]*S[0] (+ fma(L[c], S[c], a) for further classes)
-//     h   = fma(c, p, a)
+//     one class:  h = fma(L[0], S[0], c*p)
+//     two classes: a = L[0]*S[0], a = fma(L[1], S[1], a), h = fma(c, p, a)
 template <typename T, int NC>
 __device__ __forceinline__ void hpsi(typename Cplx<T>::type p, const typename Cplx<T>::type *S, const T *L, T L0,
                                      T vdt, T gdt, T &hx, T &hy, T &nrm)
 {
     nrm = d_fma(p.x, p.x, d_mul(p.y, p.y));
     const T c = d_fma(gdt, nrm, d_add(L0, vdt));
+    if (NC == 1) {
+        // One class (TETRA12): h = fma(L, S, c*p), the product c*p rounded first.
+        // This is the rounding of the reference's update as compiled for the GPU:
+        // with it (and the reference's neighbour order) results equal its kernel
+        // bit for bit.
+        hx = d_fma(L[0], S[0].x, d_mul(c, p.x));
+        hy = d_fma(L[0], S[0].y, d_mul(c, p.y));
+        return;
+    }
     T ax = d_mul(L[0], S[0].x);
     T ay = d_mul(L[0], S[0].y);
 #pragma unroll

@@ -115,6 +115,18 @@ struct Entry {
     double w;
 };
 
+// The weights and volumes of these lattices are small dyadic rationals (1.5,
+// 0.75, 0.25, 0.5) or irrational (sqrt(32/9)); computed from the geometry they
+// carry a few ulp of rounding.  A value within 8 ulp of a multiple of 2^-32 is
+// taken to be that multiple, so that the factors built from it are the ones the
+// reference builds from its exact constants (getLaplacian returns 1.5).
+double snap_dyadic(double v)
+{
+    const double r = std::ldexp(std::nearbyint(std::ldexp(v, 32)), -32);
+    const double ulp = std::nextafter(std::fabs(v), INFINITY) - std::fabs(v);
+    return std::fabs(r - v) <= 8.0 * ulp ? r : v;
+}
+
 void finish(gpe_lattice_info *info, std::vector<std::vector<Entry>> &tab)
 {
     // Weight classes: distinct weights, largest first.
@@ -124,7 +136,7 @@ void finish(gpe_lattice_info *info, std::vector<std::vector<Entry>> &tab)
             bool found = false;
             for (double c : cls)
                 if (std::fabs(c - e.w) <= 1e-12 * std::fabs(c)) found = true;
-            if (!found) cls.push_back(e.w);
+            if (!found) cls.push_back(snap_dyadic(e.w));
         }
     std::sort(cls.begin(), cls.end(), std::greater<double>());
     info->classes = int(cls.size());
@@ -223,6 +235,42 @@ gpe_status build_tetra12(gpe_lattice_info *info)
     for (int s = 0; s < 12; s++)
         for (int k = 0; k < 3; k++) info->position[s][k] = order[s][k] * std::sqrt(8.0) / 8.0;
     finish(info, tab);
+    // Summation order of the four neighbours: the order in which the reference's
+    // getLaplacian lists them (GPUGrossPitaevskii_BCC.cu:90-142), which its kernel
+    // sums in.  In geometric terms: a circumcentre has one coordinate at 7/8 of the
+    // block (its major axis).  First come the two neighbours whose displacement has
+    // no component along that axis, then the other two.  Within each pair the two
+    // displacements differ in one component; the first pair is ordered by it
+    // ascending, the second descending.
+    for (int s = 0; s < 12; s++) {
+        int m = 0;
+        for (int k = 1; k < 3; k++)
+            if (order[s][k] > order[s][m]) m = k;
+        std::array<std::array<int, 5>, 4> row;
+        std::array<I3, 4> disp;
+        for (int k = 0; k < 4; k++) {
+            for (int c = 0; c < 5; c++) row[k][c] = info->entry[s][k][c];
+            const I3 &to = order[row[k][3]];
+            disp[k] = {8 * row[k][0] + to[0] - order[s][0], 8 * row[k][1] + to[1] - order[s][1],
+                       8 * row[k][2] + to[2] - order[s][2]};
+        }
+        std::array<int, 4> idx = {0, 1, 2, 3};
+        std::vector<int> flat, axial;
+        for (int k : idx) (disp[k][m] == 0 ? flat : axial).push_back(k);
+        if (flat.size() != 2 || axial.size() != 2) return GPE_ERR_INTERNAL;
+        auto order_pair = [&](std::vector<int> &pair, bool ascending) {
+            const I3 &a = disp[pair[0]], &b = disp[pair[1]];
+            int c = 0;
+            while (c < 3 && a[c] == b[c]) c++;
+            if (c == 3) return false;
+            if ((a[c] < b[c]) != ascending) std::swap(pair[0], pair[1]);
+            return true;
+        };
+        if (!order_pair(flat, true) || !order_pair(axial, false)) return GPE_ERR_INTERNAL;
+        const int seq[4] = {flat[0], flat[1], axial[0], axial[1]};
+        for (int k = 0; k < 4; k++)
+            for (int c = 0; c < 5; c++) info->entry[s][k][c] = row[seq[k]][c];
+    }
     return GPE_OK;
 }
 
@@ -299,7 +347,7 @@ gpe_status build_bcc2(gpe_lattice_info *info)
     info->slots = 2;
     info->neighbours = 14;
     info->block_width = 1.0;
-    info->cell_volume = dual_volume;
+    info->cell_volume = snap_dyadic(dual_volume);
     for (int s = 0; s < 2; s++)
         for (int k = 0; k < 3; k++) info->position[s][k] = slot_pos[s][k] / 8.0;
     finish(info, tab);
