@@ -323,13 +323,15 @@ typedef struct gpe_relax_result {
  * `count` independent states at once; each state's f and mu are updated in place
  * and results[k] (may be NULL) describes state k.  The sweep is the reference's
  * Gauss-Seidel order exactly; the per-iteration sums are formed per row in chunks
- * of 32 columns, so values agree with the reference to rounding (with a CPU
- * restatement of that order bit for bit).  Needs rsize >= 2.  Error
+ * of 16 columns and over rows in groups of 16, so values agree with the
+ * reference to rounding (with a CPU restatement of that order bit for bit).
+ * Needs rsize >= 2.  Error
  * GPE_ERR_TIMEOUT if a sweep's bounded wait on the row above ran out. */
 gpe_status gpe_vortex_relax(gpe_vortex *states, int32_t count, const gpe_relax_desc *d, gpe_relax_result *results);
 
 /* Test hook: the relaxation sweep's division (from a correctly rounded
- * reciprocal, two Markstein corrections) and __ddiv_rn on the same n pairs; host
+ * reciprocal and its low part, one Markstein correction) and __ddiv_rn on the
+ * same n pairs; host
  * arrays, out ours[n] and ref[n]. */
 gpe_status gpe_debug_divide(const double *a, const double *b, double *ours, double *ref, int64_t n, int32_t device);
 
