@@ -1,4 +1,4 @@
-"""Benchmark: vertex-updates/s of the GPE stepper on one GB300 (or N replicas).
+"""Benchmark: vertex-updates/s of the GPE stepper on one GB300 (or N ranks).
 
 Default workload (the batched configuration the headline metric is quoted on):
 64 independent condensates on the BCC2 lattice, grid edge per instance uniform
@@ -10,9 +10,11 @@ steps.  One bench step = one leapfrog step (two half-steps) of every instance.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line (rank 0).  Multi-GPU: replicas only (the batch is
-independent condensates; each rank advances its own copy; no collective on the
-data path), value = all ranks' vertex-updates / max-over-ranks time.
+Prints one JSON line (rank 0).  Multi-GPU: the condensates are independent, so
+each rank advances its own shard with no collective on the data path; value =
+all ranks' vertex-updates / max-over-ranks time.  --scaling weak (default): 64
+condensates per rank, same sizes, own g / trap / noise; rank 0 holds the batch
+above.  --scaling strong: the batch above split over the ranks by size.
 """
 import argparse
 import json
@@ -130,15 +132,38 @@ def _max_over_ranks(dist, v, device=None):
     return float(t.item())
 
 
+def _sum_over_ranks(dist, v, device=None):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def replica_value(vertices_per_rank, world_size, steps, ms_max):
-    """Whole-job vertex-updates/s: every rank advances its own copy of the batch
+    """Whole-job vertex-updates/s when every rank advances a batch of equal size
     (no data-path collective); the job takes as long as the slowest rank."""
     return vertices_per_rank * world_size * steps / (ms_max * 1e-3)
 
 
-def build_batch():
+def job_value(vertices_all_ranks, steps, ms_max):
+    """Whole-job vertex-updates/s from the vertices of all ranks together."""
+    return vertices_all_ranks * steps / (ms_max * 1e-3)
+
+
+def build_batch(rank=0, world_size=1, scaling="weak"):
+    """This rank's condensates.  weak: a job of 64 x world_size independent
+    condensates, 64 per rank, every rank the same size sequence (equal work) with
+    its own g, traps and noise; rank 0 holds the single-GPU batch.  strong: the
+    single-GPU batch split over the ranks by size (largest first onto the rank
+    with the fewest vertices).  No data-path exchange either way."""
     from vaikkari_gb300 import workloads
-    return workloads.config4()
+    if scaling == "weak":
+        return workloads.config4(shard=rank)
+    conds = workloads.config4()
+    part = workloads.shard_by_size([c.inst for c in conds], world_size)[rank]
+    return [conds[i] for i in part]
 
 
 def prepare_fields(stepper, conds, precision_dtype):
@@ -282,9 +307,10 @@ def run_ours(args):
     torch.cuda.set_device(local)
     dist = _init_pg(ws, "nccl")
     from vaikkari_gb300.gpe import Kernel, Lattice, Mode, Potential, Precision, Stepper
-    conds = build_batch()
+    conds = build_batch(rank, ws, args.scaling)
     insts = [c.inst for c in conds]
     verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
+    verts_job = _sum_over_ranks(dist, verts, device=torch.device("cuda", local))
     tile, zchunk, tuned = args.tile, args.zchunk, None
     if tile < 0:
         # untimed: pick the kernel variant and z-chunk for this batch (cached per device)
@@ -316,7 +342,7 @@ def run_ours(args):
     if dist:
         dist.barrier()
     ms_max = _max_over_ranks(dist, ms, device=torch.device("cuda", local))
-    value = replica_value(verts, ws, args.steps, ms_max)
+    value = job_value(verts_job, args.steps, ms_max)
 
     # Roofline of the fused kernel: it is the only kernel in the timed region
     # (two launches per step), so the average launch lasts ms / launches.
@@ -347,7 +373,8 @@ def run_ours(args):
     st.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_s = _max_over_ranks(dist, e2e_s, device=torch.device("cuda", local))
-    e2e_value = verts * ws * args.steps / e2e_s
+    e2e_value = verts_job * args.steps / e2e_s
+    h2d_job = int(_sum_over_ranks(dist, h2d, device=torch.device("cuda", local)))
     finite = all(o["finite"] for o in obs)
     st.close()
 
@@ -377,12 +404,14 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "scaling": args.scaling, "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batch64_bcc2_fp32_trap_realtime", "instances": len(insts),
-                       "vertices": verts, "sizes": sorted({i.nx for i in insts}), "dt": 1e-4,
+                       "vertices": verts, "vertices_all_ranks": verts_job,
+                       "sizes": sorted({i.nx for i in insts}), "dt": 1e-4,
                        "graph_steps": 100, "kernel": "fused", "variant": tile, "zchunk": zchunk,
                        "autotuned": tuned is not None,
-                       "parallelism": f"replicas{ws}" if ws > 1 else "single",
+                       "parallelism": (f"condensate shards x{ws} ({args.scaling}), no collective"
+                                       if ws > 1 else "single"),
                        "l2": f"inputs larger than L2 (fields {2 * 8 * verts / 1e6:.0f} MB vs {L2_BYTES / 1e6:.0f} MB)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
@@ -390,7 +419,8 @@ def run_ours(args):
                          "peak_source": f"{peak_kind} hbm_gbs", "kernel": "fused_bcc2_kernel"},
             "gpu_launches": launches,
             "clocks": clk.summary(),
-            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d_job,
+                    "d2h_bytes_per_step": h2d_job,
                     "steps_per_call": args.steps, "seconds": e2e_s, "finite": finite},
             "cpu_baseline": cpu,
             "accuracy": acc,
@@ -787,6 +817,8 @@ def main():
     ap.add_argument("--workload", default="batch64",
                     help="batch64 (the headline), config1/config2/config3/config5 (accuracy cases), relax "
                          "(the vortex relaxation) or production (main() at production size)")
+    ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
+                    help="multi-GPU split: weak = 64 condensates per rank, strong = the 64 split over ranks")
     ap.add_argument("--production-iters", type=int, default=2)
     ap.add_argument("--relax-batch", type=int, default=19)
     ap.add_argument("--relax-batch-iters", type=int, default=2000)

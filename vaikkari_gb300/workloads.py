@@ -24,7 +24,7 @@ from __future__ import annotations
 
 import math
 from dataclasses import dataclass
-from typing import List, Optional
+from typing import List, Sequence, Optional
 
 import numpy as np
 
@@ -128,11 +128,16 @@ def config3(lattice: Lattice = Lattice.BCC2, n: int = 192) -> Condensate:
 
 
 def config4(lattice: Lattice = Lattice.BCC2, count: int = 64, sizes=(24, 32, 48, 64, 96),
-            dt: float = 1e-4) -> List[Condensate]:
+            dt: float = 1e-4, shard: int = 0) -> List[Condensate]:
+    """The 64-condensate batch (seed 2).  shard > 0 gives another batch of the
+    same sizes with its own g, traps and noise: one rank's part of a job of
+    64 x ranks condensates, as heavy as shard 0."""
     info = lattice_info(lattice)
     mk = bcc2_instance if lattice == Lattice.BCC2 else tetra12_instance
     rng = np.random.default_rng(2)
     ns = rng.choice(np.asarray(sizes), size=count)
+    if shard:
+        rng = np.random.default_rng((2, shard))
     gs = np.exp(rng.uniform(math.log(100.0), math.log(5000.0), size=count))
     om = rng.uniform(0.5, 2.0, size=(count, 3))
     out = []
@@ -158,3 +163,18 @@ def config5(lattice: Lattice = Lattice.BCC2, n: int = 512) -> Condensate:
 def odd_from_even(psi: np.ndarray, mu: float, dt: float) -> np.ndarray:
     """odd = even * exp(+i mu dt/2) (GPUGrossPitaevskii_BCC.cu:325,342)."""
     return psi * complex(math.cos(0.5 * mu * dt), math.sin(0.5 * mu * dt))
+
+
+def shard_by_size(instances: Sequence, world: int) -> List[List[int]]:
+    """Splits independent condensates over `world` ranks by size: largest first,
+    each to the rank with the fewest values so far (ties to the lowest rank).
+    Returns the instance indices of every rank, each list in ascending order."""
+    load = [0] * world
+    parts: List[List[int]] = [[] for _ in range(world)]
+    order = sorted(range(len(instances)), key=lambda i: (-instances[i].nx * instances[i].ny * instances[i].nz, i))
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        parts[r].append(i)
+        inst = instances[i]
+        load[r] += inst.nx * inst.ny * inst.nz
+    return [sorted(p) for p in parts]
