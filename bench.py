@@ -33,6 +33,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "vertex-updates/s"
 BYTES_PER_VERTEX_STEP = 48  # FP32, trap potential in-kernel: 2 half-steps x (read prev 8 B + RMW next 16 B)
+BYTES_PER_VERTEX_STEP_COMP = 64  # FP32C: plus the next field's bf16x2 residual, read and written (2 x 8 B)
 L2_BYTES = 129e6
 
 
@@ -383,6 +384,11 @@ def run_ours(args):
     if rank == 0 and not args.skip_accuracy:
         acc = accuracy_block(conds, insts, local)
 
+    # The same batch with compensated FP32 storage (accuracy in `accuracy`).
+    comp = None
+    if rank == 0 and not args.skip_comp:
+        comp = compensated_block(conds, insts, local, args.steps, args.warmup, tune=args.tile < 0)
+
     # The FP64 plain path, one instance at a time (the drop-in denominator).
     fp64 = None
     if rank == 0 and not args.skip_fp64:
@@ -424,6 +430,7 @@ def run_ours(args):
                     "steps_per_call": args.steps, "seconds": e2e_s, "finite": finite},
             "cpu_baseline": cpu,
             "accuracy": acc,
+            "compensated": comp,
             "fp64_plain": fp64,
         }
         print(json.dumps(line), flush=True)
@@ -437,7 +444,7 @@ def accuracy_block(conds, insts, device):
     steps = 1000
     res = {}
     outs = {}
-    for prec, dt_ in ((Precision.FP32, np.float32), (Precision.FP64, np.float64)):
+    for prec, dt_ in ((Precision.FP32, np.float32), (Precision.FP64, np.float64), (Precision.FP32C, np.float64)):
         st = Stepper(insts, lattice=Lattice.BCC2, precision=prec, kernel=Kernel.FUSED, potential=Potential.TRAP,
                      graph_steps=100, device=device)
         prepare_fields(st, conds, dt_)
@@ -459,7 +466,62 @@ def accuracy_block(conds, insts, device):
     res["max_norm_drift_fp32_vs_fp64"] = max(abs(a - b) / b for a, b in zip(n32, n64))
     res["max_energy_drift_fp32_vs_fp64"] = max(abs(a - b) / abs(b) for a, b in zip(e32, e64))
     res["max_norm_drift_fp64_scheme"] = max(abs(a - b) / b for a, b in zip(n64, n0))
+    # per-instance relative L2 (each condensate weighted alike)
+    per32 = [math.sqrt(float(np.sum((a - b) ** 2)) / float(np.sum(b ** 2)))
+             for a, b in zip(outs[Precision.FP32][2], outs[Precision.FP64][2])]
+    res["max_instance_rel_l2_fp32"] = max(per32)
+    res["instances_over_1e-5_fp32"] = sum(1 for v in per32 if v > 1e-5)
+    # compensated storage (Precision.FP32C)
+    cf = outs[Precision.FP32C][2]
+    numc = sum(float(np.sum((a - b) ** 2)) for a, b in zip(cf, outs[Precision.FP64][2]))
+    perc = [math.sqrt(float(np.sum((a - b) ** 2)) / float(np.sum(b ** 2)))
+            for a, b in zip(cf, outs[Precision.FP64][2])]
+    nc = [o["norm"] for o in outs[Precision.FP32C][1]]
+    ec = [o["energy"] for o in outs[Precision.FP32C][1]]
+    res["rel_l2_fp32c_vs_fp64"] = math.sqrt(numc / den)
+    res["max_instance_rel_l2_fp32c"] = max(perc)
+    res["max_norm_drift_fp32c_vs_fp64"] = max(abs(a - b) / b for a, b in zip(nc, n64))
+    res["max_energy_drift_fp32c_vs_fp64"] = max(abs(a - b) / abs(b) for a, b in zip(ec, e64))
     return res
+
+
+def compensated_block(conds, insts, device, steps, warmup, tune=True):
+    """The batch in Precision.FP32C (compensated FP32 storage): its own
+    autotuned variant, K timed steps after W + 100 warm-up steps, and the
+    roofline at 64 B per vertex-step."""
+    import torch
+    from vaikkari_gb300.gpe import Kernel, Lattice, Potential, Precision, Stepper
+    tile, zchunk = 0, 0
+    if tune:
+        from vaikkari_gb300.autotune import autotune
+        t = autotune(insts, precision=Precision.FP32C, potential=Potential.TRAP, device=device)
+        tile, zchunk = t["tile"], t["zchunk"]
+    st = Stepper(insts, lattice=Lattice.BCC2, precision=Precision.FP32C, kernel=Kernel.FUSED,
+                 potential=Potential.TRAP, graph_steps=100, tile=tile, zchunk=zchunk, device=device)
+    prepare_fields(st, conds, np.float64)
+    st.step(warmup)
+    st.step(100)
+    st.synchronize()
+    stream = torch.cuda.ExternalStream(st.stream_handle(), device=device)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    n0 = st.launch_count()
+    ev0.record(stream)
+    st.step(steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = st.launch_count() - n0
+    ms = ev0.elapsed_time(ev1)
+    verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
+    st.close()
+    peak, kind = _peaks()
+    achieved = verts * (BYTES_PER_VERTEX_STEP_COMP / 2) / ((ms * 1e-3) / max(launches, 1)) / 1e9
+    return {"value": verts * steps / (ms * 1e-3), "unit": METRIC, "ms_per_step": ms / steps, "steps": steps,
+            "variant": tile, "zchunk": zchunk, "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "algorithmic_bytes_per_vertex_step": BYTES_PER_VERTEX_STEP_COMP,
+                         "peak_source": f"{kind} hbm_gbs"},
+            "storage": "FP32 value + bf16 residual per component (12 B per value and field)"}
 
 
 def fp64_plain_rate(conds, insts, device, steps):
@@ -813,6 +875,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=200)
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-comp", action="store_true", help="skip the compensated-storage (FP32C) timing")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--workload", default="batch64",
                     help="batch64 (the headline), config1/config2/config3/config5 (accuracy cases), relax "

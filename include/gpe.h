@@ -27,7 +27,9 @@
  *   (((z * ny) + y) * nx + x) * slots + slot
  * for block (x, y, z) and value `slot` of that block; complex values are
  * interleaved (re, im).  The element type follows the handle's precision
- * (double for GPE_FP64, float for GPE_FP32).
+ * (double for GPE_FP64, float for GPE_FP32).  GPE_FP32C exchanges the fields
+ * as double (each value is split into an FP32 value and a bf16 residual on
+ * upload and recombined on download) and potential arrays as float.
  *
  * Threading: one handle per host thread; a handle owns its CUDA stream.
  */
@@ -67,7 +69,13 @@ typedef enum gpe_lattice {
     GPE_LATTICE_BCC2 = 1
 } gpe_lattice;
 
-typedef enum gpe_precision { GPE_FP64 = 0, GPE_FP32 = 1 } gpe_precision;
+/* GPE_FP32C: FP32 fields and arithmetic, and in real time a bf16 residual per
+ * component carried from step to step, so that the accumulation of the leapfrog
+ * sums loses about 8 bits less per step than FP32 storage (the stored field
+ * rounds with an exact two-sum and keeps its rounding error).  BCC2, fused
+ * kernel, real time, one-half-step variants only; 12 instead of 8 bytes per
+ * value of a field. */
+typedef enum gpe_precision { GPE_FP64 = 0, GPE_FP32 = 1, GPE_FP32C = 2 } gpe_precision;
 
 typedef enum gpe_time_mode {
     GPE_REAL_TIME = 0,      /* staggered leapfrog, two fields (even, odd)      */

@@ -26,6 +26,22 @@ int oracle_get_threads(void)
 #endif
 }
 
+/* bf16 with round-to-nearest-even on the bit pattern (finite inputs), and back. */
+static inline uint16_t bf16_rn(float f)
+{
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+static inline float bf16_value(uint16_t b)
+{
+    const uint32_t u = (uint32_t)b << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
 #define IDX(g, x, y, z, s) (((((size_t)(z) * (g)->ny) + (size_t)(y)) * (g)->nx + (size_t)(x)) * (g)->slots + (size_t)(s))
 
 /*
@@ -189,7 +205,19 @@ void oracle_leapfrog_f32(const oracle_grid *g, float *even, float *odd, const fl
                     ax = FMA(Lc1, sax, ax);                                                         \
                     ay = FMA(Lc1, say, ay);                                                         \
                     const T hx = FMA(cc, px, ax), hy = FMA(cc, py, ay);                             \
-                    if (mode == 0) {                                                                \
+                    if (mode == 0 && next_lo) { /* compensated storage: exact two-sum */            \
+                        const T tx = (T)bf16_value(next_lo[2 * o]) + hy;                            \
+                        const T ty = (T)bf16_value(next_lo[2 * o + 1]) - hx;                        \
+                        const T ux = next[2 * o], uy = next[2 * o + 1];                             \
+                        const T wx = ux + tx, wy = uy + ty;                                         \
+                        const T bx = wx - ux, by = wy - uy;                                         \
+                        const T rx = (ux - (wx - bx)) + (tx - bx);                                  \
+                        const T ry = (uy - (wy - by)) + (ty - by);                                  \
+                        next[2 * o] = wx;                                                           \
+                        next[2 * o + 1] = wy;                                                       \
+                        next_lo[2 * o] = bf16_rn((float)rx);                                        \
+                        next_lo[2 * o + 1] = bf16_rn((float)ry);                                    \
+                    } else if (mode == 0) {                                                         \
                         next[2 * o] = next[2 * o] + hy;                                             \
                         next[2 * o + 1] = next[2 * o + 1] - hx;                                     \
                     } else {                                                                        \
@@ -203,6 +231,7 @@ void oracle_leapfrog_f32(const oracle_grid *g, float *even, float *odd, const fl
 void oracle_half_step_bcc2_f64(const oracle_grid *g, const double *prev, double *next, const double *vdt, int mode,
                                double sigma)
 {
+    uint16_t *const next_lo = NULL;
     BCC2_BODY(double, fma)
 }
 
@@ -287,7 +316,28 @@ static void bcc2_value_f64(const oracle_grid *g0, const double *prev, double *ne
 void oracle_half_step_bcc2_f32(const oracle_grid *g, const float *prev, float *next, const float *vdt, int mode,
                                float sigma)
 {
+    uint16_t *const next_lo = NULL;
     BCC2_BODY(float, fmaf)
+}
+
+/* Real time with compensated storage (GPE_FP32C): next_lo holds a bf16 residual
+ * per component, (re, im) per value in block order. */
+void oracle_half_step_bcc2_f32c(const oracle_grid *g, const float *prev, float *next, uint16_t *next_lo,
+                                const float *vdt)
+{
+    const int mode = 0;
+    const float sigma = 1.0f;
+    (void)sigma;
+    BCC2_BODY(float, fmaf)
+}
+
+void oracle_leapfrog_bcc2_f32c(const oracle_grid *g, float *even, float *odd, uint16_t *even_lo, uint16_t *odd_lo,
+                               const float *vdt, long steps)
+{
+    for (long k = 0; k < steps; k++) {
+        oracle_half_step_bcc2_f32c(g, even, odd, odd_lo, vdt);
+        oracle_half_step_bcc2_f32c(g, odd, even, even_lo, vdt);
+    }
 }
 
 /*

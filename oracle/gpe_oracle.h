@@ -23,6 +23,8 @@
 #ifndef GPE_ORACLE_H
 #define GPE_ORACLE_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -60,6 +62,13 @@ void oracle_half_step_bcc2_f32(const oracle_grid *g, const float *prev, float *n
                                float sigma);
 void oracle_leapfrog_bcc2_f64(const oracle_grid *g, double *even, double *odd, const double *vdt, long steps);
 void oracle_leapfrog_bcc2_f32(const oracle_grid *g, float *even, float *odd, const float *vdt, long steps);
+/* BCC2 real time with compensated storage: next += -i h as an exact two-sum of
+ * the stored FP32 value and (residual + increment); the rounding error is kept
+ * as a bf16 residual per component (re, im per value, block order). */
+void oracle_half_step_bcc2_f32c(const oracle_grid *g, const float *prev, float *next, uint16_t *next_lo,
+                                const float *vdt);
+void oracle_leapfrog_bcc2_f32c(const oracle_grid *g, float *even, float *odd, uint16_t *even_lo, uint16_t *odd_lo,
+                               const float *vdt, long steps);
 
 /* The BCC2 real-time half-step/leapfrog with direct indexing for interior values
  * (bit-identical to the _bcc2_ functions); the timed CPU baseline. */

@@ -47,6 +47,8 @@ def load():
     lib.oracle_half_step_bcc2_f32.argtypes = [G, vp, vp, vp, C.c_int, C.c_float]
     lib.oracle_leapfrog_bcc2_f64.argtypes = [G, vp, vp, vp, C.c_long]
     lib.oracle_leapfrog_bcc2_f32.argtypes = [G, vp, vp, vp, C.c_long]
+    lib.oracle_half_step_bcc2_f32c.argtypes = [G, vp, vp, vp, vp]
+    lib.oracle_leapfrog_bcc2_f32c.argtypes = [G, vp, vp, vp, vp, vp, C.c_long]
     lib.oracle_leapfrog_bcc2_fast_f64.argtypes = [G, vp, vp, vp, C.c_long]
     lib.oracle_leapfrog_f64.argtypes = [G, vp, vp, vp, C.c_long]
     lib.oracle_leapfrog_f32.argtypes = [G, vp, vp, vp, C.c_long]
@@ -90,6 +92,29 @@ def factors(class_weight, entry_classes, block_scale, dt, g):
         wsum = wsum + counts[1] * w[1]
     L0 = (0.5 * wsum) * dt
     return {"Lc": Lc, "L0": L0, "gdt": g * dt, "w": w + [0.0] * (2 - len(w))}
+
+
+def bf16_rn(x):
+    """float32 -> bf16 bits (uint16), round to nearest even (finite values)."""
+    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def bf16_value(b):
+    """bf16 bits (uint16) -> float32."""
+    return (np.asarray(b, np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+
+def split_comp(x):
+    """Compensated storage of float64 values: hi = float32(x), lo = bf16(float32(x - hi))."""
+    x = np.asarray(x, np.float64)
+    hi = x.astype(np.float32)
+    return hi, bf16_rn((x - hi.astype(np.float64)).astype(np.float32))
+
+
+def join_comp(hi, lo):
+    """float64(hi) + float64(lo): the value a compensated field stands for."""
+    return hi.astype(np.float64) + bf16_value(lo).astype(np.float64)
 
 
 class Grid:
@@ -138,6 +163,16 @@ class Grid:
             assert a.flags.c_contiguous
         fn = lib.oracle_leapfrog_bcc2_f64 if even.dtype == np.float64 else lib.oracle_leapfrog_bcc2_f32
         fn(C.byref(self._g), self._p(even), self._p(odd), self._p(vdt), int(steps))
+
+    def leapfrog_bcc2_comp(self, even, odd, even_lo, odd_lo, vdt, steps):
+        """In place, BCC2, FP32 with compensated storage: even/odd float32
+        (..., 2), even_lo/odd_lo uint16 (..., 2) bf16 residuals (split_comp)."""
+        lib = load()
+        assert self.slots == 2 and even.dtype == np.float32 and even_lo.dtype == np.uint16
+        for a in (even, odd, even_lo, odd_lo, vdt):
+            assert a.flags.c_contiguous
+        lib.oracle_leapfrog_bcc2_f32c(C.byref(self._g), self._p(even), self._p(odd), self._p(even_lo),
+                                      self._p(odd_lo), self._p(vdt), int(steps))
 
     def leapfrog_bcc2_fast(self, even, odd, vdt, steps):
         """FP64, BCC2: the box-order leapfrog with direct interior indexing (bit-identical)."""

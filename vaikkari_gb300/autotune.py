@@ -73,7 +73,7 @@ def measure(instances: List[Instance], tile: int, zchunk: int, fields=None, latt
                 v = fields[i][2] if len(fields[i]) > 2 else None
             else:
                 shp = st.shape(i)
-                e = o = np.full(shp + (2,), 1e-3, dtype=st.dtype)
+                e = o = np.full(shp + (2,), 1e-3, dtype=st.field_dtype)
                 v = np.zeros(shp, dtype=st.dtype) if potential == Potential.ARRAY else None
             st.upload(i, e, None if mode != Mode.REAL else o, v)
         st.time_steps(103)      # warm-up, graph instantiation
@@ -89,7 +89,8 @@ def autotune(instances: List[Instance], fields=None, lattice=Lattice.BCC2, preci
              zchunks: Sequence[int] = (0, 16, 32), verbose: bool = False, mode=Mode.REAL) -> dict:
     """Best (tile, zchunk) for this batch.  Every variant is timed with the
     automatic z-chunk, then the three fastest with each z-chunk in `zchunks`.
-    Imaginary time skips the variants that advance whole real-time steps."""
+    Imaginary time and compensated storage (Precision.FP32C) skip the variants
+    that advance whole real-time steps."""
     name = _device_name(device)
     sig = signature(instances, lattice, precision, potential, name, mode)
     db = _load() if cache else {}
@@ -97,7 +98,7 @@ def autotune(instances: List[Instance], fields=None, lattice=Lattice.BCC2, preci
         return db[sig]
     results = []
     for v in variants():
-        if mode != Mode.REAL and v["half_steps"] != 1:
+        if (mode != Mode.REAL or Precision(precision) == Precision.FP32C) and v["half_steps"] != 1:
             continue
         r = measure(instances, v["tile"], 0, fields, lattice, precision, potential, steps, device, mode)
         results.append({"tile": v["tile"], "zchunk": 0, "vups": r})

@@ -59,7 +59,10 @@ struct gpe_handle_ {
     std::vector<gpe_instance> inst;
     gpe_lattice_info lat{};
     int ns = 0;
-    size_t esize = 0;  // bytes per real element
+    size_t esize = 0;  // bytes per real element on the device
+    size_t hsize = 0;  // bytes per real element of a host field array (8 for GPE_FP32C)
+    bool comp = false;                   // GPE_FP32C: compensated real-time storage
+    void *lo[2] = {nullptr, nullptr};    // GPE_FP32C: bf16x2 residual per value of fields 0 and 1
     std::vector<InstDev> idev_host;
     InstDev *idev = nullptr;
     size_t field_elems = 0, v_elems = 0;
@@ -235,6 +238,8 @@ gpe_status enqueue_step_real(gpe_handle h)
             l.zcmax = h->zcmax;
             l.inject_skip_plane = h->inject;
             l.src = half == 0 ? 0 : 1;
+            l.comp = h->comp ? 1 : 0;
+            l.next_lo = h->lo[half == 0 ? 1 : 0];
             l.err = h->err;
             l.num_instances = h->cfg.num_instances;
             GPE_CUDA_TRY(launch_fused_step(l, h->stream));
@@ -439,6 +444,7 @@ void free_handle(gpe_handle h)
     for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);
     cudaFree(h->idev);
     for (void *b : h->buf) cudaFree(b);
+    for (void *b : h->lo) cudaFree(b);
     cudaFree(h->vpot);
     cudaFree(h->items_dev);
     cudaFree(h->item_begin_dev);
@@ -512,7 +518,7 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
     *out = nullptr;
     if (cfg->lattice != GPE_LATTICE_TETRA12 && cfg->lattice != GPE_LATTICE_BCC2)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: unknown lattice");
-    if (cfg->precision != GPE_FP64 && cfg->precision != GPE_FP32)
+    if (cfg->precision != GPE_FP64 && cfg->precision != GPE_FP32 && cfg->precision != GPE_FP32C)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: unknown precision");
     if (cfg->mode != GPE_REAL_TIME && cfg->mode != GPE_IMAGINARY_TIME)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: unknown time mode");
@@ -524,6 +530,11 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: need at least one instance");
     if (cfg->kernel == GPE_KERNEL_FUSED && cfg->lattice != GPE_LATTICE_BCC2)
         return fail(GPE_ERR_UNSUPPORTED, "gpe_create: the fused kernel is built for the BCC2 lattice only");
+    if (cfg->precision == GPE_FP32C &&
+        (cfg->lattice != GPE_LATTICE_BCC2 || cfg->kernel == GPE_KERNEL_PLAIN || cfg->mode != GPE_REAL_TIME ||
+         (cfg->tile > 0 && cfg->tile < fused_tile_count() && fused_half_steps(cfg->tile) != 1)))
+        return fail(GPE_ERR_UNSUPPORTED, "gpe_create: GPE_FP32C needs the BCC2 lattice, the fused kernel, real "
+                                         "time and a one-half-step variant");
     for (int i = 0; i < cfg->num_instances; i++) {
         const gpe_instance &in = cfg->instances[i];
         if (in.nx < 1 || in.ny < 1 || in.nz < 1)
@@ -550,6 +561,8 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
     }
     h->ns = h->lat.slots;
     h->esize = cfg->precision == GPE_FP64 ? 8 : 4;
+    h->comp = cfg->precision == GPE_FP32C;
+    h->hsize = h->comp ? 8 : h->esize;
     h->fused = (cfg->lattice == GPE_LATTICE_BCC2) && (cfg->kernel != GPE_KERNEL_PLAIN);
     if (h->fused && !bcc2_order_matches(h->lat)) {
         free_handle(h);
@@ -638,6 +651,11 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
     GPE_CREATE_TRY(cudaMalloc(&h->buf[1], cbytes * h->field_elems));
     GPE_CREATE_TRY(cudaMemsetAsync(h->buf[0], 0, cbytes * h->field_elems, h->stream));
     GPE_CREATE_TRY(cudaMemsetAsync(h->buf[1], 0, cbytes * h->field_elems, h->stream));
+    if (h->comp)
+        for (int f = 0; f < 2; f++) {
+            GPE_CREATE_TRY(cudaMalloc(&h->lo[f], sizeof(uint32_t) * h->field_elems));
+            GPE_CREATE_TRY(cudaMemsetAsync(h->lo[f], 0, sizeof(uint32_t) * h->field_elems, h->stream));
+        }
     GPE_CREATE_TRY(cudaMalloc(&h->vpot, h->esize * std::max<size_t>(h->v_elems, 1)));
     GPE_CREATE_TRY(cudaMemsetAsync(h->vpot, 0, h->esize * std::max<size_t>(h->v_elems, 1), h->stream));
     std::vector<std::vector<float>> traps32(cfg->num_instances);
@@ -654,7 +672,7 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
             }
         }
     }
-    h->staging_bytes = std::max<size_t>(std::max(max_vals * cbytes, out_bytes), 64);
+    h->staging_bytes = std::max<size_t>(std::max(max_vals * 2 * h->hsize, out_bytes), 64);
     GPE_CREATE_TRY(cudaMalloc(&h->staging, h->staging_bytes));
     GPE_CREATE_TRY(cudaMalloc(&h->imag, sizeof(ImagScalars) * cfg->num_instances));
     std::vector<ImagScalars> imag_init(cfg->num_instances);
@@ -807,10 +825,14 @@ gpe_status gpe_upload(gpe_handle h, int32_t instance, const void *even, const vo
     const void *srcs[2] = {even, odd};
     for (int f = 0; f < 2; f++) {
         if (!srcs[f]) continue;
-        st = upload_raw(h, srcs[f], vals * 2 * h->esize);
+        st = upload_raw(h, srcs[f], vals * 2 * h->hsize);
         if (st != GPE_OK) return st;
-        GPE_CUDA_TRY(launch_pack(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->staging, field_buf(h, f), 1,
-                                 1.0, h->stream));
+        if (h->comp)
+            GPE_CUDA_TRY(launch_pack_split(h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->staging, field_buf(h, f),
+                                           h->lo[f], h->stream));
+        else
+            GPE_CUDA_TRY(launch_pack(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->staging, field_buf(h, f),
+                                     1, 1.0, h->stream));
         h->launches++;
         GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
     }
@@ -839,10 +861,14 @@ gpe_status gpe_download(gpe_handle h, int32_t instance, void *even, void *odd)
     void *dsts[2] = {even, odd};
     for (int f = 0; f < 2; f++) {
         if (!dsts[f]) continue;
-        GPE_CUDA_TRY(launch_unpack(h->cfg.precision, h->idev, instance, in.nx, in.ny, in.nz, h->ns, field_buf(h, f),
-                                   h->staging, nullptr, h->stream));
+        if (h->comp)
+            GPE_CUDA_TRY(launch_unpack_join(h->idev, instance, in.nx, in.ny, in.nz, h->ns, field_buf(h, f), h->lo[f],
+                                            h->staging, h->stream));
+        else
+            GPE_CUDA_TRY(launch_unpack(h->cfg.precision, h->idev, instance, in.nx, in.ny, in.nz, h->ns,
+                                       field_buf(h, f), h->staging, nullptr, h->stream));
         h->launches++;
-        GPE_CUDA_TRY(cudaMemcpyAsync(dsts[f], h->staging, vals * 2 * h->esize, cudaMemcpyDeviceToHost, h->stream));
+        GPE_CUDA_TRY(cudaMemcpyAsync(dsts[f], h->staging, vals * 2 * h->hsize, cudaMemcpyDeviceToHost, h->stream));
         GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
     }
     return GPE_OK;

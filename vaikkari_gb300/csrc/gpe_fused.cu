@@ -39,9 +39,21 @@
 // Imaginary time adds fused reductions: per-thread compensated sums, FP64
 // across the CTA, one row per work item; the last CTA to finish reduces each
 // instance's rows in fixed order and updates its ImagScalars.
+//
+// Compensated real time (MODE 2, FP32 only): every value of the next field also
+// carries a bf16 residual per component (one 32-bit word, same padded index as
+// the field).  The update adds the residual to the increment, adds that to the
+// stored value with an exact two-sum, and stores the rounded sum and the bf16 of
+// its rounding error:
+//   t = lo + (hy, -hx);  s = n + t;  b = s - n;  r = (n - (s - b)) + (t - b)
+// so the time accumulation keeps about 8 more bits than FP32 storage.  The
+// residuals are read from L2 (ld.global.cg) one plane ahead of their use.
 
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <cstring>
 
 #include <string>
 
@@ -58,6 +70,7 @@ struct FusedArgs {
     int src;                  // field the previous values come from (0 or 1)
     const void *prev;
     void *next;
+    uint32_t *next_lo;        // MODE 2: bf16x2 residuals of the next field
     const void *vpot;
     ImagScalars *imag;
     double *partials;
@@ -221,6 +234,16 @@ __device__ __forceinline__ float2 f2_mul(float2 a, float2 b)
     return r;
 }
 
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "sub.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
 __device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c)
 {
     float2 r;
@@ -257,9 +280,37 @@ template <> struct Ops<float> {
     }
 };
 
+// Residual loads bypass L1 (ld.global.cg): L1 is not coherent between SMs, and
+// with programmatic dependent launch consecutive grids overlap on the SMs, so a
+// residual written two launches earlier must come from L2 (the field values
+// arrive by TMA, which reads L2).
+__device__ __forceinline__ uint32_t ld_l2_u32(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Compensated update of one value (MODE 2): returns the new stored value and
+// replaces *lo (bf16 pair, x in the low half) with the new residual.
+__device__ __forceinline__ float2 integrate_comp(float2 n, float hx, float hy, uint32_t &lo)
+{
+    __nv_bfloat162 lb;
+    memcpy(&lb, &lo, 4);
+    const float2 t = f2_add(__bfloat1622float2(lb), make_float2(hy, -hx));
+    const float2 s = f2_add(n, t);
+    const float2 b = f2_sub(s, n);
+    const float2 r = f2_add(f2_sub(n, f2_sub(s, b)), f2_sub(t, b));
+    lb = __floats2bfloat162_rn(r.x, r.y);
+    memcpy(&lo, &lb, 4);
+    return s;
+}
+
 template <typename T, int TX, int TY, int MODE, int POT, int STAGES, int MINB>
 __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_bcc2_kernel(const FusedArgs a)
 {
+    static_assert(MODE != 2 || sizeof(T) == 4, "compensated storage is an FP32 mode");
+    constexpr bool REAL = MODE != 1;  // MODE 0 and 2 advance real time
     using S = FusedShape<T, TX, TY>;
     using T2 = typename S::T2;
     constexpr int NT = S::NT;
@@ -328,7 +379,7 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
                     issued = k;
                     break;
                 }
-                const bool with_next = (MODE == 0) && (k >= 2);
+                const bool with_next = REAL && (k >= 2);
                 mbar_arrive_expect_tx(full + 8 * st, S::HALO_BYTES + (with_next ? S::NEXT_BYTES : 0));
                 // padded coordinates: x0-2 -> x0, y0-1 -> y0, plane q -> q+1
                 tma_load_4d(base + st * S::STAGE_BYTES, halo, w.x0 * S::XE, w.y0, 0, w.z0 + k, full + 8 * st);
@@ -355,6 +406,8 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
         const T Lw[2] = {T(d.Lc[0]), T(d.Lc[1])};
         const T L0 = T(d.L0), gdt = T(d.gdt);
         T2 *__restrict__ nxt = (T2 *)a.next;
+        uint32_t *__restrict__ nlo = a.next_lo;
+        uint32_t lo0 = 0u, lo1 = 0u, lo0n = 0u, lo1n = 0u;  // MODE 2: residuals of this / the next output plane
         const T *__restrict__ vpot = (const T *)a.vpot;
         T vxy0 = T(0), vxy1 = T(0);
         if (POT == GPE_POTENTIAL_TRAP && valid) {
@@ -374,6 +427,12 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
         const int lx = tx + 2, ly = ty + 1;
         for (int k = 0; k < nplanes; k++) {
             const int st = k % STAGES;
+            if (MODE == 2 && valid && k >= 1 && k + 1 < nplanes) {
+                // residuals of output plane z0+k-1, used in the next iteration
+                const long long i1 = col + (long long)(w.z0 + k - 1) * zstride;
+                lo0n = ld_l2_u32(nlo + i1);
+                lo1n = ld_l2_u32(nlo + i1 + plane);
+            }
             if (!mbar_wait_bounded(full + 8 * st, (k / STAGES) & 1)) {
                 atomicExch(a.err, kErrTimeout);
                 abort_flag = 1;
@@ -392,7 +451,7 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
             const T2 qB = at(Bp, 0, 0), qBxm = at(Bp, -1, 0), qBxp = at(Bp, 1, 0), qBym = at(Bp, 0, -1),
                      qByp = at(Bp, 0, 1), qBmm = at(Bp, -1, -1);
             T2 n0 = zero2, n1 = zero2;
-            if (MODE == 0 && k >= 2) {
+            if (REAL && k >= 2) {
                 const T2 *Np = (const T2 *)(sb + S::NEXT_OFF);
                 n0 = Np[ty * TX + tx];
                 n1 = Np[TX * TY + ty * TX + tx];
@@ -424,7 +483,9 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
                 S2[0] = sd0;
                 S2[1] = Ops<T>::add(Ops<T>::add(cm, qC), axyC);
                 Ops<T>::hpsi(cc, S2, Lw, L0, v0, gdt, hx, hy, nrm);
-                const T2 o0 = integrate<T, MODE>(n0, cc, hx, hy);
+                T2 o0;
+                if constexpr (MODE == 2) o0 = integrate_comp(n0, hx, hy, lo0);
+                else o0 = integrate<T, MODE>(n0, cc, hx, hy);
                 if (MODE == 1) {
                     s0.add(nrm);
                     s1.add(d_fma(cc.x, hx, d_mul(cc.y, hy)));
@@ -435,7 +496,9 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
                 S2[0] = Ops<T>::add(bCc, bCq);
                 S2[1] = Ops<T>::add(Ops<T>::add(bm, qB), axyB);
                 Ops<T>::hpsi(bc, S2, Lw, L0, v1, gdt, hx, hy, nrm);
-                const T2 o1 = integrate<T, MODE>(n1, bc, hx, hy);
+                T2 o1;
+                if constexpr (MODE == 2) o1 = integrate_comp(n1, hx, hy, lo1);
+                else o1 = integrate<T, MODE>(n1, bc, hx, hy);
                 if (MODE == 1) {
                     s0.add(nrm);
                     s1.add(d_fma(bc.x, hx, d_mul(bc.y, hy)));
@@ -445,7 +508,13 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
                 const long long i0 = col + z * zstride;
                 nxt[i0] = o0;
                 nxt[i0 + plane] = o1;
+                if (MODE == 2) {
+                    nlo[i0] = lo0;
+                    nlo[i0 + plane] = lo1;
+                }
             }
+            lo0 = lo0n;
+            lo1 = lo1n;
             cm = cc;
             cc = qC;
             bm = bc;
@@ -1039,7 +1108,7 @@ static cudaError_t launch_one(const FusedArgs &a, int grid, cudaStream_t s)
     // Real time: programmatic dependent launch.  Imaginary time ends every grid with
     // a serial fold in one CTA; there an early-scheduled next grid only holds SM
     // slots, so it launches plainly (the griddepcontrol instructions are then no-ops).
-    if (MODE == 0) return launch_pdl(kern, grid, FusedShape<T, TX, TY>::NTHREADS, bytes, s, a);
+    if (MODE != 1) return launch_pdl(kern, grid, FusedShape<T, TX, TY>::NTHREADS, bytes, s, a);
     kern<<<grid, FusedShape<T, TX, TY>::NTHREADS, bytes, s>>>(a);
     return cudaGetLastError();
 }
@@ -1047,6 +1116,12 @@ static cudaError_t launch_one(const FusedArgs &a, int grid, cudaStream_t s)
 template <typename T, int TX, int TY, int ST, int MB>
 static cudaError_t fused_launch_t(const FusedLaunch &l, const FusedArgs &a, cudaStream_t s)
 {
+    if constexpr (sizeof(T) == 4) {
+        if (l.mode == GPE_REAL_TIME && l.comp) {
+            if (l.potential == GPE_POTENTIAL_ARRAY) return launch_one<T, TX, TY, ST, MB, 2, 0>(a, l.grid, s);
+            return launch_one<T, TX, TY, ST, MB, 2, 1>(a, l.grid, s);
+        }
+    }
     if (l.mode == GPE_REAL_TIME) {
         if (l.potential == GPE_POTENTIAL_ARRAY) return launch_one<T, TX, TY, ST, MB, 0, 0>(a, l.grid, s);
         return launch_one<T, TX, TY, ST, MB, 0, 1>(a, l.grid, s);
@@ -1085,6 +1160,7 @@ cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s)
     a.src = l.src;
     a.prev = l.prev;
     a.next = l.next;
+    a.next_lo = (uint32_t *)l.next_lo;
     a.vpot = l.vpot;
     a.imag = l.imag;
     a.partials = l.partials;

@@ -53,6 +53,8 @@ cudaError_t launch_plain_step(const StepLaunch &l, cudaStream_t s);
 
 struct FusedLaunch {
     int precision, mode, potential, tile;
+    int comp;             // real time, FP32: compensated storage (next_lo holds the residuals)
+    void *next_lo;        // bf16x2 residual per value of the next field, same padded index
     const void *maps;     // CUtensorMap[num_instances][2 fields][2 boxes] in device memory
     int zcmax;            // longest z-range of a work item
     int src;              // field index of prev (0 or 1)
@@ -116,6 +118,11 @@ cudaError_t launch_pack(int precision, const InstDev *inst, int inst_index, int 
 cudaError_t launch_unpack(int precision, const InstDev *inst, int inst_index, int nx, int ny, int nz,
                           int slots, const void *field, void *host_order, const ImagScalars *imag,
                           cudaStream_t s);
+// GPE_FP32C: double host order <-> FP32 field plus bf16x2 residuals.
+cudaError_t launch_pack_split(const InstDev *inst, int ii, int nx, int ny, int nz, int slots, const void *host_order,
+                              void *field, void *lo, cudaStream_t s);
+cudaError_t launch_unpack_join(const InstDev *inst, int ii, int nx, int ny, int nz, int slots, const void *field,
+                               const void *lo, void *host_order, cudaStream_t s);
 // Field outputs (gpe_output.cu).
 cudaError_t launch_volume(int precision, const InstDev *inst, int ii, const void *field, double unit, int quirk,
                           uint16_t *out, long long total, cudaStream_t s);

@@ -8,7 +8,10 @@
 // reference's lanes are 192 bytes apart), and the neighbour table is read from
 // constant memory with a warp-uniform index.
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <cstring>
 
 #include "gpe_internal.h"
 
@@ -346,6 +349,59 @@ __global__ void scale_field_kernel(const InstDev *__restrict__ insts, int ii, T 
     }
 }
 
+// GPE_FP32C transfers.  Upload: a double x becomes hi = float(x) and the
+// residual lo = bf16(float(x - hi)) (x - hi is exact in double); download:
+// double(hi) + double(lo).  lo holds both components in one word, re in the low half.
+__global__ void pack_split_kernel(const InstDev *__restrict__ insts, int ii, const double *__restrict__ src,
+                                  float *__restrict__ hi, uint32_t *__restrict__ lo)
+{
+    const InstDev &d = insts[ii];
+    const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
+         v += (long long)gridDim.x * blockDim.x) {
+        long long r = v;
+        const int s = int(r % d.slots);
+        r /= d.slots;
+        const int x = int(r % d.nx);
+        r /= d.nx;
+        const int y = int(r % d.ny);
+        const int z = int(r / d.ny);
+        const long long o = field_index(d, s, x, y, z);
+        const double a = src[2 * v], b = src[2 * v + 1];
+        const float ha = __double2float_rn(a), hb = __double2float_rn(b);
+        hi[2 * o] = ha;
+        hi[2 * o + 1] = hb;
+        const __nv_bfloat162 l = __floats2bfloat162_rn(__double2float_rn(a - double(ha)), __double2float_rn(b - double(hb)));
+        uint32_t w;
+        memcpy(&w, &l, 4);
+        lo[o] = w;
+    }
+}
+
+__global__ void unpack_join_kernel(const InstDev *__restrict__ insts, int ii, const float *__restrict__ hi,
+                                   const uint32_t *__restrict__ lo, double *__restrict__ dst)
+{
+    const InstDev &d = insts[ii];
+    const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
+         v += (long long)gridDim.x * blockDim.x) {
+        long long r = v;
+        const int s = int(r % d.slots);
+        r /= d.slots;
+        const int x = int(r % d.nx);
+        r /= d.nx;
+        const int y = int(r % d.ny);
+        const int z = int(r / d.ny);
+        const long long o = field_index(d, s, x, y, z);
+        __nv_bfloat162 l;
+        const uint32_t w = lo[o];
+        memcpy(&l, &w, 4);
+        const float2 lf = __bfloat1622float2(l);
+        dst[2 * v] = double(hi[2 * o]) + double(lf.x);
+        dst[2 * v + 1] = double(hi[2 * o + 1]) + double(lf.y);
+    }
+}
+
 static int grid_for(long long total)
 {
     long long g = (total + 255) / 256;
@@ -375,6 +431,22 @@ cudaError_t launch_unpack(int precision, const InstDev *inst, int ii, int nx, in
         unpack_kernel<double><<<g, 256, 0, s>>>(inst, ii, (const double *)field, (double *)host_order, imag);
     else
         unpack_kernel<float><<<g, 256, 0, s>>>(inst, ii, (const float *)field, (float *)host_order, imag);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_split(const InstDev *inst, int ii, int nx, int ny, int nz, int slots, const void *host_order,
+                              void *field, void *lo, cudaStream_t s)
+{
+    const int g = grid_for((long long)nx * ny * nz * slots);
+    pack_split_kernel<<<g, 256, 0, s>>>(inst, ii, (const double *)host_order, (float *)field, (uint32_t *)lo);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_join(const InstDev *inst, int ii, int nx, int ny, int nz, int slots, const void *field,
+                               const void *lo, void *host_order, cudaStream_t s)
+{
+    const int g = grid_for((long long)nx * ny * nz * slots);
+    unpack_join_kernel<<<g, 256, 0, s>>>(inst, ii, (const float *)field, (const uint32_t *)lo, (double *)host_order);
     return cudaGetLastError();
 }
 

@@ -34,6 +34,9 @@ class Lattice(enum.IntEnum):
 class Precision(enum.IntEnum):
     FP64 = 0
     FP32 = 1
+    # FP32 fields with a bf16 residual per component carried across real-time
+    # steps (BCC2, fused kernel); fields are exchanged as float64.
+    FP32C = 2
 
 
 class Mode(enum.IntEnum):
@@ -355,6 +358,8 @@ class Stepper:
         _check(self.lib.gpe_create(C.byref(cfg), C.byref(h)), "gpe_create")
         self.h = h
         self.dtype = np.float64 if self.precision == Precision.FP64 else np.float32
+        # element type of host field arrays (GPE_FP32C exchanges fields as double)
+        self.field_dtype = np.float64 if self.precision != Precision.FP32 else np.float32
 
     # -- helpers ------------------------------------------------------------
     def shape(self, i: int):
@@ -364,8 +369,8 @@ class Stepper:
         return (inst.nz, inst.ny, inst.nx, self.slots)
 
     def _carray(self, a, shape, complex_=True):
-        """Host array in the handle's element type; complex fields may be given
-        as complex (shape) or interleaved real (shape + (2,))."""
+        """Host array in the handle's element type (fields: field_dtype); complex
+        fields may be given as complex (shape) or interleaved real (shape + (2,))."""
         if a is None:
             return None, None
         a = np.asarray(a)
@@ -380,7 +385,7 @@ class Stepper:
         if a.shape != want:
             raise ValueError(f"array shape {a.shape} does not match {want} "
                              "(block order (nz, ny, nx, slots), complex or interleaved (..., 2))")
-        a = np.ascontiguousarray(a, dtype=self.dtype)
+        a = np.ascontiguousarray(a, dtype=self.field_dtype if complex_ else self.dtype)
         return a, a.ctypes.data_as(C.c_void_p)
 
     # -- API ----------------------------------------------------------------
@@ -394,8 +399,8 @@ class Stepper:
 
     def download(self, i: int, odd: bool = True):
         shp = self.shape(i) + (2,)
-        e = np.empty(shp, self.dtype)
-        o = np.empty(shp, self.dtype) if odd else None
+        e = np.empty(shp, self.field_dtype)
+        o = np.empty(shp, self.field_dtype) if odd else None
         _check(self.lib.gpe_download(self.h, i, e.ctypes.data_as(C.c_void_p),
                                      o.ctypes.data_as(C.c_void_p) if odd else None), "gpe_download")
         return e, o
