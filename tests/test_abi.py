@@ -80,7 +80,7 @@ def test_binding_rejects_wrong_shapes():
     st = Stepper.__new__(Stepper)
     st.instances = [Instance(4, 3, 2, 0.5, 1e-3, 1.0)]
     st.slots = 2
-    st.dtype = np.float32
+    st.dtype = st.field_dtype = np.float32
     shp = st.shape(0)
     assert shp == (2, 3, 4, 2)
     with pytest.raises(ValueError):
