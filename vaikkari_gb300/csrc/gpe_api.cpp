@@ -81,6 +81,7 @@ struct gpe_handle_ {
     double *partials = nullptr;       // fused imaginary-time rows
     unsigned int *counter = nullptr;
     void *maps = nullptr;             // fused: CUtensorMap[num_instances][2][2] (fields or buffer sets)
+    void *lo_maps = nullptr;          // GPE_FP32C: CUtensorMap[num_instances][2] (residual arrays)
     int *err = nullptr;               // device error word of the bounded waits
     double *obs_partials = nullptr;   // observables CTA rows
     double *obs_sums = nullptr;       // per instance, 6 sums
@@ -240,6 +241,7 @@ gpe_status enqueue_step_real(gpe_handle h)
             l.src = half == 0 ? 0 : 1;
             l.comp = h->comp ? 1 : 0;
             l.next_lo = h->lo[half == 0 ? 1 : 0];
+            l.lo_maps = h->lo_maps;
             l.err = h->err;
             l.num_instances = h->cfg.num_instances;
             GPE_CUDA_TRY(launch_fused_step(l, h->stream));
@@ -454,6 +456,7 @@ void free_handle(gpe_handle h)
     cudaFree(h->obs_partials);
     cudaFree(h->obs_sums);
     cudaFree(h->maps);
+    cudaFree(h->lo_maps);
     cudaFree(h->err);
     cudaFree(h->staging);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -769,6 +772,20 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
         GPE_CREATE_TRY(cudaMalloc(&h->maps, sizeof(CUtensorMap) * maps.size()));
         GPE_CREATE_TRY(cudaMemcpyAsync(h->maps, maps.data(), sizeof(CUtensorMap) * maps.size(),
                                        cudaMemcpyHostToDevice, h->stream));
+        std::vector<CUtensorMap> lo_maps(h->comp ? 2 * cfg->num_instances : 0);
+        for (int i = 0; i < int(lo_maps.size()) / 2; i++)
+            for (int f = 0; f < 2; f++) {
+                gpe_status ms = make_residual_map(&lo_maps[2 * i + f], h->idev_host[i], h->lo[f], h->tile);
+                if (ms != GPE_OK) {
+                    free_handle(h);
+                    return ms;
+                }
+            }
+        if (!lo_maps.empty()) {
+            GPE_CREATE_TRY(cudaMalloc(&h->lo_maps, sizeof(CUtensorMap) * lo_maps.size()));
+            GPE_CREATE_TRY(cudaMemcpyAsync(h->lo_maps, lo_maps.data(), sizeof(CUtensorMap) * lo_maps.size(),
+                                           cudaMemcpyHostToDevice, h->stream));
+        }
         GPE_CREATE_TRY(cudaMalloc(&h->items_dev, sizeof(WorkItem) * h->items.size()));
         GPE_CREATE_TRY(cudaMemcpyAsync(h->items_dev, h->items.data(), sizeof(WorkItem) * h->items.size(),
                                        cudaMemcpyHostToDevice, h->stream));

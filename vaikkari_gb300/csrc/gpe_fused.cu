@@ -47,7 +47,10 @@
 // its rounding error:
 //   t = lo + (hy, -hx);  s = n + t;  b = s - n;  r = (n - (s - b)) + (t - b)
 // so the time accumulation keeps about 8 more bits than FP32 storage.  The
-// residuals are read from L2 (ld.global.cg) one plane ahead of their use.
+// residual tile travels by TMA in the same stage as the next field's tile (TMA
+// reads L2; plain loads through L1 saw stale residuals when consecutive grids
+// overlapped under programmatic dependent launch); results are stored from
+// registers.
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -66,6 +69,7 @@ struct FusedArgs {
     const WorkItem *__restrict__ items;
     int num_items;
     const CUtensorMap *maps;  // [instance][field][halo box, interior box]
+    const CUtensorMap *lo_maps;  // MODE 2: [instance][field] residual box
     int zcmax;                // longest z-range of a work item
     int src;                  // field the previous values come from (0 or 1)
     const void *prev;
@@ -162,7 +166,7 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map
 
 constexpr int kErrTimeout = 1;
 
-template <typename T, int TX, int TY>
+template <typename T, int TX, int TY, bool COMP = false>
 struct FusedShape {
     using T2 = typename Cplx<T>::type;
     static constexpr int NT = TX * TY;       // consumer threads
@@ -173,14 +177,19 @@ struct FusedShape {
     static constexpr int HALO_BYTES = 2 * SLOT * (int)sizeof(T2);
     static constexpr int NEXT_BYTES = 2 * TX * TY * (int)sizeof(T2);
     static constexpr int NEXT_OFF = ((HALO_BYTES + 127) / 128) * 128;
-    static constexpr int STAGE_BYTES = ((NEXT_OFF + NEXT_BYTES + 127) / 128) * 128;
+    // compensated storage: the residual tile, columns x0-2 .. x0+TX+1 (its copy
+    // starts on the 16-byte boundary of column x0-2), TY rows, both slots
+    static constexpr int LO_W = TX + 4;
+    static constexpr int LO_BYTES = COMP ? 2 * TY * LO_W * 4 : 0;
+    static constexpr int LO_OFF = ((NEXT_OFF + NEXT_BYTES + 127) / 128) * 128;
+    static constexpr int STAGE_BYTES = ((LO_OFF + LO_BYTES + 127) / 128) * 128;
     static constexpr int XE = (int)sizeof(T2) / 8;  // 8-byte TMA elements per complex
 };
 
-template <typename T, int TX, int TY, int STAGES>
+template <typename T, int TX, int TY, int STAGES, bool COMP = false>
 int fused_smem_bytes(int zcmax)
 {
-    return STAGES * FusedShape<T, TX, TY>::STAGE_BYTES + 128 /* align */ + 16 * STAGES /* barriers */ +
+    return STAGES * FusedShape<T, TX, TY, COMP>::STAGE_BYTES + 128 /* align */ + 16 * STAGES /* barriers */ +
            2 * zcmax * (int)sizeof(T) + 16;
 }
 
@@ -280,17 +289,6 @@ template <> struct Ops<float> {
     }
 };
 
-// Residual loads bypass L1 (ld.global.cg): L1 is not coherent between SMs, and
-// with programmatic dependent launch consecutive grids overlap on the SMs, so a
-// residual written two launches earlier must come from L2 (the field values
-// arrive by TMA, which reads L2).
-__device__ __forceinline__ uint32_t ld_l2_u32(const uint32_t *p)
-{
-    uint32_t v;
-    asm volatile("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
 // Compensated update of one value (MODE 2): returns the new stored value and
 // replaces *lo (bf16 pair, x in the low half) with the new residual.
 __device__ __forceinline__ float2 integrate_comp(float2 n, float hx, float hy, uint32_t &lo)
@@ -311,7 +309,7 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
 {
     static_assert(MODE != 2 || sizeof(T) == 4, "compensated storage is an FP32 mode");
     constexpr bool REAL = MODE != 1;  // MODE 0 and 2 advance real time
-    using S = FusedShape<T, TX, TY>;
+    using S = FusedShape<T, TX, TY, MODE == 2>;
     using T2 = typename S::T2;
     constexpr int NT = S::NT;
     constexpr int NWARPS = S::NTHREADS / 32;
@@ -380,12 +378,15 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
                     break;
                 }
                 const bool with_next = REAL && (k >= 2);
-                mbar_arrive_expect_tx(full + 8 * st, S::HALO_BYTES + (with_next ? S::NEXT_BYTES : 0));
+                mbar_arrive_expect_tx(full + 8 * st, S::HALO_BYTES + (with_next ? S::NEXT_BYTES + S::LO_BYTES : 0));
                 // padded coordinates: x0-2 -> x0, y0-1 -> y0, plane q -> q+1
                 tma_load_4d(base + st * S::STAGE_BYTES, halo, w.x0 * S::XE, w.y0, 0, w.z0 + k, full + 8 * st);
                 if (with_next)  // next field, interior tile of plane q-1 = z0+k-2
                     tma_load_4d(base + st * S::STAGE_BYTES + S::NEXT_OFF, inner, (w.x0 + 2) * S::XE, w.y0 + 1, 0,
                                 w.z0 + k - 1, full + 8 * st);
+                if (MODE == 2 && with_next)  // its residuals, from padded column x0 (16-byte aligned)
+                    tma_load_4d(base + st * S::STAGE_BYTES + S::LO_OFF, a.lo_maps + 2 * w.inst + (1 - a.src), w.x0,
+                                w.y0 + 1, 0, w.z0 + k - 1, full + 8 * st);
                 issued = k + 1;
             }
             if (abort_flag) {
@@ -407,7 +408,7 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
         const T L0 = T(d.L0), gdt = T(d.gdt);
         T2 *__restrict__ nxt = (T2 *)a.next;
         uint32_t *__restrict__ nlo = a.next_lo;
-        uint32_t lo0 = 0u, lo1 = 0u, lo0n = 0u, lo1n = 0u;  // MODE 2: residuals of this / the next output plane
+        uint32_t lo0 = 0u, lo1 = 0u;  // MODE 2: residuals of the output plane
         const T *__restrict__ vpot = (const T *)a.vpot;
         T vxy0 = T(0), vxy1 = T(0);
         if (POT == GPE_POTENTIAL_TRAP && valid) {
@@ -427,12 +428,6 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
         const int lx = tx + 2, ly = ty + 1;
         for (int k = 0; k < nplanes; k++) {
             const int st = k % STAGES;
-            if (MODE == 2 && valid && k >= 1 && k + 1 < nplanes) {
-                // residuals of output plane z0+k-1, used in the next iteration
-                const long long i1 = col + (long long)(w.z0 + k - 1) * zstride;
-                lo0n = ld_l2_u32(nlo + i1);
-                lo1n = ld_l2_u32(nlo + i1 + plane);
-            }
             if (!mbar_wait_bounded(full + 8 * st, (k / STAGES) & 1)) {
                 atomicExch(a.err, kErrTimeout);
                 abort_flag = 1;
@@ -455,6 +450,11 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
                 const T2 *Np = (const T2 *)(sb + S::NEXT_OFF);
                 n0 = Np[ty * TX + tx];
                 n1 = Np[TX * TY + ty * TX + tx];
+                if (MODE == 2) {
+                    const uint32_t *Lp = (const uint32_t *)(sb + S::LO_OFF);
+                    lo0 = Lp[ty * S::LO_W + tx + 2];
+                    lo1 = Lp[(TY + ty) * S::LO_W + tx + 2];
+                }
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(empty + 8 * st);  // this warp is done with stage st
@@ -513,8 +513,6 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
                     nlo[i0 + plane] = lo1;
                 }
             }
-            lo0 = lo0n;
-            lo1 = lo1n;
             cm = cc;
             cc = qC;
             bm = bc;
@@ -998,6 +996,35 @@ gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *f
     return GPE_OK;
 }
 
+// The residual map of one field of one instance (GPE_FP32C): 4-D over the
+// padded layout in 32-bit words (x, y, slot, z); box TX + 4 columns from a
+// 16-byte-aligned column, TY rows, both slots, one plane.
+gpe_status make_residual_map(void *out_map, const InstDev &d, void *lo_arena, int tile)
+{
+    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+        return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    Encode encode = (Encode)fn;
+    int tx, ty;
+    fused_tile_shape(tile, &tx, &ty);
+    const cuuint64_t dims[4] = {(cuuint64_t)d.px, (cuuint64_t)d.py, 2, (cuuint64_t)d.nz + 2};
+    const cuuint64_t strides[3] = {(cuuint64_t)d.px * 4, (cuuint64_t)d.plane * 4, (cuuint64_t)d.zstride * 4};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const cuuint32_t box[4] = {(cuuint32_t)(tx + 4), (cuuint32_t)ty, 2, 1};
+    void *gaddr = (char *)lo_arena + (size_t)d.base * 4;
+    CUresult r = encode((CUtensorMap *)out_map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, gaddr, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return GPE_OK;
+}
+
 // The two-step kernel's maps of one buffer set of one instance: out_map[0] the
 // E box (tile plus 2 columns either side, 2 rows either side), out_map[1] the O
 // box (tile plus 2 columns, 1 row either side); both slots, one plane.
@@ -1097,7 +1124,7 @@ cudaError_t launch_twostep(const FusedLaunch &l, cudaStream_t s)
 template <typename T, int TX, int TY, int ST, int MB, int MODE, int POT>
 static cudaError_t launch_one(const FusedArgs &a, int grid, cudaStream_t s)
 {
-    const int bytes = fused_smem_bytes<T, TX, TY, ST>(a.zcmax);
+    const int bytes = fused_smem_bytes<T, TX, TY, ST, MODE == 2>(a.zcmax);
     auto kern = fused_bcc2_kernel<T, TX, TY, MODE, POT, ST, MB>;
     static int allowed = 48 * 1024;  // dynamic shared memory granted to this instantiation
     if (bytes > allowed) {
@@ -1156,6 +1183,7 @@ cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s)
     a.items = l.items;
     a.num_items = l.num_items;
     a.maps = (const CUtensorMap *)l.maps;
+    a.lo_maps = (const CUtensorMap *)l.lo_maps;
     a.zcmax = l.zcmax;
     a.src = l.src;
     a.prev = l.prev;

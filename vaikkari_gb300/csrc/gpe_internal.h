@@ -55,6 +55,7 @@ struct FusedLaunch {
     int precision, mode, potential, tile;
     int comp;             // real time, FP32: compensated storage (next_lo holds the residuals)
     void *next_lo;        // bf16x2 residual per value of the next field, same padded index
+    const void *lo_maps;  // CUtensorMap[num_instances][2 fields] of the residual arrays
     const void *maps;     // CUtensorMap[num_instances][2 fields][2 boxes] in device memory
     int zcmax;            // longest z-range of a work item
     int src;              // field index of prev (0 or 1)
@@ -89,6 +90,8 @@ void fused_variant(int tile, int *tx, int *ty, int *stages, int *minb);
 // Encodes the fused kernel's two 4-D tensor maps (halo box, interior box) of
 // one field of one instance into out_map[0..1].
 gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *field_arena, int tile);
+// GPE_FP32C: the 4-D map of one field's residual array (32-bit words).
+gpe_status make_residual_map(void *out_map, const InstDev &d, void *lo_arena, int tile);
 
 struct ObsLaunch {
     int lattice, precision, potential;
