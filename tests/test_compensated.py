@@ -8,7 +8,8 @@ compensated leapfrog against FP64 of the same scheme (much closer than plain
 FP32).  GPU: the fused kernel's compensated mode equals the oracle bit for bit
 (values and residuals, through the float64 download), refuses the set-ups it
 does not cover, and keeps a strongly interacting condensate of the 64-instance
-batch within 1e-5 of FP64 after 1000 steps where plain FP32 is above 1e-4."""
+batch within 1e-5 of FP64 after 1000 steps where plain FP32 is above 1e-4; the
+whole batch, run twice, gives identical results in FP32 and FP32C."""
 import numpy as np
 import pytest
 
@@ -189,3 +190,31 @@ def test_fp32c_strongly_interacting_condensate_within_1e5():
     errc = rel_l2(out[Precision.FP32C][0], ref)
     assert errc < 1e-5 < err32, (errc, err32)
     assert abs(out[Precision.FP32C][1] - n64) / n64 <= 1e-6
+
+
+@pytest.mark.gpu
+def test_batch_runs_are_identical():
+    """The 64-instance batch, 120 steps (a graph of 100 plus 20 launches), run twice:
+    identical fields in FP32 and FP32C.  Consecutive launches overlap on the SMs
+    under programmatic dependent launch; data a launch reads that an earlier launch
+    wrote must not come from a stale L1 line (an earlier form of the residual loads
+    failed exactly this)."""
+    from vaikkari_gb300 import workloads
+    conds = workloads.config4()
+    insts = [c.inst for c in conds]
+
+    def run(prec):
+        st = Stepper(insts, lattice=Lattice.BCC2, precision=prec, kernel=Kernel.FUSED, potential=Potential.TRAP,
+                     graph_steps=100)
+        for k, c in enumerate(conds):
+            st.upload(k, c.psi, c.psi)
+        st.step(120)
+        out = [st.download(k) for k in range(len(insts))]
+        st.close()
+        return out
+
+    for prec in (Precision.FP32, Precision.FP32C):
+        a, b = run(prec), run(prec)
+        diff = [i for i in range(len(insts)) if not (np.array_equal(a[i][0], b[i][0]) and
+                                                     np.array_equal(a[i][1], b[i][1]))]
+        assert not diff, (prec.name, diff)
