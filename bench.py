@@ -46,9 +46,9 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _profile_traffic():
+def _profile_traffic(name="fused_bcc2_batch64.md"):
     """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "fused_bcc2_batch64.md")
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -313,14 +313,18 @@ def run_ours(args):
     verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
     verts_job = _sum_over_ranks(dist, verts, device=torch.device("cuda", local))
     tile, zchunk, tuned = args.tile, args.zchunk, None
+    comp_main = args.precision == "fp32c"
+    prec = Precision.FP32C if comp_main else Precision.FP32
+    host_t = np.float64 if comp_main else np.float32
+    bytes_vs = BYTES_PER_VERTEX_STEP_COMP if comp_main else BYTES_PER_VERTEX_STEP
     if tile < 0:
         # untimed: pick the kernel variant and z-chunk for this batch (cached per device)
         from vaikkari_gb300.autotune import autotune
-        tuned = autotune(insts, precision=Precision.FP32, potential=Potential.TRAP, device=local)
+        tuned = autotune(insts, precision=prec, potential=Potential.TRAP, device=local)
         tile, zchunk = tuned["tile"], tuned["zchunk"]
-    st = Stepper(insts, lattice=Lattice.BCC2, precision=Precision.FP32, kernel=Kernel.FUSED,
+    st = Stepper(insts, lattice=Lattice.BCC2, precision=prec, kernel=Kernel.FUSED,
                  potential=Potential.TRAP, graph_steps=100, tile=tile, zchunk=zchunk, device=local)
-    evens, odds = prepare_fields(st, conds, np.float32)
+    evens, odds = prepare_fields(st, conds, host_t)
 
     # Warm-up: W steps, plus one replay of the 100-step graph so that the
     # graph is instantiated before the timed region.
@@ -349,15 +353,16 @@ def run_ours(args):
     # (two launches per step), so the average launch lasts ms / launches.
     peak, peak_kind = _peaks()
     per_launch_s = (ms * 1e-3) / max(launches, 1)
-    achieved = verts * (BYTES_PER_VERTEX_STEP / 2) / per_launch_s / 1e9
-    traffic = _profile_traffic()
+    achieved = verts * (bytes_vs / 2) / per_launch_s / 1e9
+    traffic = _profile_traffic("fused_bcc2_fp32c_batch64.md" if comp_main else "fused_bcc2_batch64.md")
 
     # End to end through the public API with pinned host buffers: upload every
     # instance, run the steps, read the observables, download every field.
     pinned_e, pinned_o = [], []
     for e, o in zip(evens, odds):
-        pe = torch.empty(e.shape, dtype=torch.float32, pin_memory=True).numpy()
-        po = torch.empty(o.shape, dtype=torch.float32, pin_memory=True).numpy()
+        tt = torch.float64 if comp_main else torch.float32
+        pe = torch.empty(e.shape, dtype=tt, pin_memory=True).numpy()
+        po = torch.empty(o.shape, dtype=tt, pin_memory=True).numpy()
         pe[...] = e
         po[...] = o
         pinned_e.append(pe)
@@ -386,7 +391,7 @@ def run_ours(args):
 
     # The same batch with compensated FP32 storage (accuracy in `accuracy`).
     comp = None
-    if rank == 0 and not args.skip_comp:
+    if rank == 0 and not args.skip_comp and not comp_main:
         comp = compensated_block(conds, insts, local, args.steps, args.warmup, tune=args.tile < 0)
 
     # The FP64 plain path, one instance at a time (the drop-in denominator).
@@ -411,7 +416,8 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": args.scaling, "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batch64_bcc2_fp32_trap_realtime", "instances": len(insts),
+            "config": {"workload": "batch64_bcc2_fp32_trap_realtime" + ("_compensated" if comp_main else ""),
+                       "storage": "fp32 + bf16 residual" if comp_main else "fp32", "instances": len(insts),
                        "vertices": verts, "vertices_all_ranks": verts_job,
                        "sizes": sorted({i.nx for i in insts}), "dt": 1e-4,
                        "graph_steps": 100, "kernel": "fused", "variant": tile, "zchunk": zchunk,
@@ -421,7 +427,7 @@ def run_ours(args):
                        "l2": f"inputs larger than L2 (fields {2 * 8 * verts / 1e6:.0f} MB vs {L2_BYTES / 1e6:.0f} MB)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "algorithmic_bytes_per_vertex_step": BYTES_PER_VERTEX_STEP,
+                         "algorithmic_bytes_per_vertex_step": bytes_vs,
                          "peak_source": f"{peak_kind} hbm_gbs", "kernel": "fused_bcc2_kernel"},
             "gpu_launches": launches,
             "clocks": clk.summary(),
@@ -519,6 +525,7 @@ def compensated_block(conds, insts, device, steps, warmup, tune=True):
     return {"value": verts * steps / (ms * 1e-3), "unit": METRIC, "ms_per_step": ms / steps, "steps": steps,
             "variant": tile, "zchunk": zchunk, "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": _profile_traffic("fused_bcc2_fp32c_batch64.md"),
                          "algorithmic_bytes_per_vertex_step": BYTES_PER_VERTEX_STEP_COMP,
                          "peak_source": f"{kind} hbm_gbs"},
             "storage": "FP32 value + bf16 residual per component (12 B per value and field)"}
@@ -876,6 +883,8 @@ def main():
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-comp", action="store_true", help="skip the compensated-storage (FP32C) timing")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32c"],
+                    help="batch64: storage of the timed path (fp32c = FP32 + bf16 residual)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--workload", default="batch64",
                     help="batch64 (the headline), config1/config2/config3/config5 (accuracy cases), relax "
