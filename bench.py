@@ -846,11 +846,48 @@ def _tmp_save(v):
     return path
 
 
+def run_tetra12(args):
+    """The drop-in's arithmetic on the production grid: TETRA12 (the reference's
+    discretisation, 12 values per block), plain kernel, array potential, one
+    instance of 87 x 87 x 302 blocks (main()'s grid at block scale 0.06997) with
+    seeded random fields.  FP64 (bit-identical to the reference's kernel) and FP32,
+    each timed with CUDA events over --steps steps (best of three) after a graph
+    of 100 steps."""
+    from vaikkari_gb300.gpe import Instance, Kernel, Lattice, Potential, Precision, Stepper
+    rng = np.random.default_rng(5)
+    inst = Instance(87, 87, 302, 0.06997, 1e-4, 100.0, origin=(-3.0, -3.0, -10.0))
+    shp = (inst.nz, inst.ny, inst.nx, 12)
+    e = (rng.standard_normal(shp) + 1j * rng.standard_normal(shp)) * 0.3
+    o = (rng.standard_normal(shp) + 1j * rng.standard_normal(shp)) * 0.3
+    V = rng.uniform(0.0, 10.0, shp)
+    vals = inst.nx * inst.ny * inst.nz * 12
+    rates = {}
+    for name, prec in (("fp64", Precision.FP64), ("fp32", Precision.FP32)):
+        st = Stepper([inst], lattice=Lattice.TETRA12, precision=prec, kernel=Kernel.PLAIN,
+                     potential=Potential.ARRAY, graph_steps=100)
+        st.upload(0, e, o, V)
+        st.time_steps(100)
+        ms = min(st.time_steps(args.steps) for _ in range(3))
+        st.close()
+        rates[name] = vals * args.steps / (ms * 1e-3)
+    line = {"metric": METRIC, "value": rates["fp64"], "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "tetra12_plain_production_grid", "values": vals, "blocks": [87, 87, 302],
+                       "lattice": "TETRA12", "kernel": "plain", "potential": "array"},
+            "fp32": rates["fp32"],
+            "note": "FP64 performs the reference kernel's rounded operations (16 FP64 operations per value "
+                    "and half-step); its bound is this GPU's FP64 rate"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_workload(args):
     from vaikkari_gb300 import workloads
     name = args.workload
     if name == "relax":
         return run_relax(args)
+    if name == "tetra12":
+        return run_tetra12(args)
     if name == "production":
         return run_production(args)
     if name == "config1":
@@ -888,7 +925,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--workload", default="batch64",
                     help="batch64 (the headline), config1/config2/config3/config5 (accuracy cases), relax "
-                         "(the vortex relaxation) or production (main() at production size)")
+                         "(the vortex relaxation), production (main() at production size) or tetra12 (the "
+                         "drop-in's FP64/FP32 kernel on the production grid)")
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
                     help="multi-GPU split: weak = 64 condensates per rank, strong = the 64 split over ranks")
     ap.add_argument("--production-iters", type=int, default=2)

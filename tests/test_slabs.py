@@ -6,7 +6,9 @@ half-step evolves exactly as the undivided grid.
 CPU: the oracle on gloo ranks (world size 2), each rank a slab with one ghost
 plane per side, halo planes sent between ranks; bit-identical to the undivided
 oracle.  GPU: SlabStepper (slabs of one batch, exchanged by the library) against
-one Stepper on the whole grid, bit-identical, plain and fused kernels."""
+one Stepper on the whole grid, bit-identical, plain and fused kernels, and with
+compensated storage (halo planes carry the FP32 values; residuals are needed
+only where values are updated)."""
 import os
 import socket
 
@@ -126,6 +128,7 @@ def test_slab_halo_exchange_on_cpu_ranks_is_exact():
     ("BCC2", "FP64", "FUSED", "ARRAY", 2, 120),
     ("BCC2", "FP32", "PLAIN", "ARRAY", 4, 37),
     ("TETRA12", "FP64", "PLAIN", "ARRAY", 3, 130),
+    ("BCC2", "FP32C", "FUSED", "TRAP", 3, 130),
 ])
 def test_slab_stepper_equals_undivided_grid(lattice_name, precision, kernel, potential, slabs, steps):
     """Slabs of one batch with library-side halo exchange against the whole grid
