@@ -13,14 +13,23 @@ from vaikkari_gb300.gpe import GpeError, Instance, Kernel, Lattice, Potential, P
 pytestmark = pytest.mark.gpu
 
 
-def _stepper(kernel=Kernel.FUSED):
+def _stepper(kernel=Kernel.FUSED, tile=0):
     inst = Instance(8, 8, 8, 0.4, 1e-3, 50.0, origin=(-1.6, -1.6, -1.6))
     return Stepper([inst], lattice=Lattice.BCC2, precision=Precision.FP32, kernel=kernel, potential=Potential.TRAP,
-                   graph_steps=-1)
+                   graph_steps=-1, tile=tile)
 
 
-def test_bounded_wait_timeout_is_reported_and_context_survives():
-    st = _stepper()
+def _tiles():
+    """The default variant and the first and last whole-step variants (double
+    buffered sets; their consumers agree on a timeout at the per-plane barrier)."""
+    from vaikkari_gb300.gpe import variants
+    two = [v["tile"] for v in variants() if v["half_steps"] == 2]
+    return [0, two[0], two[-1]]
+
+
+@pytest.mark.parametrize("which", [0, 1, 2])
+def test_bounded_wait_timeout_is_reported_and_context_survives(which):
+    st = _stepper(tile=_tiles()[which])
     shp = st.shape(0)
     e, o = random_state(shp, 1, 0.3), random_state(shp, 2, 0.3)
     st.upload(0, e, o)
