@@ -171,6 +171,35 @@ def test_imaginary_time_fp64_matches_oracle(lattice, kernel):
     assert mu[0] == pytest.approx(mu_hist[-1], rel=1e-11)
 
 
+@pytest.mark.parametrize("prec", [Precision.FP64, Precision.FP32])
+def test_imaginary_time_batch_equals_single_runs(prec):
+    """Three different condensates in one fused imaginary-time batch: each ends
+    bit-identical to its own single-instance run (same variant and z-chunk, so
+    the same work items; each instance's rows fold in a fixed order), including
+    mu and the step count at convergence."""
+    insts = [Instance(10, 9, 8, 0.45, 2e-3, 40.0, origin=(-2.25, -2.0, -1.8), trap=(1.0, 1.0, 4.0)),
+             Instance(17, 6, 13, 0.4, 1e-3, 10.0, origin=(-3.4, -1.2, -2.6)),
+             Instance(33, 12, 5, 0.3, 3e-3, 80.0, origin=(-4.95, -1.8, -0.75), trap=(2.0, 0.5, 1.0))]
+    rng = np.random.default_rng(8)
+    psis = [np.exp(1j * rng.uniform(0, 2 * np.pi, size=(i.nz, i.ny, i.nx, 2))) for i in insts]
+    kw = dict(lattice=Lattice.BCC2, precision=prec, mode=Mode.IMAGINARY, kernel=Kernel.FUSED,
+              potential=Potential.TRAP, graph_steps=20, tile=2, zchunk=4)
+    st = Stepper(insts, **kw)
+    for i, p in enumerate(psis):
+        st.upload(i, p)
+    steps, conv, mu = st.imaginary_time(150, 1e-6)
+    batch = [st.download(i, odd=False)[0] for i in range(len(insts))]
+    st.close()
+    for i, p in enumerate(psis):
+        one = Stepper([insts[i]], **kw)
+        one.upload(0, p)
+        s1, c1, mu1 = one.imaginary_time(steps, 0.0)
+        got = one.download(0, odd=False)[0]
+        one.close()
+        np.testing.assert_array_equal(batch[i], got)
+        assert mu[i] == mu1[0]
+
+
 @pytest.mark.parametrize("kernel", [Kernel.PLAIN, Kernel.FUSED])
 def test_imaginary_time_converges_to_harmonic_ground_state(kernel):
     """g = 0, isotropic trap: mu -> 3/2 up to the O(a^2) discretisation error."""

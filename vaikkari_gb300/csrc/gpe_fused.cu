@@ -308,6 +308,7 @@ template <typename T, int TX, int TY, int MODE, int POT, int STAGES, int MINB>
 __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_bcc2_kernel(const FusedArgs a)
 {
     static_assert(MODE != 2 || sizeof(T) == 4, "compensated storage is an FP32 mode");
+    static_assert(MODE != 1 || TX * TY + 32 > 64, "the imaginary-time fold uses threads 0, 32 and 64");
     constexpr bool REAL = MODE != 1;  // MODE 0 and 2 advance real time
     using S = FusedShape<T, TX, TY, MODE == 2>;
     using T2 = typename S::T2;
@@ -321,6 +322,7 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
     const uint32_t empty = full + 8 * STAGES;
     T *const ztab = (T *)(gbase + STAGES * S::STAGE_BYTES + 16 * STAGES);
     __shared__ int abort_flag;
+    __shared__ double row_sums[4];  // imaginary time: this work item's four sums
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
@@ -535,26 +537,33 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
             if (tid < 4) {
                 double t = 0.0;
                 for (int wi = 0; wi < NT / 32; wi++) t += red[wi][tid];
-                a.partials[4ll * it + tid] = t;
+                row_sums[tid] = t;
             }
         }
     }
 
     launch_dependents();  // the next grid may be scheduled; it waits for this one to finish
     if (MODE == 1) {
-        // Last CTA to finish reduces every instance's rows (fixed order).
+        // Last CTA to finish reduces every instance's rows (fixed order).  The
+        // producer warp's first lane publishes this CTA's row: it has no field
+        // stores in flight, so its fence only waits for the row itself (a fence
+        // in a consumer thread waits for all of that thread's output stores).
         __shared__ bool last;
-        __threadfence();
         __syncthreads();
         if (abort_flag) return;
-        if (tid == 0) last = (atomicAdd(a.counter, 1u) == gridDim.x - 1);
+        if (warp == NWARPS - 1 && lane == 0) {
+            for (int k = 0; k < 4; k++) a.partials[4ll * it + k] = row_sums[k];
+            __threadfence();
+            last = (atomicAdd(a.counter, 1u) == gridDim.x - 1);
+            if (last) __threadfence();
+        }
         __syncthreads();
         if (!last) return;
-        __threadfence();
         // Each instance's rows are summed by the whole CTA: thread t folds rows
         // b+t, b+t+NTHREADS, ... (compensated), then warps and the CTA combine
         // in a fixed order, so the result does not depend on timing.
         __shared__ double fin[NWARPS][4];
+        __shared__ double tot[4];
         for (int i = 0; i < a.num_instances; i++) {
             const int b = a.inst_item_begin[2 * i], e = a.inst_item_begin[2 * i + 1];
             double sk[4] = {0.0, 0.0, 0.0, 0.0}, ck[4] = {0.0, 0.0, 0.0, 0.0};
@@ -576,25 +585,31 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
             if (lane == 0)
                 for (int k = 0; k < 4; k++) fin[warp][k] = sk[k];
             __syncthreads();
+            // The fold is the serial tail of every imaginary-time step, and FP64
+            // operations are long-latency here: the four sums run on four lanes
+            // at once, and the three scalars on three warps at once (same
+            // operations and order as one thread doing all of it).
+            if (tid < 4) {
+                double acc = 0.0;
+                for (int wi = 0; wi < NWARPS; wi++) acc += fin[wi][tid];
+                tot[tid] = acc;
+            }
+            __syncthreads();
+            // tot: |p'|^2, Re(conj(p') dt H p'), |p'|^4, |next|^2 over values
+            const InstDev &di = a.inst[i];
+            ImagScalars &sc = a.imag[i];
             if (tid == 0) {
-                double acc[4];
-                for (int k = 0; k < 4; k++) {
-                    acc[k] = 0.0;
-                    for (int wi = 0; wi < NWARPS; wi++) acc[k] += fin[wi][k];
-                }
-                const InstDev &di = a.inst[i];
-                ImagScalars &sc = a.imag[i];
-                // acc: |p'|^2, Re(conj(p') dt H p'), |p'|^4, |next|^2 over values
-                const double nin = di.vol * acc[0];
-                const double mu = acc[1] / (di.dt * acc[0]);
-                sc.norm_in = nin;
-                sc.energy = di.vol * (acc[1] / di.dt - 0.5 * di.g * acc[2]);
+                const double mu = tot[1] / (di.dt * tot[0]);
                 sc.mu_prev = sc.mu;
                 sc.mu = mu;
                 sc.dmu = (sc.steps > 0) ? fabs(mu - sc.mu_prev) : INFINITY;
                 if (sc.steps > 0 && sc.conv_step < 0 && sc.dmu < a.tol) sc.conv_step = sc.steps;
                 sc.steps += 1;
-                sc.sigma = 1.0 / sqrt(di.vol * acc[3]);
+            } else if (tid == 32) {
+                sc.norm_in = di.vol * tot[0];
+                sc.energy = di.vol * (tot[1] / di.dt - 0.5 * di.g * tot[2]);
+            } else if (tid == 64) {
+                sc.sigma = 1.0 / sqrt(di.vol * tot[3]);
             }
             __syncthreads();
         }
