@@ -183,12 +183,13 @@ def prepare_fields(stepper, conds, precision_dtype):
     return evens, odds
 
 
-def cpu_sample(conds, evens64, odds64, budget_s, threads):
+def cpu_sample(conds, evens64, odds64, budget_s, threads, lattice=None):
     """Oracle FP64 leapfrog (the reference's update restated in C, all threads)
     over the batch, as many whole steps as fit the time budget (>= 1)."""
     import oracle.oracle as orc
     from vaikkari_gb300.gpe import Lattice, lattice_info
-    info = lattice_info(Lattice.BCC2)
+    lattice = Lattice.BCC2 if lattice is None else lattice
+    info = lattice_info(lattice)
     orc.set_threads(threads)
     grids, vdts, es, os_ = [], [], [], []
     for c, e, o in zip(conds, evens64, odds64):
@@ -202,12 +203,15 @@ def cpu_sample(conds, evens64, odds64, budget_s, threads):
         vdts.append(vdt)
         es.append(e.copy())
         os_.append(o.copy())
-    verts = sum(c.inst.nx * c.inst.ny * c.inst.nz * 2 for c in conds)
+    verts = sum(c.inst.nx * c.inst.ny * c.inst.nz * info["slots"] for c in conds)
     t0 = time.perf_counter()
     steps = 0
     while True:
         for g, e, o, v in zip(grids, es, os_, vdts):
-            g.leapfrog_bcc2_fast(e, o, v, 1)
+            if lattice == Lattice.BCC2:
+                g.leapfrog_bcc2_fast(e, o, v, 1)
+            else:
+                g.leapfrog(e, o, v, 1)
         steps += 1
         el = time.perf_counter() - t0
         if el >= budget_s or steps >= 1000:
@@ -561,10 +565,11 @@ def fp64_plain_rate(conds, insts, device, steps):
 # ---------------------------------------------------------------------------
 # The other configurations: parity and accuracy cases (not the headline line).
 
-def _stepper(conds, prec, kernel, mode, tile=0, graph_steps=100, device=0, zchunk=0):
+def _stepper(conds, prec, kernel, mode, tile=0, graph_steps=100, device=0, zchunk=0, lattice=None):
     from vaikkari_gb300.gpe import Lattice, Potential, Stepper
-    return Stepper([c.inst for c in conds], lattice=Lattice.BCC2, precision=prec, kernel=kernel, mode=mode,
-                   potential=Potential.TRAP, graph_steps=graph_steps, tile=tile, device=device, zchunk=zchunk)
+    return Stepper([c.inst for c in conds], lattice=Lattice.BCC2 if lattice is None else lattice, precision=prec,
+                   kernel=kernel, mode=mode, potential=Potential.TRAP, graph_steps=graph_steps, tile=tile,
+                   device=device, zchunk=zchunk)
 
 
 def _rel_l2(a, b):
@@ -591,28 +596,35 @@ def _download(st, n):
     return [st.download(i, odd=False)[0] for i in range(n)]
 
 
-def _cpu_config_rate(conds, budget_s=5.0):
+def _cpu_config_rate(conds, budget_s=5.0, lattice=None):
     """FP64 oracle port on all host threads: whole leapfrog steps of every
     condensate for about `budget_s` seconds (at least one step)."""
     e64 = [np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1)) for c in conds]
-    v, n, el, nv = cpu_sample(conds, e64, [a.copy() for a in e64], budget_s, os.cpu_count() or 1)
+    v, n, el, nv = cpu_sample(conds, e64, [a.copy() for a in e64], budget_s, os.cpu_count() or 1, lattice)
     return {"value": v, "unit": METRIC, "cores": os.cpu_count() or 1, "kind": "port",
             "sample": f"{n} leapfrog step(s), {nv} vertices, FP64 oracle port, {el:.2f} s"}
 
 
-def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1):
-    """FP32 fused against FP64 fused of the same scheme at each checkpoint, plus
-    throughput of the FP32 fused and FP64 plain paths."""
-    from vaikkari_gb300.gpe import Kernel, Mode, Precision
+def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1, lattice=None):
+    """FP32 against FP64 of the same scheme at each checkpoint, plus throughput.
+    BCC2 (config-mode): the fused kernel, and the FP64 plain path beside it.
+    TETRA12 (ref-mode, the reference's discretisation): the plain kernel."""
+    from vaikkari_gb300.gpe import Kernel, Lattice, Mode, Precision
+    lattice = Lattice.BCC2 if lattice is None else Lattice(lattice)
+    ref_mode = lattice == Lattice.TETRA12
     insts = [c.inst for c in conds]
-    verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
-    if tile < 0:
+    slots = 12 if ref_mode else 2
+    verts = sum(i.nx * i.ny * i.nz for i in insts) * slots
+    kern = Kernel.PLAIN if ref_mode else Kernel.FUSED
+    if ref_mode:
+        tile = 0
+    elif tile < 0:
         from vaikkari_gb300.autotune import autotune
         tile = autotune(insts)["tile"]
     fp64_last = fp64_steps or checkpoints[-1]
     runs = {}
     for prec, dt_, last in ((Precision.FP64, np.float64, fp64_last), (Precision.FP32, np.float32, checkpoints[-1])):
-        st = _stepper(conds, prec, Kernel.FUSED, Mode.REAL, tile=tile)
+        st = _stepper(conds, prec, kern, Mode.REAL, tile=tile, lattice=lattice)
         prepare_fields(st, conds, dt_)
         o0 = st.observables(0)
         done, cps = 0, {}
@@ -641,33 +653,45 @@ def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1):
         acc.append(row)
     # throughput: FP32 fused and FP64 plain, device time of 200 steps after warm-up
     rates = {}
-    for key, prec, kern in (("fp32_fused", Precision.FP32, Kernel.FUSED), ("fp64_fused", Precision.FP64, Kernel.FUSED),
-                            ("fp64_plain", Precision.FP64, Kernel.PLAIN)):
-        st = _stepper(conds, prec, kern, Mode.REAL, tile=tile)
+    cases = ((("fp32_plain", Precision.FP32, Kernel.PLAIN), ("fp64_plain", Precision.FP64, Kernel.PLAIN)) if ref_mode
+             else (("fp32_fused", Precision.FP32, Kernel.FUSED), ("fp64_fused", Precision.FP64, Kernel.FUSED),
+                   ("fp64_plain", Precision.FP64, Kernel.PLAIN)))
+    for key, prec, kern_ in cases:
+        st = _stepper(conds, prec, kern_, Mode.REAL, tile=tile, lattice=lattice)
         prepare_fields(st, conds, np.float64 if prec == Precision.FP64 else np.float32)
         st.time_steps(103)
         ms = min(st.time_steps(200) for _ in range(2))
         rates[key] = verts * 200 / (ms * 1e-3)
         st.close()
-    return {"metric": METRIC, "value": rates["fp32_fused"], "unit": METRIC, "dtype": "f32",
-            "config": {"workload": name, "instances": len(insts), "vertices": verts, "dt": insts[0].dt,
-                       "variant": tile},
-            "rates": rates, "accuracy": acc, "cpu_baseline": _cpu_config_rate(conds)}
+    return {"metric": METRIC, "value": rates["fp32_plain" if ref_mode else "fp32_fused"], "unit": METRIC,
+            "dtype": "f32",
+            "config": {"workload": name, "lattice": lattice.name, "instances": len(insts), "vertices": verts,
+                       "dt": insts[0].dt, "variant": tile,
+                       "mode": "ref-mode (12 values per block, block scale a/sqrt(8))" if ref_mode
+                       else "config-mode (2 values per cell)"},
+            "rates": rates, "accuracy": acc, "cpu_baseline": _cpu_config_rate(conds, lattice=lattice)}
 
 
-def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1):
-    from vaikkari_gb300.gpe import Kernel, Mode, Precision
+def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1, lattice=None):
+    """BCC2: FP64 fused to the criterion, FP32 fused over the same steps.  TETRA12
+    (ref-mode): the plain kernel, both precisions over a fixed `max_steps`."""
+    from vaikkari_gb300.gpe import Kernel, Lattice, Mode, Precision
+    lattice = Lattice.BCC2 if lattice is None else Lattice(lattice)
+    ref_mode = lattice == Lattice.TETRA12
     insts = [c.inst for c in conds]
-    verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
+    verts = sum(i.nx * i.ny * i.nz for i in insts) * (12 if ref_mode else 2)
+    kern = Kernel.PLAIN if ref_mode else Kernel.FUSED
     zchunk = 0
-    if tile < 0:
+    if ref_mode:
+        tile, tol = 0, 0.0
+    elif tile < 0:
         from vaikkari_gb300.autotune import autotune
         best = autotune(insts, mode=Mode.IMAGINARY, zchunks=(0, 16, 32, 64))
         tile, zchunk = best["tile"], best["zchunk"]
     res = {}
     steps64 = None
     for prec in (Precision.FP64, Precision.FP32):
-        st = _stepper(conds, prec, Kernel.FUSED, Mode.IMAGINARY, tile=tile, zchunk=zchunk)
+        st = _stepper(conds, prec, kern, Mode.IMAGINARY, tile=tile, zchunk=zchunk, lattice=lattice)
         for i, c in enumerate(conds):
             st.upload(i, c.psi)
         t0 = time.perf_counter()
@@ -691,27 +715,28 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1):
            "rel_mu_fp32_vs_fp64": max(abs(a - b) / abs(b) for a, b in zip(r32["mu_obs"], r64["mu_obs"])),
            "rel_energy_fp32_vs_fp64": max(abs(a - b) / abs(b) for a, b in zip(r32["energy"], r64["energy"])),
            "rel_l2_fp32_vs_fp64": _rel_l2_phase(r32["fields"], r64["fields"])}
-    # throughput of the fused imaginary-time step (FP32), device time
-    st = _stepper(conds, Precision.FP32, Kernel.FUSED, Mode.IMAGINARY, tile=tile, zchunk=zchunk)
+    # throughput of the imaginary-time step (FP32), device time
+    st = _stepper(conds, Precision.FP32, kern, Mode.IMAGINARY, tile=tile, zchunk=zchunk, lattice=lattice)
     for i, c in enumerate(conds):
         st.upload(i, c.psi)
     st.time_steps(100)
     ms = min(st.time_steps(1000) for _ in range(2))
     st.close()
     return {"metric": METRIC, "value": verts * 1000 / (ms * 1e-3), "unit": METRIC, "dtype": "f32",
-            "config": {"workload": name, "instances": len(insts), "vertices": verts, "dt": insts[0].dt,
-                       "tol": tol, "mode": "imaginary", "variant": tile, "zchunk": zchunk},
-            "accuracy": acc, "cpu_baseline": _cpu_imag_rate(conds)}
+            "config": {"workload": name, "lattice": lattice.name, "instances": len(insts), "vertices": verts,
+                       "dt": insts[0].dt, "tol": tol, "max_steps": max_steps, "mode": "imaginary", "variant": tile,
+                       "zchunk": zchunk, "kernel": kern.name.lower()},
+            "accuracy": acc, "cpu_baseline": _cpu_imag_rate(conds, lattice=lattice)}
 
 
-def _cpu_imag_rate(conds, budget_s=5.0):
+def _cpu_imag_rate(conds, budget_s=5.0, lattice=None):
     """FP64 oracle imaginary-time steps (observables, then the normalised Euler
     step, all host threads for the step) of every condensate for about
     `budget_s` seconds."""
     import oracle.oracle as orc
     from vaikkari_gb300.gpe import Lattice, lattice_info, value_positions
     from vaikkari_gb300.workloads import harmonic
-    info = lattice_info(Lattice.BCC2)
+    info = lattice_info(Lattice.BCC2 if lattice is None else lattice)
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
     jobs = []
@@ -722,7 +747,7 @@ def _cpu_imag_rate(conds, budget_s=5.0):
         vdt = np.ascontiguousarray(harmonic(value_positions(inst, info), inst.trap) * inst.dt)
         psi = np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1), dtype=np.float64)
         jobs.append((g, psi, vdt, info["cell_volume"] * inst.block_scale ** 3))
-    verts = sum(c.inst.nx * c.inst.ny * c.inst.nz * 2 for c in conds)
+    verts = sum(c.inst.nx * c.inst.ny * c.inst.nz * info["slots"] for c in conds)
     steps, t0 = 0, time.perf_counter()
     while True:
         for g, psi, vdt, vol in jobs:
@@ -890,16 +915,27 @@ def run_workload(args):
         return run_tetra12(args)
     if name == "production":
         return run_production(args)
+    from vaikkari_gb300.gpe import Lattice
+    lat = Lattice.TETRA12 if args.lattice == "tetra12" else Lattice.BCC2
+    tag = lat.name.lower()
     if name == "config1":
-        line = run_config_realtime("config1_bcc2_32_realtime_1000", [workloads.config1()], [1000], tile=args.tile)
+        line = run_config_realtime(f"config1_{tag}_32_realtime_1000", [workloads.config1(lat)], [1000],
+                                   tile=args.tile, lattice=lat)
     elif name == "config2":
-        line = run_config_imaginary("config2_bcc2_128_imaginary", [workloads.config2()], tile=args.tile)
+        if lat == Lattice.TETRA12:
+            line = run_config_imaginary(f"config2_{tag}_128_imaginary_2000_steps", [workloads.config2(lat)],
+                                        max_steps=2000, lattice=lat)
+        else:
+            line = run_config_imaginary(f"config2_{tag}_128_imaginary", [workloads.config2(lat)], tile=args.tile)
     elif name == "config3":
-        line = run_config_realtime("config3_bcc2_192_vortex_ring", [workloads.config3()], [1000, 5000, 10000],
-                                   tile=args.tile)
+        line = run_config_realtime(f"config3_{tag}_192_vortex_ring", [workloads.config3(lat)], [1000, 5000, 10000],
+                                   tile=args.tile, lattice=lat)
+    elif name == "config4":
+        line = run_config_realtime(f"config4_{tag}_batch64_realtime_1000", workloads.config4(lat), [1000],
+                                   tile=args.tile, lattice=lat)
     elif name == "config5":
-        line = run_config_realtime("config5_bcc2_512_realtime", [workloads.config5()], [200, 2000], fp64_steps=200,
-                                   tile=args.tile)
+        line = run_config_realtime(f"config5_{tag}_512_realtime", [workloads.config5(lat)], [200, 2000],
+                                   fp64_steps=200, tile=args.tile, lattice=lat)
     else:
         raise SystemExit(f"unknown workload {name}")
     line["n_gpus"] = 1
@@ -927,6 +963,9 @@ def main():
                     help="batch64 (the headline), config1/config2/config3/config5 (accuracy cases), relax "
                          "(the vortex relaxation), production (main() at production size) or tetra12 (the "
                          "drop-in's FP64/FP32 kernel on the production grid)")
+    ap.add_argument("--lattice", default="bcc2", choices=["bcc2", "tetra12"],
+                    help="config1-5: config-mode (bcc2, 2 values per cell) or ref-mode (tetra12, the reference's "
+                         "12 values per block)")
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
                     help="multi-GPU split: weak = 64 condensates per rank, strong = the 64 split over ranks")
     ap.add_argument("--production-iters", type=int, default=2)
