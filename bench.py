@@ -900,8 +900,9 @@ def run_tetra12(args):
             "config": {"workload": "tetra12_plain_production_grid", "values": vals, "blocks": [87, 87, 302],
                        "lattice": "TETRA12", "kernel": "plain", "potential": "array"},
             "fp32": rates["fp32"],
-            "note": "FP64 performs the reference kernel's rounded operations (16 FP64 operations per value "
-                    "and half-step); its bound is this GPU's FP64 rate"}
+            "note": "FP64 performs the reference kernel's rounded operations and equals its results bit for "
+                    "bit; the per-value constant L0 + V*dt is added once per potential upload, leaving 15 FP64 "
+                    "operations per value and half-step; the bound is this GPU's FP64 rate"}
     print(json.dumps(line), flush=True)
     return 0
 

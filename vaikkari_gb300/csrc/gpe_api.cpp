@@ -71,6 +71,7 @@ struct gpe_handle_ {
     void *buf[4] = {nullptr, nullptr, nullptr, nullptr};
     bool two_step = false;
     void *vpot = nullptr;
+    void *vbase = nullptr;  // array potential: L0 + V*dt per value for the plain kernel
     bool fused = false;
     int tile = 0, tx = 32, ty = 8, zchunk = 0, zcmax = 1;
     std::vector<WorkItem> items;
@@ -262,6 +263,7 @@ gpe_status enqueue_step_real(gpe_handle h)
                 l.prev = prev;
                 l.next = next;
                 l.vpot = h->vpot;
+                l.vbase = h->vbase;
                 GPE_CUDA_TRY(launch_plain_step(l, h->stream));
                 h->launches++;
             }
@@ -346,6 +348,7 @@ gpe_status enqueue_step_imag(gpe_handle h, int parity)
         l.prev = prev;
         l.next = next;
         l.vpot = h->vpot;
+        l.vbase = h->vbase;
         l.imag = h->imag;
         GPE_CUDA_TRY(launch_plain_step(l, h->stream));
         h->launches += 2;
@@ -448,6 +451,7 @@ void free_handle(gpe_handle h)
     for (void *b : h->buf) cudaFree(b);
     for (void *b : h->lo) cudaFree(b);
     cudaFree(h->vpot);
+    cudaFree(h->vbase);
     cudaFree(h->items_dev);
     cudaFree(h->item_begin_dev);
     cudaFree(h->imag);
@@ -661,6 +665,10 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
         }
     GPE_CREATE_TRY(cudaMalloc(&h->vpot, h->esize * std::max<size_t>(h->v_elems, 1)));
     GPE_CREATE_TRY(cudaMemsetAsync(h->vpot, 0, h->esize * std::max<size_t>(h->v_elems, 1), h->stream));
+    if (cfg->potential == GPE_POTENTIAL_ARRAY) {
+        GPE_CREATE_TRY(cudaMalloc(&h->vbase, h->esize * std::max<size_t>(h->v_elems, 1)));
+        GPE_CREATE_TRY(cudaMemsetAsync(h->vbase, 0, h->esize * std::max<size_t>(h->v_elems, 1), h->stream));
+    }
     std::vector<std::vector<float>> traps32(cfg->num_instances);
     if (cfg->potential == GPE_POTENTIAL_TRAP) {
         for (int i = 0; i < cfg->num_instances; i++) {
@@ -858,7 +866,9 @@ gpe_status gpe_upload(gpe_handle h, int32_t instance, const void *even, const vo
         if (st != GPE_OK) return st;
         GPE_CUDA_TRY(launch_pack(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->staging, h->vpot, 0, in.dt,
                                  h->stream));
-        h->launches++;
+        GPE_CUDA_TRY(launch_potential_base(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->vpot, h->vbase,
+                                           h->stream));
+        h->launches += 2;
     }
     GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->imag_ready = false;

@@ -101,12 +101,14 @@ __device__ __forceinline__ typename Cplx<T>::type c_scale(T s, typename Cplx<T>:
 //     c   = fma(gdt, nrm, L0 + Vdt)
 //     one class:  h = fma(L[0], S[0], c*p)
 //     two classes: a = L[0]*S[0], a = fma(L[1], S[1], a), h = fma(c, p, a)
-template <typename T, int NC>
+// With BASE, `vdt` already holds L0 + Vdt (rounded the same way, once per
+// potential upload) and L0 is not used: one FP64 operation fewer per value.
+template <typename T, int NC, bool BASE = false>
 __device__ __forceinline__ void hpsi(typename Cplx<T>::type p, const typename Cplx<T>::type *S, const T *L, T L0,
                                      T vdt, T gdt, T &hx, T &hy, T &nrm)
 {
     nrm = d_fma(p.x, p.x, d_mul(p.y, p.y));
-    const T c = d_fma(gdt, nrm, d_add(L0, vdt));
+    const T c = BASE ? d_fma(gdt, nrm, vdt) : d_fma(gdt, nrm, d_add(L0, vdt));
     if (NC == 1) {
         // One class (TETRA12): h = fma(L, S, c*p), the product c*p rounded first.
         // This is the rounding of the reference's update as compiled for the GPU:

@@ -47,9 +47,13 @@ struct StepLaunch {
     int nx, ny, nz, slots;
     void *prev, *next;    // field arenas (T2*)
     const void *vpot;     // potential arena (T*) or trap tables
+    const void *vbase;    // array potential: L0 + V*dt per value (T*), same index as vpot
     const ImagScalars *imag;  // imaginary time: per-instance scale of prev (device), may be null
 };
 cudaError_t launch_plain_step(const StepLaunch &l, cudaStream_t s);
+// Array potential: vbase = L0 + V*dt (in the handle's precision) for one instance.
+cudaError_t launch_potential_base(int precision, const InstDev *inst, int ii, int nx, int ny, int nz, int slots,
+                                  const void *vpot, void *vbase, cudaStream_t s);
 
 struct FusedLaunch {
     int precision, mode, potential, tile;

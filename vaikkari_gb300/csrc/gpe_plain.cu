@@ -45,6 +45,7 @@ cudaError_t set_plain_table(const gpe_lattice_info &info)
     return cudaMemcpyToSymbol(c_tab_bcc2, packed, sizeof(int) * 2 * 14);
 }
 
+// vpot: the trap tables (POT == TRAP), or L0 + V*dt per value (POT == ARRAY).
 template <typename T, int LAT, int MODE, int POT>
 __global__ void __launch_bounds__(256) plain_step_kernel(const InstDev *__restrict__ insts, int ii,
                                                          const typename Cplx<T>::type *__restrict__ prev,
@@ -82,7 +83,7 @@ __global__ void __launch_bounds__(256) plain_step_kernel(const InstDev *__restri
     Lw[0] = T(d.Lc[0]);
     if (L::NC > 1) Lw[L::NC - 1] = T(d.Lc[1]);
     T hx, hy, nrm;
-    hpsi<T, L::NC>(p, S, Lw, T(d.L0), vdt, T(d.gdt), hx, hy, nrm);
+    hpsi<T, L::NC, POT == GPE_POTENTIAL_ARRAY>(p, S, Lw, T(d.L0), vdt, T(d.gdt), hx, hy, nrm);
     T2 n;
     if (MODE == 0) n = next[self];
     next[self] = integrate<T, MODE>(n, p, hx, hy);
@@ -96,7 +97,7 @@ static cudaError_t plain_dispatch_mode(const StepLaunch &l, cudaStream_t st)
     dim3 grid((l.nx + 31) / 32, (l.ny + 7) / 8, l.nz * Lat<LAT>::NS);
     const T2 *prev = (const T2 *)l.prev;
     T2 *next = (T2 *)l.next;
-    const T *v = (const T *)l.vpot;
+    const T *v = (const T *)(l.potential == GPE_POTENTIAL_ARRAY ? l.vbase : l.vpot);
     if (l.mode == GPE_REAL_TIME) {
         if (l.potential == GPE_POTENTIAL_ARRAY)
             plain_step_kernel<T, LAT, 0, 0><<<grid, block, 0, st>>>(l.inst, l.inst_index, prev, next, v, l.imag);
@@ -108,6 +109,40 @@ static cudaError_t plain_dispatch_mode(const StepLaunch &l, cudaStream_t st)
         else
             plain_step_kernel<T, LAT, 1, 1><<<grid, block, 0, st>>>(l.inst, l.inst_index, prev, next, v, l.imag);
     }
+    return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void potential_base_kernel(const InstDev *__restrict__ insts, int ii, const T *__restrict__ vpot,
+                                      T *__restrict__ vbase)
+{
+    const InstDev &d = insts[ii];
+    const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
+    const T L0 = T(d.L0);
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
+         v += (long long)gridDim.x * blockDim.x) {
+        long long r = v;
+        const int x = int(r % d.nx);
+        r /= d.nx;
+        const int y = int(r % d.ny);
+        r /= d.ny;
+        const int s = int(r % d.slots);
+        const int z = int(r / d.slots);
+        const long long o = field_index(d, s, x, y, z) - d.base + d.vbase;
+        vbase[o] = d_add(L0, vpot[o]);  // the add hpsi would do every half-step
+    }
+}
+
+cudaError_t launch_potential_base(int precision, const InstDev *inst, int ii, int nx, int ny, int nz, int slots,
+                                  const void *vpot, void *vbase, cudaStream_t s)
+{
+    long long g = ((long long)nx * ny * nz * slots + 255) / 256;
+    if (g > 152 * 32) g = 152 * 32;
+    if (g < 1) g = 1;
+    if (precision == GPE_FP64)
+        potential_base_kernel<double><<<int(g), 256, 0, s>>>(inst, ii, (const double *)vpot, (double *)vbase);
+    else
+        potential_base_kernel<float><<<int(g), 256, 0, s>>>(inst, ii, (const float *)vpot, (float *)vbase);
     return cudaGetLastError();
 }
 
