@@ -907,9 +907,56 @@ def run_tetra12(args):
     return 0
 
 
+def run_batch_imaginary(args):
+    """The 64-condensate batch in imaginary time: all condensates advance in one
+    fused launch per step, each renormalised every step.  FP32 and FP64 run
+    --imag-steps steps from the same random-phase start (seed 4); the line
+    reports the FP32 rate (autotuned, device time of 300 steps) and mu / energy
+    of FP32 against FP64 per condensate."""
+    from vaikkari_gb300 import workloads
+    from vaikkari_gb300.autotune import autotune
+    from vaikkari_gb300.gpe import Kernel, Lattice, Mode, Potential, Precision, Stepper
+    conds = workloads.config4()
+    insts = [c.inst for c in conds]
+    verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
+    rng = np.random.default_rng(4)
+    psis = [np.exp(1j * rng.uniform(0, 2 * np.pi, size=(i.nz, i.ny, i.nx, 2))) for i in insts]
+    t = autotune(insts, precision=Precision.FP32, potential=Potential.TRAP, mode=Mode.IMAGINARY,
+                 zchunks=(0, 16, 32, 64))
+    tile, zchunk = t["tile"], t["zchunk"]
+    res = {}
+    for prec in (Precision.FP64, Precision.FP32):
+        st = Stepper(insts, lattice=Lattice.BCC2, precision=prec, kernel=Kernel.FUSED, mode=Mode.IMAGINARY,
+                     potential=Potential.TRAP, graph_steps=100, tile=tile, zchunk=zchunk)
+        for i, p in enumerate(psis):
+            st.upload(i, p)
+        steps, conv, mu = st.imaginary_time(args.imag_steps, 0.0)
+        obs = st.observables(0)
+        if prec == Precision.FP32:
+            st.time_steps(100)
+            ms = min(st.time_steps(300) for _ in range(2))
+            res["rate"] = verts * 300 / (ms * 1e-3)
+            res["ms_per_step"] = ms / 300
+        st.close()
+        res[prec] = (mu, [o["energy"] for o in obs])
+    mu64, e64 = res[Precision.FP64]
+    mu32, e32 = res[Precision.FP32]
+    line = {"metric": METRIC, "value": res["rate"], "unit": METRIC, "n_gpus": 1, "dtype": "f32",
+            "data": "synthetic", "ms_per_step": res["ms_per_step"],
+            "config": {"workload": "batch64_bcc2_imaginary", "instances": len(insts), "vertices": verts,
+                       "steps": args.imag_steps, "variant": tile, "zchunk": zchunk, "kernel": "fused"},
+            "accuracy": {"max_rel_mu_fp32_vs_fp64": max(abs(a - b) / abs(b) for a, b in zip(mu32, mu64)),
+                         "max_rel_energy_fp32_vs_fp64": max(abs(a - b) / abs(b) for a, b in zip(e32, e64)),
+                         "mu_fp64_range": [min(mu64), max(mu64)]}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_workload(args):
     from vaikkari_gb300 import workloads
     name = args.workload
+    if name == "batch64_imag":
+        return run_batch_imaginary(args)
     if name == "relax":
         return run_relax(args)
     if name == "tetra12":
@@ -962,13 +1009,15 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--workload", default="batch64",
                     help="batch64 (the headline), config1/config2/config3/config5 (accuracy cases), relax "
-                         "(the vortex relaxation), production (main() at production size) or tetra12 (the "
-                         "drop-in's FP64/FP32 kernel on the production grid)")
+                         "(the vortex relaxation), production (main() at production size), tetra12 (the "
+                         "drop-in's FP64/FP32 kernel on the production grid) or batch64_imag (the batch in "
+                         "imaginary time)")
     ap.add_argument("--lattice", default="bcc2", choices=["bcc2", "tetra12"],
                     help="config1-5: config-mode (bcc2, 2 values per cell) or ref-mode (tetra12, the reference's "
                          "12 values per block)")
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
                     help="multi-GPU split: weak = 64 condensates per rank, strong = the 64 split over ranks")
+    ap.add_argument("--imag-steps", type=int, default=2000, help="batch64_imag: imaginary-time steps")
     ap.add_argument("--production-iters", type=int, default=2)
     ap.add_argument("--relax-batch", type=int, default=19)
     ap.add_argument("--relax-batch-iters", type=int, default=2000)
