@@ -97,3 +97,28 @@ def test_shard_by_size_balance():
         loads = [sum(insts[i].nx ** 3 for i in p) for p in parts]
         if world <= len(insts):
             assert max(loads) - min(loads) <= 96 ** 3
+
+
+def _tune_writer(rank, path, n):
+    import json
+    os.environ["GPE_AUTOTUNE_CACHE"] = path
+    import importlib
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import vaikkari_gb300.autotune as at
+    importlib.reload(at)
+    for k in range(n):
+        db = at._load()
+        db[f"rank{rank}-{k}"] = {"tile": k}
+        at._store(db)
+    json.load(open(path))  # the file is always complete
+
+
+def test_autotune_cache_survives_concurrent_writers(tmp_path):
+    """Ranks of one job store autotune results at the same time: every write
+    leaves a complete file (no shared temporary file)."""
+    import json
+    path = str(tmp_path / "cache.json")
+    mp.start_processes(_tune_writer, args=(path, 20), nprocs=4, join=True, start_method="spawn")
+    db = json.load(open(path))
+    assert len(db) >= 20 and all(k.startswith("rank") for k in db)

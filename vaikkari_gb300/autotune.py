@@ -53,8 +53,11 @@ def _load():
 
 
 def _store(db):
+    """Writes the cache atomically; ranks of one job may store at the same time,
+    so each writes its own temporary file and the last replace wins (entries a
+    concurrent writer added in between are re-measured on a later run)."""
     os.makedirs(os.path.dirname(CACHE), exist_ok=True)
-    tmp = CACHE + ".tmp"
+    tmp = f"{CACHE}.{os.getpid()}.tmp"
     with open(tmp, "w") as f:
         json.dump(db, f, indent=1)
     os.replace(tmp, CACHE)
@@ -117,6 +120,7 @@ def autotune(instances: List[Instance], fields=None, lattice=Lattice.BCC2, preci
     entry = {"tile": best["tile"], "zchunk": best["zchunk"], "vups": best["vups"], "device": name,
              "candidates": results}
     if cache:
+        db = _load()  # entries other processes stored meanwhile
         db[sig] = entry
         _store(db)
     return entry
