@@ -13,9 +13,9 @@ from vaikkari_gb300.gpe import GpeError, Instance, Kernel, Lattice, Potential, P
 pytestmark = pytest.mark.gpu
 
 
-def _stepper(kernel=Kernel.FUSED, tile=0):
+def _stepper(kernel=Kernel.FUSED, tile=0, precision=Precision.FP32):
     inst = Instance(8, 8, 8, 0.4, 1e-3, 50.0, origin=(-1.6, -1.6, -1.6))
-    return Stepper([inst], lattice=Lattice.BCC2, precision=Precision.FP32, kernel=kernel, potential=Potential.TRAP,
+    return Stepper([inst], lattice=Lattice.BCC2, precision=precision, kernel=kernel, potential=Potential.TRAP,
                    graph_steps=-1, tile=tile)
 
 
@@ -50,6 +50,32 @@ def test_bounded_wait_timeout_is_reported_and_context_survives(which):
     st.close()
     np.testing.assert_array_equal(ge, we)
     np.testing.assert_array_equal(go, wo)
+
+
+def test_bounded_wait_timeout_with_compensated_storage():
+    """The compensated kernel's stages also carry the residual tile; a withheld
+    copy still ends in GPE_ERR_TIMEOUT, and a clean run afterwards equals the
+    oracle bit for bit."""
+    import oracle.oracle as orc
+    st = _stepper(precision=Precision.FP32C)
+    shp = st.shape(0)
+    e, o = random_state(shp, 1, 0.3), random_state(shp, 2, 0.3)
+    st.upload(0, e, o)
+    st.debug_inject(3)
+    st.step(1)
+    with pytest.raises(GpeError) as err:
+        st.synchronize()
+    assert err.value.status == Status.TIMEOUT
+    st.debug_inject(-1)
+    st.upload(0, e, o)
+    st.step(3)
+    ge, go = st.download(0)
+    eh, el = orc.split_comp(interleave(e, np.float64))
+    oh, ol = orc.split_comp(interleave(o, np.float64))
+    grid_for(st, 0).leapfrog_bcc2_comp(eh, oh, el, ol, vdt_for(st, 0), 3)
+    st.close()
+    np.testing.assert_array_equal(ge, orc.join_comp(eh, el))
+    np.testing.assert_array_equal(go, orc.join_comp(oh, ol))
 
 
 def test_nan_in_field_trips_the_watchdog():
