@@ -203,6 +203,40 @@ def test_imaginary_time_batch_equals_single_runs(prec):
         assert mu[i] == mu1[0]
 
 
+def test_imaginary_time_many_instances_equal_single_runs():
+    """40 small condensates (more than the CTA's warps, so the fold takes the
+    instances in several rounds): each equals its own single run bit for bit."""
+    rng = np.random.default_rng(12)
+    insts, psis = [], []
+    for k in range(40):
+        nx, ny, nz = (int(v) for v in rng.integers(1, 7, size=3))
+        insts.append(Instance(nx, ny, nz, 0.4 + 0.01 * k, 1e-3, 5.0 + k, origin=(-0.2 * nx, -0.2 * ny, -0.2 * nz)))
+        psis.append(np.exp(1j * rng.uniform(0, 2 * np.pi, size=(nz, ny, nx, 2))))
+    kw = dict(lattice=Lattice.BCC2, precision=Precision.FP64, mode=Mode.IMAGINARY, kernel=Kernel.FUSED,
+              potential=Potential.TRAP, graph_steps=10, tile=0, zchunk=2)
+    st = Stepper(insts, **kw)
+    for i, p in enumerate(psis):
+        st.upload(i, p)
+    steps, conv, mu = st.imaginary_time(25, 0.0)
+    batch = [st.download(i, odd=False)[0] for i in range(len(insts))]
+    st.close()
+    for i in range(0, len(insts), 3):
+        one = Stepper([insts[i]], **kw)
+        one.upload(0, psis[i])
+        _, _, mu1 = one.imaginary_time(steps, 0.0)
+        got = one.download(0, odd=False)[0]
+        one.close()
+        np.testing.assert_array_equal(batch[i], got, err_msg=f"instance {i}")
+        assert mu[i] == mu1[0]
+
+
+def test_fused_batch_of_300_tiny_instances_bit_exact():
+    """One fused launch over 300 instances of 1..4 blocks per side."""
+    rng = np.random.default_rng(13)
+    dims = [tuple(int(v) for v in rng.integers(1, 5, size=3)) for _ in range(300)]
+    _run_real(Lattice.BCC2, Precision.FP32, Kernel.FUSED, Potential.TRAP, dims, steps=3, seed=4)
+
+
 @pytest.mark.parametrize("kernel", [Kernel.PLAIN, Kernel.FUSED])
 def test_imaginary_time_converges_to_harmonic_ground_state(kernel):
     """g = 0, isotropic trap: mu -> 3/2 up to the O(a^2) discretisation error."""
