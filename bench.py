@@ -361,7 +361,8 @@ def run_ours(args):
     traffic = _profile_traffic("fused_bcc2_fp32c_batch64.md" if comp_main else "fused_bcc2_batch64.md")
 
     # End to end through the public API with pinned host buffers: upload every
-    # instance, run the steps, read the observables, download every field.
+    # instance (one batched call), run the steps, read the observables, download
+    # every field (one batched call).
     pinned_e, pinned_o = [], []
     for e, o in zip(evens, odds):
         tt = torch.float64 if comp_main else torch.float32
@@ -374,12 +375,10 @@ def run_ours(args):
     h2d = sum(a.nbytes for a in pinned_e) + sum(a.nbytes for a in pinned_o)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for i in range(len(insts)):
-        st.upload(i, pinned_e[i], pinned_o[i], None)
+    st.upload_many([(i, pinned_e[i], pinned_o[i], None) for i in range(len(insts))])
     st.step(args.steps)
     obs = st.observables(0)
-    for i in range(len(insts)):
-        st.lib.gpe_download(st.h, i, pinned_e[i].ctypes.data, pinned_o[i].ctypes.data)
+    st.download_many(range(len(insts)), outs=list(zip(pinned_e, pinned_o)))
     st.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_s = _max_over_ranks(dist, e2e_s, device=torch.device("cuda", local))

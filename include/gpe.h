@@ -175,6 +175,19 @@ gpe_status gpe_upload(gpe_handle h, int32_t instance, const void *even, const vo
 /* Copies one instance's fields back (either pointer may be NULL). */
 gpe_status gpe_download(gpe_handle h, int32_t instance, void *even, void *odd);
 
+/* The same for `count` instances in one call: every copy and layout conversion
+ * is queued on the handle's stream, with one wait at the end instead of one per
+ * field (each transfer has its own device staging slot; with pinned host memory
+ * the copies run at the link's bandwidth).  instances[k] names the instance of
+ * entry k; even/odd/potential hold one pointer per entry (odd may be NULL in
+ * imaginary time, potential may be NULL for the trap form; in gpe_download_many
+ * either array, or any entry, may be NULL).  No counterpart in the reference,
+ * which has one condensate. */
+gpe_status gpe_upload_many(gpe_handle h, int32_t count, const int32_t *instances, const void *const *even,
+                           const void *const *odd, const void *const *potential);
+gpe_status gpe_download_many(gpe_handle h, int32_t count, const int32_t *instances, void *const *even,
+                             void *const *odd);
+
 /* Real time: advances every instance by `steps` leapfrog steps (odd <- even,
  * then even <- odd; GPUGrossPitaevskii_BCC.cu:475-481).  Imaginary time:
  * `steps` normalised Euler steps.  Asynchronous on the handle's stream. */

@@ -89,6 +89,10 @@ struct gpe_handle_ {
     int obs_max_ctas = 2048;
     void *staging = nullptr;
     size_t staging_bytes = 0;
+    void *batch_staging = nullptr;  // gpe_upload_many / gpe_download_many: one slot per transfer
+    size_t batch_bytes = 0;
+    cudaStream_t copy_stream = nullptr;     // their host<->device copies, beside the conversions
+    std::vector<cudaEvent_t> xfer_events;   // one per transfer slot
     cudaStream_t stream = nullptr;
     std::map<GraphKey, cudaGraphExec_t> graphs;
     int parity = 0;      // imaginary time: which buffer holds psi; two-step: which set holds the fields
@@ -463,6 +467,9 @@ void free_handle(gpe_handle h)
     cudaFree(h->lo_maps);
     cudaFree(h->err);
     cudaFree(h->staging);
+    cudaFree(h->batch_staging);
+    for (cudaEvent_t e : h->xfer_events) cudaEventDestroy(e);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -898,6 +905,159 @@ gpe_status gpe_download(gpe_handle h, int32_t instance, void *even, void *odd)
         GPE_CUDA_TRY(cudaMemcpyAsync(dsts[f], h->staging, vals * 2 * h->hsize, cudaMemcpyDeviceToHost, h->stream));
         GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
     }
+    return GPE_OK;
+}
+
+namespace {
+
+// Device buffer of at least `bytes` for the batched transfers, grown on demand.
+gpe_status ensure_batch_staging(gpe_handle h, size_t bytes)
+{
+    if (h->batch_bytes >= bytes) return GPE_OK;
+    GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    cudaFree(h->batch_staging);
+    h->batch_staging = nullptr;
+    h->batch_bytes = 0;
+    GPE_CUDA_TRY(cudaMalloc(&h->batch_staging, bytes));
+    h->batch_bytes = bytes;
+    return GPE_OK;
+}
+
+size_t slot_bytes(size_t b) { return round_up(b, 256); }
+
+// The copy stream and at least n events for one batched transfer.
+gpe_status ensure_xfer(gpe_handle h, size_t n)
+{
+    if (!h->copy_stream) GPE_CUDA_TRY(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    while (h->xfer_events.size() < n) {
+        cudaEvent_t e;
+        GPE_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        h->xfer_events.push_back(e);
+    }
+    return GPE_OK;
+}
+
+}  // namespace
+
+gpe_status gpe_upload_many(gpe_handle h, int32_t count, const int32_t *instances, const void *const *even,
+                           const void *const *odd, const void *const *potential)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (count < 0 || (count > 0 && (!instances || !even)))
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_upload_many: bad count or null array");
+    const bool arr = h->cfg.potential == GPE_POTENTIAL_ARRAY;
+    size_t total = 0;
+    for (int k = 0; k < count; k++) {
+        const int i = instances[k];
+        if (i < 0 || i >= h->cfg.num_instances) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_upload_many: bad instance");
+        if (!even[k]) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_upload_many: even field is required");
+        if (h->cfg.mode == GPE_REAL_TIME && (!odd || !odd[k]))
+            return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_upload_many: odd field is required in real time");
+        if (arr && (!potential || !potential[k]))
+            return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_upload_many: potential array is required");
+        const gpe_instance &in = h->inst[i];
+        const size_t vals = size_t(in.nx) * in.ny * in.nz * h->ns;
+        total += 2 * slot_bytes(vals * 2 * h->hsize) + (arr ? slot_bytes(vals * h->esize) : 0);
+    }
+    st = ensure_batch_staging(h, std::max<size_t>(total, 256));
+    if (st == GPE_OK) st = ensure_xfer(h, size_t(3) * count + 1);
+    if (st != GPE_OK) return st;
+    char *stage = (char *)h->batch_staging;
+    const int prec = h->cfg.precision;
+    // Copies go on the copy stream back to back; each conversion waits for its
+    // own copy on the handle's stream, so conversions overlap later copies.
+    // The copy stream first waits for the handle's stream (earlier work).
+    size_t ev = 0;
+    GPE_CUDA_TRY(cudaEventRecord(h->xfer_events[ev], h->stream));
+    GPE_CUDA_TRY(cudaStreamWaitEvent(h->copy_stream, h->xfer_events[ev++], 0));
+    auto copy_in = [&](void *dst, const void *src, size_t b) -> gpe_status {
+        GPE_CUDA_TRY(cudaMemcpyAsync(dst, src, b, cudaMemcpyHostToDevice, h->copy_stream));
+        GPE_CUDA_TRY(cudaEventRecord(h->xfer_events[ev], h->copy_stream));
+        GPE_CUDA_TRY(cudaStreamWaitEvent(h->stream, h->xfer_events[ev++], 0));
+        return GPE_OK;
+    };
+    for (int k = 0; k < count; k++) {
+        const int i = instances[k];
+        const gpe_instance &in = h->inst[i];
+        const size_t vals = size_t(in.nx) * in.ny * in.nz * h->ns;
+        const void *srcs[2] = {even[k], odd ? odd[k] : nullptr};
+        for (int f = 0; f < 2; f++) {
+            if (!srcs[f]) continue;
+            const size_t b = vals * 2 * h->hsize;
+            if ((st = copy_in(stage, srcs[f], b)) != GPE_OK) return st;
+            if (h->comp)
+                GPE_CUDA_TRY(launch_pack_split(h->idev, i, in.nx, in.ny, in.nz, h->ns, stage, field_buf(h, f), h->lo[f],
+                                               h->stream));
+            else
+                GPE_CUDA_TRY(launch_pack(prec, h->idev, i, in.nx, in.ny, in.nz, h->ns, stage, field_buf(h, f), 1, 1.0,
+                                         h->stream));
+            h->launches++;
+            stage += slot_bytes(b);
+        }
+        if (arr) {
+            const size_t b = vals * h->esize;
+            if ((st = copy_in(stage, potential[k], b)) != GPE_OK) return st;
+            GPE_CUDA_TRY(launch_pack(prec, h->idev, i, in.nx, in.ny, in.nz, h->ns, stage, h->vpot, 0, in.dt, h->stream));
+            GPE_CUDA_TRY(launch_potential_base(prec, h->idev, i, in.nx, in.ny, in.nz, h->ns, h->vpot, h->vbase,
+                                               h->stream));
+            h->launches += 2;
+            stage += slot_bytes(b);
+        }
+    }
+    GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->imag_ready = false;
+    return GPE_OK;
+}
+
+gpe_status gpe_download_many(gpe_handle h, int32_t count, const int32_t *instances, void *const *even,
+                             void *const *odd)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (count < 0 || (count > 0 && !instances))
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_download_many: bad count or null array");
+    size_t total = 0;
+    for (int k = 0; k < count; k++) {
+        const int i = instances[k];
+        if (i < 0 || i >= h->cfg.num_instances)
+            return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_download_many: bad instance");
+        const gpe_instance &in = h->inst[i];
+        const size_t vals = size_t(in.nx) * in.ny * in.nz * h->ns;
+        total += 2 * slot_bytes(vals * 2 * h->hsize);
+    }
+    st = sync_and_check(h);
+    if (st != GPE_OK) return st;
+    st = ensure_batch_staging(h, std::max<size_t>(total, 256));
+    if (st == GPE_OK) st = ensure_xfer(h, size_t(2) * count);
+    if (st != GPE_OK) return st;
+    char *stage = (char *)h->batch_staging;
+    // Conversions on the handle's stream; each copy waits for its conversion on
+    // the copy stream, so copies overlap later conversions.
+    size_t ev = 0;
+    for (int k = 0; k < count; k++) {
+        const int i = instances[k];
+        const gpe_instance &in = h->inst[i];
+        const size_t vals = size_t(in.nx) * in.ny * in.nz * h->ns;
+        void *dsts[2] = {even ? even[k] : nullptr, odd ? odd[k] : nullptr};
+        for (int f = 0; f < 2; f++) {
+            if (!dsts[f]) continue;
+            const size_t b = vals * 2 * h->hsize;
+            if (h->comp)
+                GPE_CUDA_TRY(launch_unpack_join(h->idev, i, in.nx, in.ny, in.nz, h->ns, field_buf(h, f), h->lo[f], stage,
+                                                h->stream));
+            else
+                GPE_CUDA_TRY(launch_unpack(h->cfg.precision, h->idev, i, in.nx, in.ny, in.nz, h->ns, field_buf(h, f),
+                                           stage, nullptr, h->stream));
+            h->launches++;
+            GPE_CUDA_TRY(cudaEventRecord(h->xfer_events[ev], h->stream));
+            GPE_CUDA_TRY(cudaStreamWaitEvent(h->copy_stream, h->xfer_events[ev++], 0));
+            GPE_CUDA_TRY(cudaMemcpyAsync(dsts[f], stage, b, cudaMemcpyDeviceToHost, h->copy_stream));
+            stage += slot_bytes(b);
+        }
+    }
+    GPE_CUDA_TRY(cudaStreamSynchronize(h->copy_stream));
+    GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
     return GPE_OK;
 }
 

@@ -202,6 +202,7 @@ __global__ void __launch_bounds__(256) observables_kernel(const InstDev *__restr
     const long long total = (long long)d.nx * d.ny * d.nz * L::NS;
     Kahan k0, k1, k2, k3;
     const double wsum = L::N0 * d.w[0] + (L::NB - L::N0) * d.w[1];
+    const double rdt = 1.0 / d.dt;
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
          v += (long long)gridDim.x * blockDim.x) {
         long long r = v;
@@ -212,14 +213,42 @@ __global__ void __launch_bounds__(256) observables_kernel(const InstDev *__restr
         const int s = int(r % L::NS);
         const int z = int(r / L::NS);
         double sx[2] = {0.0, 0.0}, sy[2] = {0.0, 0.0};
+        if constexpr (sizeof(T) == 4) {
+            // FP32 values: each class sum kept as an unevaluated float pair
+            // (hi + lo, error-free two-sums, lo accumulated in FP32) and
+            // converted once, so the FP64 pipe (slow on this GPU) sees a few
+            // operations per value instead of a conversion and an add per
+            // neighbour.  Agrees with FP64 summation to about 1e-14.
+            float hx[2] = {0.f, 0.f}, lx_[2] = {0.f, 0.f}, hy[2] = {0.f, 0.f}, ly_[2] = {0.f, 0.f};
 #pragma unroll
-        for (int k = 0; k < L::NB; k++) {
-            const int e = L::entry(s * L::NB + k);
-            const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
-            const T2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
-            const int c = (k < L::N0) ? 0 : 1;
-            sx[c] += double(q.x);
-            sy[c] += double(q.y);
+            for (int k = 0; k < L::NB; k++) {
+                const int e = L::entry(s * L::NB + k);
+                const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
+                const T2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
+                const int c = (k < L::N0) ? 0 : 1;
+                float t = __fadd_rn(hx[c], q.x), bb = __fsub_rn(t, hx[c]);
+                lx_[c] = __fadd_rn(lx_[c], __fadd_rn(__fsub_rn(hx[c], __fsub_rn(t, bb)), __fsub_rn(q.x, bb)));
+                hx[c] = t;
+                t = __fadd_rn(hy[c], q.y);
+                bb = __fsub_rn(t, hy[c]);
+                ly_[c] = __fadd_rn(ly_[c], __fadd_rn(__fsub_rn(hy[c], __fsub_rn(t, bb)), __fsub_rn(q.y, bb)));
+                hy[c] = t;
+            }
+#pragma unroll
+            for (int c = 0; c < L::NC; c++) {
+                sx[c] = double(hx[c]) + double(lx_[c]);
+                sy[c] = double(hy[c]) + double(ly_[c]);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < L::NB; k++) {
+                const int e = L::entry(s * L::NB + k);
+                const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
+                const T2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
+                const int c = (k < L::N0) ? 0 : 1;
+                sx[c] += double(q.x);
+                sy[c] += double(q.y);
+            }
         }
         const long long self = field_index(d, s, x, y, z);
         const T2 pt = f[self];
@@ -232,7 +261,7 @@ __global__ void __launch_bounds__(256) observables_kernel(const InstDev *__restr
         const double n2 = px * px + py * py;
         k0.add(n2);
         k1.add(-0.5 * (px * lx + py * ly));
-        k2.add((vdt / d.dt) * n2);
+        k2.add((vdt * rdt) * n2);
         k3.add(0.5 * d.g * n2 * n2);
     }
     double acc[6] = {k0.s, k1.s, k2.s, k3.s, 0.0, 0.0};

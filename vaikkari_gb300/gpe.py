@@ -160,6 +160,11 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_upload.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.gpe_download.restype = st
     lib.gpe_download.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
+    vpp = C.POINTER(C.c_void_p)
+    lib.gpe_upload_many.restype = st
+    lib.gpe_upload_many.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), vpp, vpp, vpp]
+    lib.gpe_download_many.restype = st
+    lib.gpe_download_many.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), vpp, vpp]
     lib.gpe_step.restype = st
     lib.gpe_step.argtypes = [C.c_void_p, C.c_int64]
     lib.gpe_synchronize.restype = st
@@ -404,6 +409,45 @@ class Stepper:
         _check(self.lib.gpe_download(self.h, i, e.ctypes.data_as(C.c_void_p),
                                      o.ctypes.data_as(C.c_void_p) if odd else None), "gpe_download")
         return e, o
+
+    def upload_many(self, items):
+        """items: (instance, even, odd, potential) tuples; one gpe_upload_many
+        call (every copy queued, one wait at the end)."""
+        keep, idx, pe, po, pv = [], [], [], [], []
+        for i, even, odd, potential in items:
+            shp = self.shape(i)
+            e, p_e = self._carray(even, shp)
+            o, p_o = self._carray(odd, shp)
+            v, p_v = self._carray(potential, shp, complex_=False)
+            keep += [e, o, v]
+            idx.append(int(i))
+            pe.append(p_e)
+            po.append(p_o)
+            pv.append(p_v)
+        n = len(idx)
+        arr = lambda xs: (C.c_void_p * n)(*[x.value if x is not None else None for x in xs])
+        _check(self.lib.gpe_upload_many(self.h, n, (C.c_int32 * n)(*idx), arr(pe), arr(po), arr(pv)),
+               "gpe_upload_many")
+
+    def download_many(self, indices, outs=None, odd: bool = True):
+        """Fields of several instances in one gpe_download_many call.  outs:
+        optional (even, odd) arrays to fill (e.g. pinned); returns the list."""
+        indices = [int(i) for i in indices]
+        if outs is None:
+            outs = []
+            for i in indices:
+                shp = self.shape(i) + (2,)
+                outs.append((np.empty(shp, self.field_dtype), np.empty(shp, self.field_dtype) if odd else None))
+        for i, (e, o) in zip(indices, outs):
+            want = self.shape(i) + (2,)
+            for a in (e, o):
+                if a is not None and (a.shape != want or a.dtype != self.field_dtype or not a.flags.c_contiguous):
+                    raise ValueError(f"output array for instance {i} must be C-contiguous {self.field_dtype} {want}")
+        n = len(indices)
+        pe = (C.c_void_p * n)(*[e.ctypes.data for e, _ in outs])
+        po = (C.c_void_p * n)(*[o.ctypes.data if o is not None else None for _, o in outs])
+        _check(self.lib.gpe_download_many(self.h, n, (C.c_int32 * n)(*indices), pe, po), "gpe_download_many")
+        return outs
 
     def step(self, steps: int):
         _check(self.lib.gpe_step(self.h, int(steps)), "gpe_step")
