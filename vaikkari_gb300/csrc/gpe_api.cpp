@@ -87,6 +87,10 @@ struct gpe_handle_ {
     double *obs_partials = nullptr;   // observables CTA rows
     double *obs_sums = nullptr;       // per instance, 6 sums
     int obs_max_ctas = 2048;
+    // all instances' observables in one launch: CTA -> instance, first CTA per instance
+    int *obs_cta_inst = nullptr, *obs_cta_begin = nullptr;
+    double *obs_batch_partials = nullptr;
+    int obs_total_ctas = 0;
     void *staging = nullptr;
     size_t staging_bytes = 0;
     void *batch_staging = nullptr;  // gpe_upload_many / gpe_download_many: one slot per transfer
@@ -463,6 +467,9 @@ void free_handle(gpe_handle h)
     cudaFree(h->counter);
     cudaFree(h->obs_partials);
     cudaFree(h->obs_sums);
+    cudaFree(h->obs_cta_inst);
+    cudaFree(h->obs_cta_begin);
+    cudaFree(h->obs_batch_partials);
     cudaFree(h->maps);
     cudaFree(h->lo_maps);
     cudaFree(h->err);
@@ -705,6 +712,22 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
     GPE_CREATE_TRY(cudaMemsetAsync(h->err, 0, sizeof(int), h->stream));
     GPE_CREATE_TRY(cudaMalloc(&h->obs_partials, sizeof(double) * 6 * h->obs_max_ctas));
     GPE_CREATE_TRY(cudaMalloc(&h->obs_sums, sizeof(double) * 6 * cfg->num_instances));
+    std::vector<int> cta_begin(cfg->num_instances + 1, 0), cta_inst;
+    for (int i = 0; i < cfg->num_instances; i++) {
+        const gpe_instance &in = h->inst[i];
+        const int c = observables_ctas((long long)in.nx * in.ny * in.nz * h->ns, h->obs_max_ctas);
+        cta_begin[i + 1] = cta_begin[i] + c;
+        cta_inst.insert(cta_inst.end(), size_t(c), i);
+    }
+    h->obs_total_ctas = cta_begin.back();
+    GPE_CREATE_TRY(cudaMalloc(&h->obs_cta_inst, sizeof(int) * cta_inst.size()));
+    GPE_CREATE_TRY(cudaMalloc(&h->obs_cta_begin, sizeof(int) * cta_begin.size()));
+    GPE_CREATE_TRY(cudaMalloc(&h->obs_batch_partials, sizeof(double) * 6 * size_t(h->obs_total_ctas)));
+    GPE_CREATE_TRY(cudaMemcpyAsync(h->obs_cta_inst, cta_inst.data(), sizeof(int) * cta_inst.size(),
+                                   cudaMemcpyHostToDevice, h->stream));
+    GPE_CREATE_TRY(cudaMemcpyAsync(h->obs_cta_begin, cta_begin.data(), sizeof(int) * cta_begin.size(),
+                                   cudaMemcpyHostToDevice, h->stream));
+    GPE_CREATE_TRY(cudaStreamSynchronize(h->stream));  // the host tables above go out of scope
 
     if (h->fused) {
         h->tile = cfg->tile > 0 && cfg->tile < fused_tile_count() ? cfg->tile : 0;
@@ -1097,10 +1120,14 @@ gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
     if (!out || (field != 0 && field != 1)) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_observables_get: bad arguments");
-    for (int i = 0; i < h->cfg.num_instances; i++) {
-        st = enqueue_observables(h, field_buf(h, field), i, h->obs_sums + 6 * i);
-        if (st != GPE_OK) return st;
-    }
+    // every instance in one launch, then one CTA per instance folds its rows
+    // (the same sums as one launch per instance)
+    GPE_CUDA_TRY(launch_observables_batch(h->cfg.lattice, h->cfg.precision, h->cfg.potential, h->idev, h->obs_cta_inst,
+                                          h->obs_cta_begin, h->obs_total_ctas, field_buf(h, field), h->vpot,
+                                          h->obs_batch_partials, h->stream));
+    GPE_CUDA_TRY(launch_reduce_partials_batch(h->obs_batch_partials, h->obs_cta_begin, h->cfg.num_instances,
+                                              h->obs_sums, h->stream));
+    h->launches += 2;
     std::vector<double> sums(6 * h->cfg.num_instances);
     GPE_CUDA_TRY(cudaMemcpyAsync(sums.data(), h->obs_sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost,
                                  h->stream));

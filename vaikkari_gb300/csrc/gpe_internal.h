@@ -109,6 +109,16 @@ struct ObsLaunch {
 };
 // Per-value observables partial sums for one instance; returns CTAs used.
 cudaError_t launch_observables(const ObsLaunch &l, cudaStream_t s, int *ctas_used);
+// CTAs the observables kernel uses for an instance of `values` values.
+int observables_ctas(long long values, int max_ctas);
+// Observables partial rows of every instance in one launch (cta_inst: instance of
+// each CTA; cta_begin: first CTA of each instance, plus the total), then one
+// CTA per instance folding its rows into out[6 * i ...].
+cudaError_t launch_observables_batch(int lattice, int precision, int potential, const InstDev *inst,
+                                     const int *cta_inst, const int *cta_begin, int total_ctas, const void *field,
+                                     const void *vpot, double *partials, cudaStream_t s);
+cudaError_t launch_reduce_partials_batch(const double *partials, const int *cta_begin, int instances, double *out,
+                                         cudaStream_t s);
 // Reduces `ctas` partial rows (6 doubles each) in fixed order with Kahan
 // compensation into out[6] (device).
 cudaError_t launch_reduce_partials(const double *partials, int ctas, int width, double *out, cudaStream_t s);

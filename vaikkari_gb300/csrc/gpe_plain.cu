@@ -191,20 +191,20 @@ __device__ void cta_tree_store(double (&v)[W], double *out)
     if (t < W) out[t] = sm[t][0];
 }
 
+// One CTA's share of one instance's sums: values first, first + stride, ...;
+// writes the CTA's row of 6 partial sums to `row`.
 template <typename T, int LAT, int POT>
-__global__ void __launch_bounds__(256) observables_kernel(const InstDev *__restrict__ insts, int ii,
-                                                          const typename Cplx<T>::type *__restrict__ f,
-                                                          const T *__restrict__ vpot, double *__restrict__ partials)
+__device__ __forceinline__ void observables_body(const InstDev &d, const typename Cplx<T>::type *__restrict__ f,
+                                                 const T *__restrict__ vpot, long long first, long long stride,
+                                                 double *__restrict__ row)
 {
     using T2 = typename Cplx<T>::type;
     using L = Lat<LAT>;
-    const InstDev &d = insts[ii];
     const long long total = (long long)d.nx * d.ny * d.nz * L::NS;
     Kahan k0, k1, k2, k3;
     const double wsum = L::N0 * d.w[0] + (L::NB - L::N0) * d.w[1];
     const double rdt = 1.0 / d.dt;
-    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
-         v += (long long)gridDim.x * blockDim.x) {
+    for (long long v = first; v < total; v += stride) {
         long long r = v;
         const int x = int(r % d.nx);
         r /= d.nx;
@@ -265,15 +265,39 @@ __global__ void __launch_bounds__(256) observables_kernel(const InstDev *__restr
         k3.add(0.5 * d.g * n2 * n2);
     }
     double acc[6] = {k0.s, k1.s, k2.s, k3.s, 0.0, 0.0};
-    cta_tree_store<6>(acc, partials + 6ll * blockIdx.x);
+    cta_tree_store<6>(acc, row);
+}
+
+template <typename T, int LAT, int POT>
+__global__ void __launch_bounds__(256) observables_kernel(const InstDev *__restrict__ insts, int ii,
+                                                          const typename Cplx<T>::type *__restrict__ f,
+                                                          const T *__restrict__ vpot, double *__restrict__ partials)
+{
+    observables_body<T, LAT, POT>(insts[ii], f, vpot, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                                  (long long)gridDim.x * blockDim.x, partials + 6ll * blockIdx.x);
+}
+
+// Every instance in one launch: CTA b belongs to instance cta_inst[b] and is its
+// (b - cta_begin[i])-th CTA of cta_begin[i+1] - cta_begin[i], so each CTA covers
+// the values it would cover in that instance's own launch (same sums, same rows).
+template <typename T, int LAT, int POT>
+__global__ void __launch_bounds__(256) observables_batch_kernel(const InstDev *__restrict__ insts,
+                                                                const int *__restrict__ cta_inst,
+                                                                const int *__restrict__ cta_begin,
+                                                                const typename Cplx<T>::type *__restrict__ f,
+                                                                const T *__restrict__ vpot,
+                                                                double *__restrict__ partials)
+{
+    const int i = cta_inst[blockIdx.x];
+    const int b = cta_begin[i], n = cta_begin[i + 1] - b;
+    observables_body<T, LAT, POT>(insts[i], f, vpot, (long long)(blockIdx.x - b) * blockDim.x + threadIdx.x,
+                                  (long long)n * blockDim.x, partials + 6ll * blockIdx.x);
 }
 
 cudaError_t launch_observables(const ObsLaunch &l, cudaStream_t s, int *ctas_used)
 {
     const long long total = (long long)l.nx * l.ny * l.nz * l.slots;
-    long long want = (total + 255) / 256;
-    int ctas = int(want < l.max_ctas ? want : l.max_ctas);
-    if (ctas < 1) ctas = 1;
+    const int ctas = observables_ctas(total, l.max_ctas);
     *ctas_used = ctas;
 #define GPE_OBS(T, LAT, POT) \
     observables_kernel<T, LAT, POT><<<ctas, 256, 0, s>>>(l.inst, l.inst_index, (const Cplx<T>::type *)l.field, (const T *)l.vpot, l.partials)
@@ -301,6 +325,57 @@ __global__ void __launch_bounds__(256) reduce_partials_kernel(const double *__re
         acc[k] = kk.s;
     }
     cta_tree_store<6>(acc, out);
+}
+
+int observables_ctas(long long values, int max_ctas)
+{
+    long long want = (values + 255) / 256;
+    int ctas = int(want < max_ctas ? want : max_ctas);
+    return ctas < 1 ? 1 : ctas;
+}
+
+cudaError_t launch_observables_batch(int lattice, int precision, int potential, const InstDev *inst,
+                                     const int *cta_inst, const int *cta_begin, int total_ctas, const void *field,
+                                     const void *vpot, double *partials, cudaStream_t s)
+{
+#define GPE_OBSB(T, LAT, POT)                                                                                     \
+    observables_batch_kernel<T, LAT, POT><<<total_ctas, 256, 0, s>>>(inst, cta_inst, cta_begin,                 \
+                                                                      (const Cplx<T>::type *)field, (const T *)vpot, \
+                                                                      partials)
+    const bool arr = potential == GPE_POTENTIAL_ARRAY;
+    if (precision == GPE_FP64) {
+        if (lattice == GPE_LATTICE_TETRA12) { if (arr) GPE_OBSB(double, 0, 0); else GPE_OBSB(double, 0, 1); }
+        else { if (arr) GPE_OBSB(double, 1, 0); else GPE_OBSB(double, 1, 1); }
+    } else {
+        if (lattice == GPE_LATTICE_TETRA12) { if (arr) GPE_OBSB(float, 0, 0); else GPE_OBSB(float, 0, 1); }
+        else { if (arr) GPE_OBSB(float, 1, 0); else GPE_OBSB(float, 1, 1); }
+    }
+#undef GPE_OBSB
+    return cudaGetLastError();
+}
+
+// One CTA per instance: instance i's rows cta_begin[i] .. cta_begin[i+1]-1, folded
+// exactly as reduce_partials_kernel folds one instance's rows.
+__global__ void __launch_bounds__(256) reduce_partials_batch_kernel(const double *__restrict__ partials,
+                                                                    const int *__restrict__ cta_begin,
+                                                                    double *__restrict__ out)
+{
+    const int i = blockIdx.x;
+    const int b = cta_begin[i], rows = cta_begin[i + 1] - b;
+    double acc[6];
+    for (int k = 0; k < 6; k++) {
+        Kahan kk;
+        for (int r = threadIdx.x; r < rows; r += 256) kk.add(partials[(long long)(b + r) * 6 + k]);
+        acc[k] = kk.s;
+    }
+    cta_tree_store<6>(acc, out + 6ll * i);
+}
+
+cudaError_t launch_reduce_partials_batch(const double *partials, const int *cta_begin, int instances, double *out,
+                                         cudaStream_t s)
+{
+    reduce_partials_batch_kernel<<<instances, 256, 0, s>>>(partials, cta_begin, out);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_reduce_partials(const double *partials, int ctas, int width, double *out, cudaStream_t s)
