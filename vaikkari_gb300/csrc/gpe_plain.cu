@@ -65,8 +65,39 @@ __global__ void __launch_bounds__(256) plain_step_kernel(const InstDev *__restri
     const int s = blockIdx.z % L::NS;
     const int z0 = (blockIdx.z / L::NS) * zc;
     if (x >= d.nx || y >= d.ny) return;
-    const int z1 = min(z0 + zc, d.nz);
     const T sig = (MODE == 1) ? T(imag[ii].sigma) : T(1);
+    if constexpr (sizeof(T) == 8) {
+        // FP64 is bound by the FP64 pipe: one value per thread (zc == 1), indices
+        // formed directly, fewest registers and most values in flight.
+        const int z = z0;
+        T2 S[L::NC];
+#pragma unroll
+        for (int k = 0; k < L::NB; k++) {
+            const int e = L::entry(s * L::NB + k);
+            const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
+            T2 v = prev[field_index(d, sl, x + dx, y + dy, z + dz)];
+            if (MODE == 1) v = c_scale<T>(sig, v);
+            const int c = (k < L::N0) ? 0 : 1;
+            if (k == 0 || k == L::N0) S[c] = v;
+            else S[c] = c_add<T>(S[c], v);
+        }
+        const long long self = field_index(d, s, x, y, z);
+        T2 p = prev[self];
+        if (MODE == 1) p = c_scale<T>(sig, p);
+        T vdt;
+        if (POT == GPE_POTENTIAL_ARRAY) vdt = vpot[self - d.base + d.vbase];
+        else vdt = trap_vdt<T>(vpot, d, s, x, y, z);
+        T Lw[L::NC];
+        Lw[0] = T(d.Lc[0]);
+        if (L::NC > 1) Lw[L::NC - 1] = T(d.Lc[1]);
+        T hx, hy, nrm;
+        hpsi<T, L::NC, POT == GPE_POTENTIAL_ARRAY>(p, S, Lw, T(d.L0), vdt, T(d.gdt), hx, hy, nrm);
+        T2 n;
+        if (MODE == 0) n = next[self];
+        next[self] = integrate<T, MODE>(n, p, hx, hy);
+        return;
+    }
+    const int z1 = min(z0 + zc, d.nz);
     const long long base0 = field_index(d, s, x, y, 0);
     long long off[L::NB];
 #pragma unroll
@@ -104,16 +135,23 @@ __global__ void __launch_bounds__(256) plain_step_kernel(const InstDev *__restri
     }
 }
 
-// Planes per thread: enough threads to fill the GPU a few times over, at most 16
-// in FP32 (issue-bound: fewer index computations per value pay) and 2 in FP64
-// (FP64-bound: more independent values in flight pay).  Measured on the
-// production grid (TETRA12, 27.4 M values): FP32 3.9e10 / 7.1e10 / 8.6e10 / 8.8e10
-// value-updates/s for 1 / 2 / 8 / 16 planes, FP64 1.649e10 for 1-2 and 1.62e10 for 16.
+// Planes per thread.  FP32 is issue-bound, so fewer index computations per value
+// pay, the more so the larger the grid; FP64 is FP64-bound and wants many
+// independent values in flight.  Measured with TETRA12 (value-updates/s):
+//   32^3  (393 K values): FP32 2.4e10 / 3.2e10 / 3.2e10 for 1 / 2 / 4 planes
+//   48^3  (1.3 M):        FP32 3.4e10 / 5.2e10 / 5.4e10 for 1 / 2 / 4
+//   96^3  (10.6 M):       FP32 4.2e10 / 7.3e10 / 8.1e10 / 8.4e10 for 1 / 2 / 4 / 8
+//   87x87x302 (27.4 M):   FP32 8.6e10 / 8.8e10 for 8 / 16; FP64 1.649e10 for 1-2, 1.62e10 for 16
+// FP64 takes one value per thread in its own code path (32 registers, as many
+// values in flight as possible); on 32^3 that path gives 1.22e10 against
+// 1.14e10 for two planes per thread in the marching path.
 static int plain_zchunk(long long values, bool fp64)
 {
-    const long long cap = fp64 ? 2 : 16;
-    long long zc = values / (152ll * 2048 * 4);
-    return int(zc < 1 ? 1 : (zc > cap ? cap : zc));
+    if (fp64) return 1;
+    if (values < (1ll << 20)) return 2;
+    if (values < (4ll << 20)) return 4;
+    if (values < (16ll << 20)) return 8;
+    return 16;
 }
 
 template <typename T, int LAT>
