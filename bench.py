@@ -297,7 +297,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "batch64_bcc2_realtime", "instances": len(items), "sample_instances": len(sample),
+        "config": {"workload": "batch64_bcc2_trap_realtime", "instances": len(items), "sample_instances": len(sample),
                    "vertices_per_step": acc, "dt": 1e-4, "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -419,7 +419,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": args.scaling, "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batch64_bcc2_fp32_trap_realtime" + ("_compensated" if comp_main else ""),
+            "config": {"workload": "batch64_bcc2_trap_realtime" + ("_compensated" if comp_main else ""),
                        "storage": "fp32 + bf16 residual" if comp_main else "fp32", "instances": len(insts),
                        "vertices": verts, "vertices_all_ranks": verts_job,
                        "sizes": sorted({i.nx for i in insts}), "dt": 1e-4,
