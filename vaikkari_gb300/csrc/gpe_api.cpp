@@ -754,14 +754,19 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
         });
         int zc = cfg->zchunk;
         if (zc <= 0) {
-            // Real time: aim for >= ~4 waves of 152 SMs x 8 CTAs while keeping chunks
-            // >= 8 planes.  Imaginary time pays a reduction per item and a final
-            // fold over all items every step, so it aims for about two items per SM.
-            const long long target = cfg->mode == GPE_IMAGINARY_TIME ? 152ll * 2 : 152ll * 8 * 4;
+            // Real time: aim for >= ~4 waves of 152 SMs x 8 CTAs, halving the chunk
+            // down to 2 planes: a small grid needs short chunks to occupy the GPU
+            // (one 32^3 instance: 1.45e10 vertex-updates/s with 2-plane chunks,
+            // 1.01e10 with 8).  Imaginary time pays a reduction per item and a final
+            // fold over all items every step, so it aims for about two items per SM
+            // and keeps chunks of at least 8 planes.
+            const bool imag = cfg->mode == GPE_IMAGINARY_TIME;
+            const long long target = imag ? 152ll * 2 : 152ll * 8 * 4;
+            const int zmin = imag ? 8 : 2;
             long long maxnz = 1;
             for (auto &in : h->inst) maxnz = std::max<long long>(maxnz, in.nz);
             zc = int(maxnz);
-            while (zc > 8) {
+            while (zc > zmin) {
                 long long items = 0;
                 for (auto &in : h->inst)
                     items += (long long)((in.nx + h->tx - 1) / h->tx) * ((in.ny + h->ty - 1) / h->ty) *
@@ -769,7 +774,7 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
                 if (items >= target) break;
                 zc = (zc + 1) / 2;
             }
-            if (zc < 8) zc = std::min<long long>(8, maxnz);
+            if (zc < zmin) zc = int(std::min<long long>(zmin, maxnz));
         }
         h->zchunk = zc;
         h->zcmax = 1;
