@@ -89,7 +89,7 @@ def measure(instances: List[Instance], tile: int, zchunk: int, fields=None, latt
 
 def autotune(instances: List[Instance], fields=None, lattice=Lattice.BCC2, precision=Precision.FP32,
              potential=Potential.TRAP, device: int = 0, steps: int = 200, cache: bool = True,
-             zchunks: Sequence[int] = (0, 16, 32), verbose: bool = False, mode=Mode.REAL) -> dict:
+             zchunks: Sequence[int] = (0, 8, 16, 32), verbose: bool = False, mode=Mode.REAL) -> dict:
     """Best (tile, zchunk) for this batch.  Every variant is timed with the
     automatic z-chunk, then the three fastest with each z-chunk in `zchunks`.
     Imaginary time and compensated storage (Precision.FP32C) skip the variants
