@@ -977,6 +977,23 @@ void fused_variant(int tile, int *tx, int *ty, int *stages, int *minb)
     *minb = v.minb;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the library
+// links only the CUDA runtime); looked up once.
+using TensorMapEncode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                     const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static TensorMapEncode tensor_map_encoder()
+{
+    static TensorMapEncode encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e == cudaSuccess && q == cudaDriverEntryPointSuccess && fn) encode = (TensorMapEncode)fn;
+    }
+    return encode;
+}
+
 // The two 4-D tensor maps of one field of one instance (out_map[0], out_map[1]):
 // dimensions (x in 8-byte elements, y, slot, z) over the padded layout; boxes =
 // tile plus a 2-column / 1-row halo (previous-field loads) and the interior tile
@@ -985,18 +1002,8 @@ void fused_variant(int tile, int *tx, int *ty, int *stages, int *minb)
 // zero-filled by the TMA unit.
 gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *field_arena, int tile)
 {
-    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-    static Encode encode = nullptr;
-    if (!encode) {
-        void *fn = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
-        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
-            return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-        encode = (Encode)fn;
-    }
+    TensorMapEncode encode = tensor_map_encoder();
+    if (!encode) return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     int tx, ty;
     fused_tile_shape(tile, &tx, &ty);
     const int csize = precision == GPE_FP64 ? 16 : 8;
@@ -1024,15 +1031,8 @@ gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *f
 // 16-byte-aligned column, TY rows, both slots, one plane.
 gpe_status make_residual_map(void *out_map, const InstDev &d, void *lo_arena, int tile)
 {
-    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-    void *fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
-    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
-        return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-    Encode encode = (Encode)fn;
+    TensorMapEncode encode = tensor_map_encoder();
+    if (!encode) return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     int tx, ty;
     fused_tile_shape(tile, &tx, &ty);
     const cuuint64_t dims[4] = {(cuuint64_t)d.px, (cuuint64_t)d.py, 2, (cuuint64_t)d.nz + 2};
@@ -1054,15 +1054,8 @@ gpe_status make_residual_map(void *out_map, const InstDev &d, void *lo_arena, in
 gpe_status make_twostep_maps(void *out_map, int precision, const InstDev &d, void *even_arena, void *odd_arena,
                              int tile)
 {
-    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-    void *fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
-    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
-        return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-    Encode encode = (Encode)fn;
+    TensorMapEncode encode = tensor_map_encoder();
+    if (!encode) return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     int tx, ty;
     fused_tile_shape(tile, &tx, &ty);
     const int csize = precision == GPE_FP64 ? 16 : 8;
