@@ -615,15 +615,17 @@ def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1, latt
     slots = 12 if ref_mode else 2
     verts = sum(i.nx * i.ny * i.nz for i in insts) * slots
     kern = Kernel.PLAIN if ref_mode else Kernel.FUSED
+    zchunk = 0
     if ref_mode:
         tile = 0
     elif tile < 0:
         from vaikkari_gb300.autotune import autotune
-        tile = autotune(insts)["tile"]
+        t = autotune(insts)
+        tile, zchunk = t["tile"], t["zchunk"]
     fp64_last = fp64_steps or checkpoints[-1]
     runs = {}
     for prec, dt_, last in ((Precision.FP64, np.float64, fp64_last), (Precision.FP32, np.float32, checkpoints[-1])):
-        st = _stepper(conds, prec, kern, Mode.REAL, tile=tile, lattice=lattice)
+        st = _stepper(conds, prec, kern, Mode.REAL, tile=tile, lattice=lattice, zchunk=zchunk)
         prepare_fields(st, conds, dt_)
         o0 = st.observables(0)
         done, cps = 0, {}
@@ -656,7 +658,8 @@ def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1, latt
              else (("fp32_fused", Precision.FP32, Kernel.FUSED), ("fp64_fused", Precision.FP64, Kernel.FUSED),
                    ("fp64_plain", Precision.FP64, Kernel.PLAIN)))
     for key, prec, kern_ in cases:
-        st = _stepper(conds, prec, kern_, Mode.REAL, tile=tile, lattice=lattice)
+        st = _stepper(conds, prec, kern_, Mode.REAL, tile=tile if kern_ == kern else 0, lattice=lattice,
+                      zchunk=zchunk if kern_ == Kernel.FUSED else 0)
         prepare_fields(st, conds, np.float64 if prec == Precision.FP64 else np.float32)
         st.time_steps(103)
         ms = min(st.time_steps(200) for _ in range(2))
@@ -665,7 +668,7 @@ def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1, latt
     return {"metric": METRIC, "value": rates["fp32_plain" if ref_mode else "fp32_fused"], "unit": METRIC,
             "dtype": "f32",
             "config": {"workload": name, "lattice": lattice.name, "instances": len(insts), "vertices": verts,
-                       "dt": insts[0].dt, "variant": tile,
+                       "dt": insts[0].dt, "variant": tile, "zchunk": zchunk,
                        "mode": "ref-mode (12 values per block, block scale a/sqrt(8))" if ref_mode
                        else "config-mode (2 values per cell)"},
             "rates": rates, "accuracy": acc, "cpu_baseline": _cpu_config_rate(conds, lattice=lattice)}

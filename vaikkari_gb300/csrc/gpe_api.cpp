@@ -775,6 +775,15 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
                 zc = (zc + 1) / 2;
             }
             if (zc < zmin) zc = int(std::min<long long>(zmin, maxnz));
+            if (!imag && zc < 8 && maxnz >= 8) {
+                // below 8 planes the two halo planes of every item weigh more: go
+                // back to 8 wherever 8 still gives about four items per SM
+                long long items8 = 0;
+                for (auto &in : h->inst)
+                    items8 += (long long)((in.nx + h->tx - 1) / h->tx) * ((in.ny + h->ty - 1) / h->ty) *
+                              ((in.nz + 7) / 8);
+                if (items8 >= 152ll * 4) zc = 8;
+            }
         }
         h->zchunk = zc;
         h->zcmax = 1;
