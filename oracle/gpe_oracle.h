@@ -1,7 +1,7 @@
 /*
  * gpe_oracle.h - CPU oracle for the GPE stepper.  TEST INFRASTRUCTURE ONLY:
- * loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as
- * the checker; never part of the shipped library.
+ * loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg to
+ * check the library's results; never part of the shipped library.
  *
  * A plain-C restatement of the reference's algorithm
  * (markus-kivioja/vaikkari, koodit/GrossPitaevskii/GPUGrossPitaevskii_BCC.cu):

@@ -1,7 +1,8 @@
 """Python binding of the CPU oracle (oracle/gpe_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py, as the checker.  The product never imports it.
+CPU-baseline leg of bench.py, to check the library's results.  The product
+never imports it.
 
 It also restates, in numpy, how the reference turns a lattice and a time step
 into the update's factors (koodit/GrossPitaevskii/GPUGrossPitaevskii_BCC.cu:
