@@ -95,3 +95,23 @@ def test_binding_rejects_wrong_shapes():
     assert a.shape == shp
     with pytest.raises(IndexError):
         st.shape(1)
+
+
+def test_batched_transfer_bindings_check_arrays_first():
+    """upload_many / download_many check every array before the library sees a
+    pointer (no GPU needed: the checks raise before any call)."""
+    st = Stepper.__new__(Stepper)
+    st.instances = [Instance(4, 3, 2, 0.5, 1e-3, 1.0), Instance(2, 2, 2, 0.5, 1e-3, 1.0)]
+    st.slots = 2
+    st.dtype = st.field_dtype = np.float32
+    shp0 = st.shape(0)
+    with pytest.raises(ValueError):
+        st.upload_many([(0, np.ones(shp0, complex), np.ones(st.shape(1), complex), None)])   # odd of the wrong size
+    with pytest.raises(IndexError):
+        st.upload_many([(2, np.ones(shp0, complex), None, None)])
+    with pytest.raises(ValueError):
+        st.download_many([0], outs=[(np.empty(shp0 + (2,), np.float64), None)])              # wrong element type
+    with pytest.raises(ValueError):
+        st.download_many([1], outs=[(np.empty(shp0 + (2,), np.float32), None)])              # wrong shape
+    with pytest.raises(ValueError):
+        st.download_many([0], outs=[(np.empty(shp0 + (2,), np.float32)[..., ::-1], None)])   # not contiguous
