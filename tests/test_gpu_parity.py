@@ -230,6 +230,42 @@ def test_imaginary_time_many_instances_equal_single_runs():
         assert mu[i] == mu1[0]
 
 
+@pytest.mark.parametrize("prec", [Precision.FP32, Precision.FP64])
+@pytest.mark.parametrize("mode", [Mode.REAL, Mode.IMAGINARY])
+def test_plain_batch_equals_single_runs(prec, mode):
+    """A batch on the plain kernel runs in one launch per half-step; each
+    instance ends bit-identical to its own single run.  Sizes differ, and one
+    instance is large enough to march more planes per thread than the others."""
+    dims = [(5, 4, 3), (17, 9, 11), (40, 30, 100), (1, 1, 1), (33, 8, 7)]
+    rng = np.random.default_rng(21)
+    insts = [Instance(nx, ny, nz, 0.2 + 0.02 * k, 1e-3, 10.0 + k, origin=(-0.1 * nx, -0.1 * ny, -0.1 * nz))
+             for k, (nx, ny, nz) in enumerate(dims)]
+    kw = dict(lattice=Lattice.TETRA12, precision=prec, kernel=Kernel.PLAIN, mode=mode, potential=Potential.ARRAY,
+              graph_steps=5)
+    fields = []
+    for inst in insts:
+        shp = (inst.nz, inst.ny, inst.nx, 12)
+        fields.append((random_state(shp, int(rng.integers(1000)), 0.3), random_state(shp, int(rng.integers(1000)), 0.3),
+                       rng.uniform(0, 5, shp)))
+
+    def run(sel):
+        st = Stepper([insts[i] for i in sel], **kw)
+        for k, i in enumerate(sel):
+            e, o, V = fields[i]
+            st.upload(k, e, o if mode == Mode.REAL else None, V)
+        if mode == Mode.REAL:
+            st.step(7)
+        else:
+            st.imaginary_time(7, 0.0)
+        out = [st.download(k, odd=False)[0] for k in range(len(sel))]
+        st.close()
+        return out
+
+    batch = run(list(range(len(insts))))
+    for i in range(len(insts)):
+        np.testing.assert_array_equal(batch[i], run([i])[0], err_msg=f"instance {i}")
+
+
 def test_fused_batch_of_300_tiny_instances_bit_exact():
     """One fused launch over 300 instances of 1..4 blocks per side."""
     rng = np.random.default_rng(13)

@@ -72,6 +72,9 @@ struct gpe_handle_ {
     bool two_step = false;
     void *vpot = nullptr;
     void *vbase = nullptr;  // array potential: L0 + V*dt per value for the plain kernel
+    // plain kernel over a batch: CTA -> instance, first CTA per instance, planes per thread
+    int *pb_inst = nullptr, *pb_begin = nullptr, *pb_zcs = nullptr;
+    int pb_blocks = 0;
     bool fused = false;
     int tile = 0, tx = 32, ty = 8, zchunk = 0, zcmax = 1;
     std::vector<WorkItem> items;
@@ -200,6 +203,26 @@ gpe_status enqueue_halo(gpe_handle h, int field)
     return GPE_OK;
 }
 
+PlainBatchLaunch plain_batch(gpe_handle h, int mode, void *prev, void *next)
+{
+    PlainBatchLaunch l{};
+    l.lattice = h->cfg.lattice;
+    l.precision = h->cfg.precision;
+    l.mode = mode;
+    l.potential = h->cfg.potential;
+    l.inst = h->idev;
+    l.blk_inst = h->pb_inst;
+    l.blk_begin = h->pb_begin;
+    l.zcs = h->pb_zcs;
+    l.blocks = h->pb_blocks;
+    l.prev = prev;
+    l.next = next;
+    l.vpot = h->vpot;
+    l.vbase = h->vbase;
+    l.imag = h->imag;
+    return l;
+}
+
 gpe_status enqueue_step_real(gpe_handle h)
 {
     if (h->two_step) {
@@ -254,6 +277,9 @@ gpe_status enqueue_step_real(gpe_handle h)
             l.err = h->err;
             l.num_instances = h->cfg.num_instances;
             GPE_CUDA_TRY(launch_fused_step(l, h->stream));
+            h->launches++;
+        } else if (h->pb_blocks > 0) {
+            GPE_CUDA_TRY(launch_plain_step_batch(plain_batch(h, GPE_REAL_TIME, prev, next), h->stream));
             h->launches++;
         } else {
             for (int i = 0; i < h->cfg.num_instances; i++) {
@@ -342,6 +368,14 @@ gpe_status enqueue_step_imag(gpe_handle h, int parity)
         gpe_status st = enqueue_observables(h, prev, i, sums);
         if (st != GPE_OK) return st;
         GPE_CUDA_TRY(launch_imag_finalize_plain(sums, h->idev, i, h->imag, h->tol, nullptr, h->stream));
+        h->launches++;
+    }
+    if (h->pb_blocks > 0) {
+        GPE_CUDA_TRY(launch_plain_step_batch(plain_batch(h, GPE_IMAGINARY_TIME, prev, next), h->stream));
+        h->launches++;
+        return GPE_OK;
+    }
+    for (int i = 0; i < h->cfg.num_instances; i++) {
         StepLaunch l{};
         l.lattice = h->cfg.lattice;
         l.precision = h->cfg.precision;
@@ -359,7 +393,7 @@ gpe_status enqueue_step_imag(gpe_handle h, int parity)
         l.vbase = h->vbase;
         l.imag = h->imag;
         GPE_CUDA_TRY(launch_plain_step(l, h->stream));
-        h->launches += 2;
+        h->launches++;
     }
     return GPE_OK;
 }
@@ -460,6 +494,9 @@ void free_handle(gpe_handle h)
     for (void *b : h->lo) cudaFree(b);
     cudaFree(h->vpot);
     cudaFree(h->vbase);
+    cudaFree(h->pb_inst);
+    cudaFree(h->pb_begin);
+    cudaFree(h->pb_zcs);
     cudaFree(h->items_dev);
     cudaFree(h->item_begin_dev);
     cudaFree(h->imag);
@@ -727,6 +764,35 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
                                    cudaMemcpyHostToDevice, h->stream));
     GPE_CREATE_TRY(cudaMemcpyAsync(h->obs_cta_begin, cta_begin.data(), sizeof(int) * cta_begin.size(),
                                    cudaMemcpyHostToDevice, h->stream));
+    // The plain kernel over a batch: one launch per half-step for all instances.
+    std::vector<int> pb_begin, pb_inst, pb_zcs;
+    if (!h->fused && cfg->num_instances > 1) {
+        pb_begin.assign(cfg->num_instances + 1, 0);
+        for (int i = 0; i < cfg->num_instances; i++) {
+            const gpe_instance &in = h->inst[i];
+            const int zc = plain_planes_per_thread((long long)in.nx * in.ny * in.nz * h->ns, cfg->precision);
+            const long long blocks = (long long)((in.nx + 31) / 32) * ((in.ny + 7) / 8) * ((in.nz + zc - 1) / zc) * h->ns;
+            if ((long long)pb_begin[i] + blocks > 0x7fffffffll) {
+                pb_begin.clear();
+                break;  // too many CTAs for one launch: keep one launch per instance
+            }
+            pb_begin[i + 1] = pb_begin[i] + int(blocks);
+            pb_inst.insert(pb_inst.end(), size_t(blocks), i);
+            pb_zcs.push_back(zc);
+        }
+        if (!pb_begin.empty()) {
+            h->pb_blocks = pb_begin.back();
+            GPE_CREATE_TRY(cudaMalloc(&h->pb_inst, sizeof(int) * pb_inst.size()));
+            GPE_CREATE_TRY(cudaMalloc(&h->pb_begin, sizeof(int) * pb_begin.size()));
+            GPE_CREATE_TRY(cudaMalloc(&h->pb_zcs, sizeof(int) * pb_zcs.size()));
+            GPE_CREATE_TRY(cudaMemcpyAsync(h->pb_inst, pb_inst.data(), sizeof(int) * pb_inst.size(),
+                                           cudaMemcpyHostToDevice, h->stream));
+            GPE_CREATE_TRY(cudaMemcpyAsync(h->pb_begin, pb_begin.data(), sizeof(int) * pb_begin.size(),
+                                           cudaMemcpyHostToDevice, h->stream));
+            GPE_CREATE_TRY(cudaMemcpyAsync(h->pb_zcs, pb_zcs.data(), sizeof(int) * pb_zcs.size(),
+                                           cudaMemcpyHostToDevice, h->stream));
+        }
+    }
     GPE_CREATE_TRY(cudaStreamSynchronize(h->stream));  // the host tables above go out of scope
 
     if (h->fused) {

@@ -51,6 +51,19 @@ struct StepLaunch {
     const ImagScalars *imag;  // imaginary time: per-instance scale of prev (device), may be null
 };
 cudaError_t launch_plain_step(const StepLaunch &l, cudaStream_t s);
+// Planes each thread of the plain kernel marches for an instance of `values` values.
+int plain_planes_per_thread(long long values, int precision);
+// The plain step of every instance in one launch (tables from the handle).
+struct PlainBatchLaunch {
+    int lattice, precision, mode, potential;
+    const InstDev *inst;
+    const int *blk_inst, *blk_begin, *zcs;  // CTA -> instance, first CTA per instance, planes per thread
+    int blocks;
+    void *prev, *next;
+    const void *vpot, *vbase;
+    const ImagScalars *imag;
+};
+cudaError_t launch_plain_step_batch(const PlainBatchLaunch &l, cudaStream_t s);
 // Array potential: vbase = L0 + V*dt (in the handle's precision) for one instance.
 cudaError_t launch_potential_base(int precision, const InstDev *inst, int ii, int nx, int ny, int nz, int slots,
                                   const void *vpot, void *vbase, cudaStream_t s);

@@ -50,20 +50,22 @@ cudaError_t set_plain_table(const gpe_lattice_info &info)
 // planes z0 .. z0+zc-1: the neighbours' offsets from the value are the same on
 // every plane, so they are formed once and each plane only advances the index
 // by one z-stride (the per-value arithmetic does not depend on this).
+// (bx, by, bz): the CTA's block of the instance's grid (32 x 8 threads,
+// bz = plane chunk * slots + slot).
 template <typename T, int LAT, int MODE, int POT>
-__global__ void __launch_bounds__(256) plain_step_kernel(const InstDev *__restrict__ insts, int ii,
-                                                         const typename Cplx<T>::type *__restrict__ prev,
-                                                         typename Cplx<T>::type *__restrict__ next,
-                                                         const T *__restrict__ vpot, const ImagScalars *__restrict__ imag,
-                                                         int zc)
+__device__ __forceinline__ void plain_step_body(const InstDev *__restrict__ insts, int ii,
+                                                const typename Cplx<T>::type *__restrict__ prev,
+                                                typename Cplx<T>::type *__restrict__ next,
+                                                const T *__restrict__ vpot, const ImagScalars *__restrict__ imag, int zc,
+                                                int bx, int by, int bz)
 {
     using T2 = typename Cplx<T>::type;
     using L = Lat<LAT>;
     const InstDev &d = insts[ii];
-    const int x = blockIdx.x * 32 + threadIdx.x;
-    const int y = blockIdx.y * 8 + threadIdx.y;
-    const int s = blockIdx.z % L::NS;
-    const int z0 = (blockIdx.z / L::NS) * zc;
+    const int x = bx * 32 + threadIdx.x;
+    const int y = by * 8 + threadIdx.y;
+    const int s = bz % L::NS;
+    const int z0 = (bz / L::NS) * zc;
     if (x >= d.nx || y >= d.ny) return;
     const T sig = (MODE == 1) ? T(imag[ii].sigma) : T(1);
     if constexpr (sizeof(T) == 8) {
@@ -133,6 +135,38 @@ __global__ void __launch_bounds__(256) plain_step_kernel(const InstDev *__restri
         if (MODE == 0) n = next[self];
         next[self] = integrate<T, MODE>(n, p, hx, hy);
     }
+}
+
+template <typename T, int LAT, int MODE, int POT>
+__global__ void __launch_bounds__(256) plain_step_kernel(const InstDev *__restrict__ insts, int ii,
+                                                         const typename Cplx<T>::type *__restrict__ prev,
+                                                         typename Cplx<T>::type *__restrict__ next,
+                                                         const T *__restrict__ vpot, const ImagScalars *__restrict__ imag,
+                                                         int zc)
+{
+    plain_step_body<T, LAT, MODE, POT>(insts, ii, prev, next, vpot, imag, zc, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// Every instance of a batch in one launch: CTA b is block b - blk_begin[i] of
+// instance i = blk_inst[b], numbered x fastest, then y, then z chunk and slot, as
+// in that instance's own launch (same values per thread, same results).
+template <typename T, int LAT, int MODE, int POT>
+__global__ void __launch_bounds__(256) plain_step_batch_kernel(const InstDev *__restrict__ insts,
+                                                               const int *__restrict__ blk_inst,
+                                                               const int *__restrict__ blk_begin,
+                                                               const int *__restrict__ zcs,
+                                                               const typename Cplx<T>::type *__restrict__ prev,
+                                                               typename Cplx<T>::type *__restrict__ next,
+                                                               const T *__restrict__ vpot,
+                                                               const ImagScalars *__restrict__ imag)
+{
+    const int i = blk_inst[blockIdx.x];
+    const int local = blockIdx.x - blk_begin[i];
+    const InstDev &d = insts[i];
+    const int gx = (d.nx + 31) / 32, gy = (d.ny + 7) / 8;
+    const int rest = local / gx;
+    plain_step_body<T, LAT, MODE, POT>(insts, i, prev, next, vpot, imag, zcs[i], local - rest * gx, rest % gy,
+                                       rest / gy);
 }
 
 // Planes per thread.  FP32 is issue-bound, so fewer index computations per value
@@ -210,6 +244,35 @@ cudaError_t launch_potential_base(int precision, const InstDev *inst, int ii, in
     else
         potential_base_kernel<float><<<int(g), 256, 0, s>>>(inst, ii, (const float *)vpot, (float *)vbase);
     return cudaGetLastError();
+}
+
+int plain_planes_per_thread(long long values, int precision) { return plain_zchunk(values, precision == GPE_FP64); }
+
+template <typename T, int LAT>
+static cudaError_t plain_batch_mode(const PlainBatchLaunch &l, cudaStream_t st)
+{
+    using T2 = typename Cplx<T>::type;
+    const T2 *prev = (const T2 *)l.prev;
+    T2 *next = (T2 *)l.next;
+    const T *v = (const T *)(l.potential == GPE_POTENTIAL_ARRAY ? l.vbase : l.vpot);
+#define GPE_PB(MODE, POT) \
+    plain_step_batch_kernel<T, LAT, MODE, POT><<<l.blocks, dim3(32, 8, 1), 0, st>>>(l.inst, l.blk_inst, l.blk_begin, \
+                                                                                 l.zcs, prev, next, v, l.imag)
+    const bool arr = l.potential == GPE_POTENTIAL_ARRAY;
+    if (l.mode == GPE_REAL_TIME) { if (arr) GPE_PB(0, 0); else GPE_PB(0, 1); }
+    else { if (arr) GPE_PB(1, 0); else GPE_PB(1, 1); }
+#undef GPE_PB
+    return cudaGetLastError();
+}
+
+cudaError_t launch_plain_step_batch(const PlainBatchLaunch &l, cudaStream_t s)
+{
+    if (l.precision == GPE_FP64) {
+        if (l.lattice == GPE_LATTICE_TETRA12) return plain_batch_mode<double, GPE_LATTICE_TETRA12>(l, s);
+        return plain_batch_mode<double, GPE_LATTICE_BCC2>(l, s);
+    }
+    if (l.lattice == GPE_LATTICE_TETRA12) return plain_batch_mode<float, GPE_LATTICE_TETRA12>(l, s);
+    return plain_batch_mode<float, GPE_LATTICE_BCC2>(l, s);
 }
 
 cudaError_t launch_plain_step(const StepLaunch &l, cudaStream_t s)
