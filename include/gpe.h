@@ -281,6 +281,8 @@ typedef struct gpe_integrate_result {
     double maxpot, dt, lapfac_dt, lapfac0_dt, g_dt;
     double odd_phase[2];
     double device_ms;         /* device time of all steps (gpe_integrate_in_time)       */
+    double setup_ms;          /* wall time of the set-up up to the fields on the device
+                                 (gpe_integrate_in_time)                                  */
 } gpe_integrate_result;
 
 /* VortexState::load (VortexState.cpp:49-72). */
@@ -296,9 +298,15 @@ gpe_status gpe_vortex_psi(gpe_vortex v, const double *p, double *out);
  * potential (V unscaled, values doubles). */
 gpe_status gpe_integrate_setup(gpe_vortex v, const gpe_integrate_desc *d, gpe_integrate_result *res,
                                double *even, double *odd, double *potential);
+/* The grid integrateInTime builds for `d` (GPUGrossPitaevskii_BCC.cu:222-268):
+ * xsize, ysize, zsize, values and p0 of `res`, the other fields zero.  It samples
+ * nothing, so callers can size their buffers cheaply. */
+gpe_status gpe_integrate_grid(const gpe_integrate_desc *d, gpe_integrate_result *res);
 /* integrateInTime (GPUGrossPitaevskii_BCC.cu:218-499): set-up, then
  * number_of_iterations iterations of steps_per_iteration leapfrog steps on the
- * GPU.  per_iteration (may be NULL) receives number_of_iterations+1 observables
+ * GPU.  The set-up's per-value work (positions, psi, V, maxpot, noise and the odd
+ * phase) runs on the GPU with the values of gpe_integrate_setup, bit for bit;
+ * the noise stream is drawn on the host in its order.  per_iteration (may be NULL) receives number_of_iterations+1 observables
  * of the even field, before each iteration and after the last; even_out/odd_out
  * (may be NULL) the final fields. */
 gpe_status gpe_integrate_in_time(gpe_vortex v, const gpe_integrate_desc *d, gpe_integrate_result *res,

@@ -56,6 +56,42 @@ def test_integrate_setup_equals_reference():
     np.testing.assert_array_equal((V * res["dt"]).reshape(-1), rp)
 
 
+def test_integrate_grid_equals_setup():
+    """gpe_integrate_grid gives the set-up's grid without sampling."""
+    ref = golden("ref_setup_small.json")
+    st = _state()
+    grid = st.grid(ref["block_scale"], ref["minp"], ref["maxp"])
+    res = st.setup(ref["block_scale"], ref["minp"], ref["maxp"])[0]
+    for k in ("xsize", "ysize", "zsize", "values", "p0"):
+        assert grid[k] == res[k], k
+    assert grid["maxpot"] == 0.0 and grid["steps_per_iteration"] == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [Precision.FP64, Precision.FP32])
+def test_integrate_setup_on_gpu_equals_reference(prec):
+    """The set-up inside gpe_integrate_in_time runs its per-value work on the GPU.
+    With no iterations the fields it returns are the reference's own set-up
+    (GPUGrossPitaevskii_BCC.cu:222-348, fixture made by running it) bit for bit,
+    in FP32 after one rounding to float."""
+    ref = golden("ref_setup_small.json")
+    res, obs, even, odd = _state().integrate_in_time(ref["block_scale"], ref["minp"], ref["maxp"], 1.0, 0,
+                                                     precision=prec)
+    assert len(obs) == 1 and res["setup_ms"] > 0.0
+    assert res["steps_per_iteration"] == ref["steps_per_iteration"]
+    for k_ours, k_ref in (("maxpot", "maxpot"), ("dt", "dt"), ("lapfac_dt", "lapfac_dt"),
+                          ("lapfac0_dt", "lapfac0_dt"), ("g_dt", "g_dt")):
+        assert res[k_ours] == ref[k_ref], k_ours
+    assert res["odd_phase"] == ref["odd_phase"]
+    n = res["values"]
+    raw = np.fromfile(os.path.join(GOLDEN, "ref_setup_small.bin"), dtype=np.float64)
+    re, ro = raw[:2 * n], raw[2 * n:4 * n]
+    if prec == Precision.FP32:
+        re, ro = re.astype(np.float32).astype(np.float64), ro.astype(np.float32).astype(np.float64)
+    np.testing.assert_array_equal(even.reshape(-1), re)
+    np.testing.assert_array_equal(odd.reshape(-1), ro)
+
+
 @pytest.mark.gpu
 def test_integrate_in_time_matches_reference_kernel():
     """Two iterations (2 x steps_per_iteration leapfrog steps) of the drop-in on

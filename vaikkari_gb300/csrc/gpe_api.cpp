@@ -1395,3 +1395,38 @@ int64_t gpe_launch_count(gpe_handle h) { return h ? h->launches : 0; }
 void *gpe_stream(gpe_handle h) { return h ? (void *)h->stream : nullptr; }
 
 }  // extern "C"
+
+namespace gpe {
+
+gpe_status upload_device_fields(gpe_handle h, int32_t instance, const void *even, const void *odd,
+                                const void *potential)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (instance < 0 || instance >= h->cfg.num_instances)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "upload_device_fields: bad instance");
+    if (h->comp) return fail(GPE_ERR_UNSUPPORTED, "upload_device_fields: not for GPE_FP32C");
+    if (!even || (h->cfg.mode == GPE_REAL_TIME && !odd) || (h->cfg.potential == GPE_POTENTIAL_ARRAY && !potential))
+        return fail(GPE_ERR_INVALID_ARGUMENT, "upload_device_fields: missing field or potential");
+    const gpe_instance &in = h->inst[instance];
+    const int prec = h->cfg.precision;
+    const void *srcs[2] = {even, odd};
+    for (int f = 0; f < 2; f++) {
+        if (!srcs[f]) continue;
+        GPE_CUDA_TRY(launch_pack(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, srcs[f], field_buf(h, f), 1,
+                                 1.0, h->stream));
+        h->launches++;
+    }
+    if (h->cfg.potential == GPE_POTENTIAL_ARRAY) {
+        GPE_CUDA_TRY(launch_pack(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, potential, h->vpot, 0, in.dt,
+                                 h->stream));
+        GPE_CUDA_TRY(launch_potential_base(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->vpot, h->vbase,
+                                           h->stream));
+        h->launches += 2;
+    }
+    GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->imag_ready = false;
+    return GPE_OK;
+}
+
+}  // namespace gpe

@@ -165,4 +165,30 @@ cudaError_t launch_imag_init(const double *sums, const InstDev *inst, int inst_i
                              cudaStream_t s);
 cudaError_t launch_set_sigma_one(ImagScalars *imag, int n, cudaStream_t s);
 
+// integrateInTime's set-up on the GPU (gpe_setup.cu).
+struct SetupGeometry {
+    uint32_t nx, ny, nz;            // blocks per axis
+    uint32_t kappa, rsize, zsize;   // the vortex profile's winding and table size
+    double p0[3];                   // position of block (0, 0, 0)
+    double bs, W;                   // block_scale and BLOCK_WIDTH = sqrt(8)
+    double bpos[12][3];             // circumcentre offsets in units of block_scale
+    double ratio, coupling;         // potentialV3's RATIO and g
+    double rplug, rstep, zstep;     // the profile's r origin and steps
+};
+// psi and V per value in block order, and the bits of max(0, max V + g|psi|^2)
+// into *maxbits (which must start at 0).
+cudaError_t launch_setup_sample(const SetupGeometry &geo, const double *f, double2 *psi0, double *V,
+                                unsigned long long *maxbits, unsigned long long nvals, cudaStream_t s);
+// even = psi (1 + amplitude * noise * 2^-31), odd = odd_phase * even and V, in
+// the element type of `precision` (GPE_FP64 or GPE_FP32).
+cudaError_t launch_setup_noise(int precision, const double2 *psi0, const int2 *noise, const double *V,
+                               double amplitude, const double odd_phase[2], void *even, void *odd, void *pot,
+                               unsigned long long nvals, cudaStream_t s);
+
+// gpe_upload for fields and potential that are already in this handle's device
+// memory, in host block order and the element type of the handle's precision
+// (not GPE_FP32C).  Returns after the packing has finished.
+gpe_status upload_device_fields(gpe_handle h, int32_t instance, const void *even, const void *odd,
+                                const void *potential);
+
 }  // namespace gpe

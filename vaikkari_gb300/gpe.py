@@ -131,7 +131,8 @@ class _IntegrateResult(C.Structure):
     _fields_ = [("xsize", C.c_uint32), ("ysize", C.c_uint32), ("zsize", C.c_uint32),
                 ("steps_per_iteration", C.c_uint32), ("values", C.c_uint64), ("p0", C.c_double * 3),
                 ("maxpot", C.c_double), ("dt", C.c_double), ("lapfac_dt", C.c_double), ("lapfac0_dt", C.c_double),
-                ("g_dt", C.c_double), ("odd_phase", C.c_double * 2), ("device_ms", C.c_double)]
+                ("g_dt", C.c_double), ("odd_phase", C.c_double * 2), ("device_ms", C.c_double),
+                ("setup_ms", C.c_double)]
 
 
 _lib = None
@@ -214,6 +215,8 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_integrate_setup.restype = st
     lib.gpe_integrate_setup.argtypes = [C.c_void_p, C.POINTER(_IntegrateDesc), C.POINTER(_IntegrateResult),
                                         C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.gpe_integrate_grid.restype = st
+    lib.gpe_integrate_grid.argtypes = [C.POINTER(_IntegrateDesc), C.POINTER(_IntegrateResult)]
     lib.gpe_integrate_in_time.restype = st
     lib.gpe_integrate_in_time.argtypes = [C.c_void_p, C.POINTER(_IntegrateDesc), C.POINTER(_IntegrateResult),
                                           C.POINTER(_Observables), C.c_void_p, C.c_void_p]
@@ -601,12 +604,19 @@ class VortexState:
         out["odd_phase"] = list(r.odd_phase)
         return out
 
+    def grid(self, block_scale, minp, maxp, **kw):
+        """The grid integrateInTime builds (sizes, values, p0), without sampling."""
+        d = self._desc(block_scale, minp, maxp, **kw)
+        r = _IntegrateResult()
+        _check(self.lib.gpe_integrate_grid(C.byref(d), C.byref(r)), "gpe_integrate_grid")
+        return self._res(r)
+
     def setup(self, block_scale, minp, maxp, **kw):
         """integrateInTime's host set-up: (result, even, odd, V) with fields in
         block order, shape (zsize, ysize, xsize, 12, 2)."""
         d = self._desc(block_scale, minp, maxp, **kw)
         r = _IntegrateResult()
-        _check(self.lib.gpe_integrate_setup(self.h, C.byref(d), C.byref(r), None, None, None), "gpe_integrate_setup")
+        _check(self.lib.gpe_integrate_grid(C.byref(d), C.byref(r)), "gpe_integrate_grid")
         shp = (r.zsize, r.ysize, r.xsize, 12)
         even = np.empty(shp + (2,))
         odd = np.empty(shp + (2,))
@@ -621,7 +631,7 @@ class VortexState:
         per iteration, final even, final odd)."""
         d = self._desc(block_scale, minp, maxp, iteration_period, number_of_iterations, **kw)
         r = _IntegrateResult()
-        _check(self.lib.gpe_integrate_setup(self.h, C.byref(d), C.byref(r), None, None, None), "gpe_integrate_setup")
+        _check(self.lib.gpe_integrate_grid(C.byref(d), C.byref(r)), "gpe_integrate_grid")
         shp = (r.zsize, r.ysize, r.xsize, 12, 2)
         even = np.empty(shp)
         odd = np.empty(shp)
