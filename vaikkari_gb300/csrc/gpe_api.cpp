@@ -35,6 +35,24 @@ gpe_status fail(gpe_status s, const std::string &msg)
     return s;
 }
 
+gpe_status exception_status(const char *where) noexcept
+{
+    gpe_status s = GPE_ERR_INTERNAL;
+    const char *what = "unexpected exception";
+    try {
+        throw;
+    } catch (const std::bad_alloc &) {
+        s = GPE_ERR_OUT_OF_MEMORY;
+        what = "host allocation failed";
+    } catch (...) {
+    }
+    try {
+        g_last_error = std::string(where) + ": " + what;
+    } catch (...) {
+    }
+    return s;
+}
+
 gpe_status cuda_fail(cudaError_t e, const char *what)
 {
     g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
@@ -560,7 +578,7 @@ const char *gpe_status_string(gpe_status s)
 
 const char *gpe_last_error(void) { return g_last_error.c_str(); }
 
-gpe_status gpe_lattice_describe(int32_t lattice, gpe_lattice_info *out)
+static gpe_status gpe_lattice_describe_impl(int32_t lattice, gpe_lattice_info *out)
 {
     if (!out) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_lattice_describe: null output");
     if (lattice != GPE_LATTICE_TETRA12 && lattice != GPE_LATTICE_BCC2)
@@ -570,7 +588,12 @@ gpe_status gpe_lattice_describe(int32_t lattice, gpe_lattice_info *out)
     return GPE_OK;
 }
 
-gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
+gpe_status gpe_lattice_describe(int32_t lattice, gpe_lattice_info *out)
+{
+    GPE_GUARD(gpe_lattice_describe_impl(lattice, out));
+}
+
+static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
 {
     if (!cfg || !out) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: null argument");
     *out = nullptr;
@@ -935,7 +958,12 @@ gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
     return GPE_OK;
 }
 
-gpe_status gpe_destroy(gpe_handle h)
+gpe_status gpe_create(const gpe_config *cfg, gpe_handle *out)
+{
+    GPE_GUARD(gpe_create_impl(cfg, out));
+}
+
+static gpe_status gpe_destroy_impl(gpe_handle h)
 {
     if (!h) return GPE_OK;
     cudaError_t e = cudaStreamSynchronize(h->stream);
@@ -944,7 +972,12 @@ gpe_status gpe_destroy(gpe_handle h)
     return GPE_OK;
 }
 
-gpe_status gpe_upload(gpe_handle h, int32_t instance, const void *even, const void *odd, const void *potential)
+gpe_status gpe_destroy(gpe_handle h)
+{
+    GPE_GUARD(gpe_destroy_impl(h));
+}
+
+static gpe_status gpe_upload_impl(gpe_handle h, int32_t instance, const void *even, const void *odd, const void *potential)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -985,7 +1018,12 @@ gpe_status gpe_upload(gpe_handle h, int32_t instance, const void *even, const vo
     return GPE_OK;
 }
 
-gpe_status gpe_download(gpe_handle h, int32_t instance, void *even, void *odd)
+gpe_status gpe_upload(gpe_handle h, int32_t instance, const void *even, const void *odd, const void *potential)
+{
+    GPE_GUARD(gpe_upload_impl(h, instance, even, odd, potential));
+}
+
+static gpe_status gpe_download_impl(gpe_handle h, int32_t instance, void *even, void *odd)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -1009,6 +1047,11 @@ gpe_status gpe_download(gpe_handle h, int32_t instance, void *even, void *odd)
         GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
     }
     return GPE_OK;
+}
+
+gpe_status gpe_download(gpe_handle h, int32_t instance, void *even, void *odd)
+{
+    GPE_GUARD(gpe_download_impl(h, instance, even, odd));
 }
 
 namespace {
@@ -1042,8 +1085,8 @@ gpe_status ensure_xfer(gpe_handle h, size_t n)
 
 }  // namespace
 
-gpe_status gpe_upload_many(gpe_handle h, int32_t count, const int32_t *instances, const void *const *even,
-                           const void *const *odd, const void *const *potential)
+static gpe_status gpe_upload_many_impl(gpe_handle h, int32_t count, const int32_t *instances, const void *const *even,
+                                       const void *const *odd, const void *const *potential)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -1113,8 +1156,14 @@ gpe_status gpe_upload_many(gpe_handle h, int32_t count, const int32_t *instances
     return GPE_OK;
 }
 
-gpe_status gpe_download_many(gpe_handle h, int32_t count, const int32_t *instances, void *const *even,
-                             void *const *odd)
+gpe_status gpe_upload_many(gpe_handle h, int32_t count, const int32_t *instances, const void *const *even,
+                           const void *const *odd, const void *const *potential)
+{
+    GPE_GUARD(gpe_upload_many_impl(h, count, instances, even, odd, potential));
+}
+
+static gpe_status gpe_download_many_impl(gpe_handle h, int32_t count, const int32_t *instances, void *const *even,
+                                         void *const *odd)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -1164,7 +1213,13 @@ gpe_status gpe_download_many(gpe_handle h, int32_t count, const int32_t *instanc
     return GPE_OK;
 }
 
-gpe_status gpe_step(gpe_handle h, int64_t steps)
+gpe_status gpe_download_many(gpe_handle h, int32_t count, const int32_t *instances, void *const *even,
+                             void *const *odd)
+{
+    GPE_GUARD(gpe_download_many_impl(h, count, instances, even, odd));
+}
+
+static gpe_status gpe_step_impl(gpe_handle h, int64_t steps)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -1188,14 +1243,24 @@ gpe_status gpe_step(gpe_handle h, int64_t steps)
     return GPE_OK;
 }
 
-gpe_status gpe_synchronize(gpe_handle h)
+gpe_status gpe_step(gpe_handle h, int64_t steps)
+{
+    GPE_GUARD(gpe_step_impl(h, steps));
+}
+
+static gpe_status gpe_synchronize_impl(gpe_handle h)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
     return sync_and_check(h);
 }
 
-gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out)
+gpe_status gpe_synchronize(gpe_handle h)
+{
+    GPE_GUARD(gpe_synchronize_impl(h));
+}
+
+static gpe_status gpe_observables_get_impl(gpe_handle h, int32_t field, gpe_observables *out)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -1231,8 +1296,13 @@ gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out
     return GPE_OK;
 }
 
-gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64_t *steps_done, int32_t *converged,
-                              double *mu_out)
+gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out)
+{
+    GPE_GUARD(gpe_observables_get_impl(h, field, out));
+}
+
+static gpe_status gpe_imaginary_time_impl(gpe_handle h, int64_t max_steps, double tol, int64_t *steps_done, int32_t *converged,
+                                          double *mu_out)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -1268,7 +1338,13 @@ gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64
     return GPE_OK;
 }
 
-gpe_status gpe_time_steps(gpe_handle h, int64_t steps, float *ms)
+gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64_t *steps_done, int32_t *converged,
+                              double *mu_out)
+{
+    GPE_GUARD(gpe_imaginary_time_impl(h, max_steps, tol, steps_done, converged, mu_out));
+}
+
+static gpe_status gpe_time_steps_impl(gpe_handle h, int64_t steps, float *ms)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -1292,7 +1368,12 @@ gpe_status gpe_time_steps(gpe_handle h, int64_t steps, float *ms)
     return sync_and_check(h);
 }
 
-gpe_status gpe_debug_inject(gpe_handle h, int32_t plane)
+gpe_status gpe_time_steps(gpe_handle h, int64_t steps, float *ms)
+{
+    GPE_GUARD(gpe_time_steps_impl(h, steps, ms));
+}
+
+static gpe_status gpe_debug_inject_impl(gpe_handle h, int32_t plane)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -1304,8 +1385,13 @@ gpe_status gpe_debug_inject(gpe_handle h, int32_t plane)
     return GPE_OK;
 }
 
-gpe_status gpe_volume_map(gpe_handle h, int32_t instance, int32_t field, double unit, int32_t reference_sum,
-                          uint16_t *out)
+gpe_status gpe_debug_inject(gpe_handle h, int32_t plane)
+{
+    GPE_GUARD(gpe_debug_inject_impl(h, plane));
+}
+
+static gpe_status gpe_volume_map_impl(gpe_handle h, int32_t instance, int32_t field, double unit, int32_t reference_sum,
+                                      uint16_t *out)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -1320,8 +1406,14 @@ gpe_status gpe_volume_map(gpe_handle h, int32_t instance, int32_t field, double 
     return sync_and_check(h);
 }
 
-gpe_status gpe_slice_rgb(gpe_handle h, int32_t instance, int32_t field, int32_t z_padded, int32_t slot, double gain,
-                         uint8_t *out)
+gpe_status gpe_volume_map(gpe_handle h, int32_t instance, int32_t field, double unit, int32_t reference_sum,
+                          uint16_t *out)
+{
+    GPE_GUARD(gpe_volume_map_impl(h, instance, field, unit, reference_sum, out));
+}
+
+static gpe_status gpe_slice_rgb_impl(gpe_handle h, int32_t instance, int32_t field, int32_t z_padded, int32_t slot, double gain,
+                                     uint8_t *out)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -1337,7 +1429,13 @@ gpe_status gpe_slice_rgb(gpe_handle h, int32_t instance, int32_t field, int32_t 
     return sync_and_check(h);
 }
 
-gpe_status gpe_link_z(gpe_handle h, int32_t lower, int32_t upper)
+gpe_status gpe_slice_rgb(gpe_handle h, int32_t instance, int32_t field, int32_t z_padded, int32_t slot, double gain,
+                         uint8_t *out)
+{
+    GPE_GUARD(gpe_slice_rgb_impl(h, instance, field, z_padded, slot, gain, out));
+}
+
+static gpe_status gpe_link_z_impl(gpe_handle h, int32_t lower, int32_t upper)
 {
     gpe_status st = check_handle(h);
     if (st != GPE_OK) return st;
@@ -1369,6 +1467,11 @@ gpe_status gpe_link_z(gpe_handle h, int32_t lower, int32_t upper)
     return GPE_OK;
 }
 
+gpe_status gpe_link_z(gpe_handle h, int32_t lower, int32_t upper)
+{
+    GPE_GUARD(gpe_link_z_impl(h, lower, upper));
+}
+
 int32_t gpe_variant_count(void) { return fused_tile_count(); }
 
 int32_t gpe_variant_half_steps(int32_t variant)
@@ -1376,8 +1479,8 @@ int32_t gpe_variant_half_steps(int32_t variant)
     return (variant >= 0 && variant < fused_tile_count()) ? fused_half_steps(variant) : 0;
 }
 
-gpe_status gpe_variant_describe(int32_t variant, int32_t *tile_x, int32_t *tile_y, int32_t *stages,
-                                int32_t *min_blocks)
+static gpe_status gpe_variant_describe_impl(int32_t variant, int32_t *tile_x, int32_t *tile_y, int32_t *stages,
+                                            int32_t *min_blocks)
 {
     if (variant < 0 || variant >= fused_tile_count())
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_variant_describe: no such variant");
@@ -1388,6 +1491,12 @@ gpe_status gpe_variant_describe(int32_t variant, int32_t *tile_x, int32_t *tile_
     if (stages) *stages = stg;
     if (min_blocks) *min_blocks = mb;
     return GPE_OK;
+}
+
+gpe_status gpe_variant_describe(int32_t variant, int32_t *tile_x, int32_t *tile_y, int32_t *stages,
+                                int32_t *min_blocks)
+{
+    GPE_GUARD(gpe_variant_describe_impl(variant, tile_x, tile_y, stages, min_blocks));
 }
 
 int64_t gpe_launch_count(gpe_handle h) { return h ? h->launches : 0; }

@@ -27,6 +27,18 @@ gpe_status build_lattice(gpe_lattice lattice, gpe_lattice_info *info);
 gpe_status fail(gpe_status s, const std::string &msg);
 gpe_status cuda_fail(cudaError_t e, const char *what);
 
+// The status for an exception that reached an entry point, called inside its
+// catch handler: std::bad_alloc becomes GPE_ERR_OUT_OF_MEMORY, anything else
+// GPE_ERR_INTERNAL, with the entry point's name in gpe_last_error().  C callers
+// cannot unwind a C++ exception, so none leaves the library.
+gpe_status exception_status(const char *where) noexcept;
+#define GPE_GUARD(call)                               \
+    try {                                             \
+        return call;                                  \
+    } catch (...) {                                   \
+        return ::gpe::exception_status(__func__);     \
+    }
+
 #define GPE_CUDA_TRY(expr)                                        \
     do {                                                          \
         cudaError_t gpe_e_ = (expr);                              \

@@ -195,9 +195,9 @@ gpe_status scratch_for_current_device(double **out)
 
 using namespace gpe;
 
-extern "C" gpe_status gpe_observables_noalloc(int32_t lattice, int32_t precision, const gpe_instance *inst,
-                                              const void *field, const void *potential, void *stream,
-                                              gpe_observables *out)
+static gpe_status gpe_observables_noalloc_impl(int32_t lattice, int32_t precision, const gpe_instance *inst,
+                                               const void *field, const void *potential, void *stream,
+                                               gpe_observables *out)
 {
     if (!inst || !field || !out) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_observables_noalloc: null argument");
     if (lattice != GPE_LATTICE_TETRA12 && lattice != GPE_LATTICE_BCC2)
@@ -252,4 +252,11 @@ extern "C" gpe_status gpe_observables_noalloc(int32_t lattice, int32_t precision
     out->pad_ = 0;
     if (!out->finite) return fail(GPE_ERR_NOT_FINITE, "gpe_observables_noalloc: NaN or Inf in the field");
     return GPE_OK;
+}
+
+extern "C" gpe_status gpe_observables_noalloc(int32_t lattice, int32_t precision, const gpe_instance *inst,
+                                              const void *field, const void *potential, void *stream,
+                                              gpe_observables *out)
+{
+    GPE_GUARD(gpe_observables_noalloc_impl(lattice, precision, inst, field, potential, stream, out));
 }

@@ -114,8 +114,8 @@ using namespace gpe;
 
 extern "C" {
 
-gpe_status gpe_write_metaimage(const char *path, const uint16_t *vol, uint32_t dx, uint32_t dy, uint32_t dz,
-                               const double *spacing)
+static gpe_status gpe_write_metaimage_impl(const char *path, const uint16_t *vol, uint32_t dx, uint32_t dy, uint32_t dz,
+                                           const double *spacing)
 {
     if (!path || !vol || !spacing || !dx || !dy || !dz)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_write_metaimage: bad arguments");
@@ -148,7 +148,13 @@ gpe_status gpe_write_metaimage(const char *path, const uint16_t *vol, uint32_t d
     return GPE_OK;
 }
 
-gpe_status gpe_write_bmp(const char *path, const uint8_t *rgb, uint32_t width, uint32_t height)
+gpe_status gpe_write_metaimage(const char *path, const uint16_t *vol, uint32_t dx, uint32_t dy, uint32_t dz,
+                               const double *spacing)
+{
+    GPE_GUARD(gpe_write_metaimage_impl(path, vol, dx, dy, dz, spacing));
+}
+
+static gpe_status gpe_write_bmp_impl(const char *path, const uint8_t *rgb, uint32_t width, uint32_t height)
 {
     if (!path || !rgb || !width || !height) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_write_bmp: bad arguments");
     // Picture::save (jukan_koodit/Output/Picture.cpp:81-129): 24-bit, bottom-up
@@ -180,6 +186,11 @@ gpe_status gpe_write_bmp(const char *path, const uint8_t *rgb, uint32_t width, u
     }
     std::fclose(fp);
     return GPE_OK;
+}
+
+gpe_status gpe_write_bmp(const char *path, const uint8_t *rgb, uint32_t width, uint32_t height)
+{
+    GPE_GUARD(gpe_write_bmp_impl(path, rgb, width, height));
 }
 
 }  // extern "C"
