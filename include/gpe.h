@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define GPE_ABI_VERSION 1
+#define GPE_ABI_VERSION 2
 
 typedef enum gpe_status {
     GPE_OK = 0,
@@ -112,6 +112,18 @@ typedef struct gpe_lattice_info {
     int32_t entry[GPE_MAX_SLOTS][GPE_MAX_NEIGHBOURS][5];
 } gpe_lattice_info;
 
+/* The face tables of the reference's multi-GPU program, getLaplacian
+ * (GPUGrossPitaevskii_BCC_multi.cu:73-271): for face f = 4 * slot + k of a
+ * TETRA12 value, the neighbour's block offset (blockDirs), its slot (valueInds)
+ * and the Hodge weight before scaling (hodges).  The update sums a slot's faces
+ * in the reference kernel's order (perms, :314-327). */
+#define GPE_FACES 48
+typedef struct gpe_face_table {
+    int32_t dir[GPE_FACES][3];
+    int32_t slot[GPE_FACES];
+    double hodge[GPE_FACES];
+} gpe_face_table;
+
 /* One condensate. */
 typedef struct gpe_instance {
     int32_t nx, ny, nz;   /* blocks per axis (>= 1)                                     */
@@ -134,6 +146,13 @@ typedef struct gpe_config {
     int32_t tile;           /* fused-kernel tile variant; 0 = autotuned/default   */
     int32_t zchunk;         /* planes per work item of the fused kernel; 0 = auto  */
     int32_t device;         /* CUDA device ordinal                                 */
+    /* TETRA12 and the plain kernel only.  NULL: the update of
+     * GPUGrossPitaevskii_BCC.cu:213, lapfac * sum(psi_f) + (lapfac0 + V + g|psi|^2) psi.
+     * Non-NULL: the Hodge (face) form of GPUGrossPitaevskii_BCC_multi.cu:329-397,
+     * sum_f h_f (psi_f - psi) + (V + g|psi|^2) psi with h_f = -0.5 hodge_f / bs^2 * dt,
+     * bit for bit as that kernel computes it in FP64.  The table must describe the
+     * TETRA12 graph (each value's four faces) with finite weights; it is copied. */
+    const gpe_face_table *faces;
 } gpe_config;
 
 /* Observables of one instance, all in FP64 (Kahan-compensated sums):

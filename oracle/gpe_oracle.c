@@ -145,6 +145,81 @@ void oracle_leapfrog_f32(const oracle_grid *g, float *even, float *odd, const fl
     }
 }
 
+/* The face form of GPUGrossPitaevskii_BCC_multi.cu:329-397 (see gpe_oracle.h). */
+#define FIDX(x, y, z, s) ((((size_t)(z) * (size_t)ny + (size_t)(y)) * (size_t)nx + (size_t)(x)) * 12 + (size_t)(s))
+#define FACES_BODY(T, FMA)                                                                          \
+    int z;                                                                                          \
+    _Pragma("omp parallel for schedule(static) num_threads(oracle_get_threads())")                  \
+    for (z = 0; z < nz; z++) {                                                                      \
+        for (int y = 0; y < ny; y++)                                                                \
+            for (int x = 0; x < nx; x++)                                                            \
+                for (int s = 0; s < 12; s++) {                                                      \
+                    const size_t o = FIDX(x, y, z, s);                                              \
+                    T px = prev[2 * o], py = prev[2 * o + 1];                                       \
+                    if (mode == 1) {                                                                \
+                        px = sigma * px;                                                            \
+                        py = sigma * py;                                                            \
+                    }                                                                               \
+                    T sx = 0, sy = 0;                                                               \
+                    for (int k = 0; k < 4; k++) {                                                   \
+                        const int *e = face + (s * 4 + k) * 4;                                      \
+                        const int xx = x + e[0], yy = y + e[1], zz = z + e[2];                      \
+                        T vx = 0, vy = 0;                                                           \
+                        if (xx >= 0 && xx < nx && yy >= 0 && yy < ny && zz >= 0 && zz < nz) {       \
+                            const size_t q = FIDX(xx, yy, zz, e[3]);                                \
+                            vx = prev[2 * q];                                                       \
+                            vy = prev[2 * q + 1];                                                   \
+                            if (mode == 1) {                                                        \
+                                vx = sigma * vx;                                                    \
+                                vy = sigma * vy;                                                    \
+                            }                                                                       \
+                        }                                                                           \
+                        sx = FMA(h[s * 4 + k], vx - px, sx);                                        \
+                        sy = FMA(h[s * 4 + k], vy - py, sy);                                        \
+                    }                                                                               \
+                    const T cc = FMA(gdt, FMA(px, px, py * py), vdt[o]);                            \
+                    sx = FMA(cc, px, sx);                                                           \
+                    sy = FMA(cc, py, sy);                                                           \
+                    if (mode == 0) {                                                                \
+                        next[2 * o] = next[2 * o] + sy;                                             \
+                        next[2 * o + 1] = next[2 * o + 1] - sx;                                     \
+                    } else {                                                                        \
+                        next[2 * o] = px - sx;                                                      \
+                        next[2 * o + 1] = py - sy;                                                  \
+                    }                                                                               \
+                }                                                                                   \
+    }
+
+void oracle_half_step_faces_f64(int nx, int ny, int nz, const int *face, const double *h, double gdt,
+                                const double *prev, double *next, const double *vdt, int mode, double sigma)
+{
+    FACES_BODY(double, fma)
+}
+
+void oracle_half_step_faces_f32(int nx, int ny, int nz, const int *face, const float *h, float gdt,
+                                const float *prev, float *next, const float *vdt, int mode, float sigma)
+{
+    FACES_BODY(float, fmaf)
+}
+
+void oracle_leapfrog_faces_f64(int nx, int ny, int nz, const int *face, const double *h, double gdt, double *even,
+                               double *odd, const double *vdt, long steps)
+{
+    for (long k = 0; k < steps; k++) {
+        oracle_half_step_faces_f64(nx, ny, nz, face, h, gdt, even, odd, vdt, 0, 1.0);
+        oracle_half_step_faces_f64(nx, ny, nz, face, h, gdt, odd, even, vdt, 0, 1.0);
+    }
+}
+
+void oracle_leapfrog_faces_f32(int nx, int ny, int nz, const int *face, const float *h, float gdt, float *even,
+                               float *odd, const float *vdt, long steps)
+{
+    for (long k = 0; k < steps; k++) {
+        oracle_half_step_faces_f32(nx, ny, nz, face, h, gdt, even, odd, vdt, 0, 1.0f);
+        oracle_half_step_faces_f32(nx, ny, nz, face, h, gdt, odd, even, vdt, 0, 1.0f);
+    }
+}
+
 /* BCC2 in the fused kernel's order (see gpe_oracle.h). */
 #define BCC2_BODY(T, FMA)                                                                           \
     const int nx = g->nx, ny = g->ny, nz = g->nz;                                                  \

@@ -10,7 +10,8 @@
  *   - leapfrog order:  :475-481 (odd <- even, then even <- odd)
  *   - zero padding:    :269-287 (psi = 0 outside the block grid)
  * over a generic neighbour table (the reference's 48-entry table of :90-142, or
- * the 14-edge BCC table); the imaginary-time step and the observables have no
+ * the 14-edge BCC table), and the face form of the multi-GPU program's update
+ * (GPUGrossPitaevskii_BCC_multi.cu:329-397); the imaginary-time step and the observables have no
  * counterpart in the reference and are restated from their definitions.
  *
  * Layout: the reference's block order, index (((z*ny)+y)*nx+x)*slots+s;
@@ -94,6 +95,23 @@ void oracle_observables_f32(const oracle_grid *g, const float *psi, const float 
  * with |mu_k - mu_{k-1}| < tol, or -1.  vol = volume per value. */
 long oracle_imaginary_f64(const oracle_grid *g, double *psi, double *work, const double *vdt, double dt,
                           double gcoef, const double *w, double vol, long steps, double tol, double *mu_hist);
+
+/* The face (Hodge) form of the reference's multi-GPU update
+ * (GPUGrossPitaevskii_BCC_multi.cu:329-397) on a 12-slot grid: per value, over
+ * its four faces in summation order (face[(s*4+k)*4 ..] = dx, dy, dz, slot;
+ * h[s*4+k] = -0.5 * hodge / bs^2 * dt), zero outside the grid,
+ *   sum = fma(h_k, psi_k - psi, sum)            k = 0..3, from sum = 0
+ *   sum = fma(fma(gdt, fma(x, x, y*y), vdt), psi, sum)
+ *   mode 0: next += -i sum;  mode 1: next = psi - sum, psi = sigma * prev.
+ * These are the roundings of that kernel as nvcc compiles it. */
+void oracle_half_step_faces_f64(int nx, int ny, int nz, const int *face, const double *h, double gdt,
+                                const double *prev, double *next, const double *vdt, int mode, double sigma);
+void oracle_half_step_faces_f32(int nx, int ny, int nz, const int *face, const float *h, float gdt,
+                                const float *prev, float *next, const float *vdt, int mode, float sigma);
+void oracle_leapfrog_faces_f64(int nx, int ny, int nz, const int *face, const double *h, double gdt, double *even,
+                               double *odd, const double *vdt, long steps);
+void oracle_leapfrog_faces_f32(int nx, int ny, int nz, const int *face, const float *h, float gdt, float *even,
+                               float *odd, const float *vdt, long steps);
 
 /* Worker threads used by the parallel loops (OpenMP). */
 void oracle_set_threads(int n);

@@ -57,6 +57,11 @@ def load():
     lib.oracle_observables_f32.argtypes = [G, vp, vp, dp, dp, vp, vp]
     lib.oracle_imaginary_f64.argtypes = [G, vp, vp, vp, dp, dp, vp, dp, C.c_long, dp, vp]
     lib.oracle_imaginary_f64.restype = C.c_long
+    ci = C.c_int
+    lib.oracle_half_step_faces_f64.argtypes = [ci, ci, ci, vp, vp, dp, vp, vp, vp, ci, dp]
+    lib.oracle_half_step_faces_f32.argtypes = [ci, ci, ci, vp, vp, C.c_float, vp, vp, vp, ci, C.c_float]
+    lib.oracle_leapfrog_faces_f64.argtypes = [ci, ci, ci, vp, vp, dp, vp, vp, vp, C.c_long]
+    lib.oracle_leapfrog_faces_f32.argtypes = [ci, ci, ci, vp, vp, C.c_float, vp, vp, vp, C.c_long]
     ui, ul = C.c_uint, C.c_long
     lib.oracle_vortex_initial.argtypes = [ui, dp, dp, ui, dp, vp]
     lib.oracle_vortex_resample.argtypes = [vp, ui, ui, dp, dp, dp, vp, ui, ui, dp, dp, dp]
@@ -265,3 +270,52 @@ class Vortex:
     def max_z(self, eps):
         cols = np.nonzero((self.f.reshape(self.rsize, self.zsize) > eps).any(axis=0))[0]
         return int(cols[-1]) * self.zstep if cols.size else 0.0
+
+
+# The face order of the reference's multi-GPU update kernel: position k of slot s
+# takes face 4*s + FACE_PERM[s][k] of its getLaplacian table
+# (GPUGrossPitaevskii_BCC_multi.cu:314-327).
+FACE_PERM = ((3, 2, 0, 1), (2, 0, 1, 3), (1, 0, 2, 3), (1, 0, 2, 3), (2, 0, 1, 3), (3, 1, 0, 2),
+             (0, 1, 2, 3), (0, 1, 2, 3), (3, 1, 0, 2), (2, 3, 0, 1), (2, 3, 0, 1), (3, 2, 0, 1))
+
+
+class Faces:
+    """The face (Hodge) form of GPUGrossPitaevskii_BCC_multi.cu:329-397 on an
+    nx*ny*nz grid of 12-slot blocks.  `table` is the reference's getLaplacian
+    output, 48 rows (dx, dy, dz, slot, hodge) for face f = 4*slot + k; the weights
+    are scaled as integrateInTime does (:483), -0.5 * hodge / bs^2 * dt, and the
+    faces summed in FACE_PERM order."""
+
+    def __init__(self, nx, ny, nz, table, block_scale, dt, g):
+        self.nx, self.ny, self.nz = nx, ny, nz
+        face, h = [], []
+        for s in range(12):
+            for k in range(4):
+                row = table[4 * s + FACE_PERM[s][k]]
+                face.extend(int(v) for v in row[:4])
+                h.append(-0.5 * float(row[4]) / (block_scale * block_scale) * dt)
+        self.face = np.array(face, dtype=np.int32)
+        self.h = np.array(h, dtype=np.float64)
+        self.h32 = self.h.astype(np.float32)
+        self.gdt = g * dt
+
+    def _args(self, dtype):
+        p = lambda a: a.ctypes.data_as(C.c_void_p)
+        if dtype == np.float64:
+            return (self.nx, self.ny, self.nz, p(self.face), p(self.h), self.gdt)
+        return (self.nx, self.ny, self.nz, p(self.face), p(self.h32), float(np.float32(self.gdt)))
+
+    def half_step(self, prev, next_, vdt, mode=0, sigma=1.0):
+        lib = load()
+        p = lambda a: a.ctypes.data_as(C.c_void_p)
+        fn = lib.oracle_half_step_faces_f64 if prev.dtype == np.float64 else lib.oracle_half_step_faces_f32
+        fn(*self._args(prev.dtype), p(prev), p(next_), p(vdt), mode, sigma)
+
+    def leapfrog(self, even, odd, vdt, steps):
+        """In place: `steps` leapfrog steps, odd <- even then even <- odd."""
+        lib = load()
+        for a in (even, odd, vdt):
+            assert a.flags.c_contiguous and a.dtype == even.dtype
+        p = lambda a: a.ctypes.data_as(C.c_void_p)
+        fn = lib.oracle_leapfrog_faces_f64 if even.dtype == np.float64 else lib.oracle_leapfrog_faces_f32
+        fn(*self._args(even.dtype), p(even), p(odd), p(vdt), int(steps))

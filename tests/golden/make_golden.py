@@ -9,6 +9,8 @@ MT19937, compiled from their sources) and records what it prints.
 
 Outputs (committed):
   ref_tables.json        getPositions/getLaplacian (GPUGrossPitaevskii_BCC.cu:73-142)
+  ref_multi_tables.json  the face tables of the multi-GPU program's Hodge-form update
+                         (GPUGrossPitaevskii_BCC_multi.cu:73-271), from oracle/_ref/ref_multi_tables
   ref_mesh_hodge.json    Mesh-library Hodge weights around interior BCC nodes/bodies
   ref_vortex_state.json  state.dat diagnostics, psi/phase samples, Random(54363) stream
   ref_vortex_state2.json the same for state2.dat
@@ -58,6 +60,7 @@ def main():
             f.write("\n")
 
     dump("ref_tables.json", run([exe, "tables"]))
+    dump("ref_multi_tables.json", run([os.path.join(ORACLE, "_ref", "ref_multi_tables")]))
     dump("ref_mesh_hodge.json", run([exe, "mesh"]))
     dump("ref_vortex_state.json", run([exe, "vortex", os.path.join(gp, "state.dat")]))
     dump("ref_vortex_state2.json", run([exe, "vortex", os.path.join(gp, "state2.dat")]))

@@ -1,6 +1,7 @@
-"""Runs the REFERENCE's own update kernel (koodit/GrossPitaevskii/
-GPUGrossPitaevskii_BCC.cu:176-216), compiled unmodified for sm_103a by
-oracle/Makefile into oracle/_ref/ref_bcc.cubin, through the CUDA driver API.
+"""Runs the REFERENCE's own update kernels through the CUDA driver API, compiled
+unmodified for sm_103a by oracle/Makefile: GPUGrossPitaevskii_BCC.cu:176-216
+(oracle/_ref/ref_bcc.cubin) and the Hodge form of GPUGrossPitaevskii_BCC_multi.cu:
+329-397 (oracle/_ref/ref_multi.cubin), both under koodit/GrossPitaevskii.
 
 Test infrastructure: lays out the reference's pitched BlockPsis/BlockPots arrays
 (one padding block on every side, :269-287), builds its int2 neighbour table of
@@ -56,15 +57,18 @@ def _ck(r, what):
 class ReferenceUpdate:
     """The reference kernel on one grid of X*Y*Z blocks (12 values each)."""
 
+    cubin = CUBIN
+    kernel = KERNEL
+
     def __init__(self, X, Y, Z):
         import torch
         torch.cuda.init()
         torch.zeros(1, device="cuda")  # make the primary context current
         drv = _driver()
         self.mod = C.c_void_p()
-        _ck(drv.cuModuleLoad(C.byref(self.mod), CUBIN.encode()), "cuModuleLoad")
+        _ck(drv.cuModuleLoad(C.byref(self.mod), self.cubin.encode()), "cuModuleLoad")
         self.fn = C.c_void_p()
-        _ck(drv.cuModuleGetFunction(C.byref(self.fn), self.mod, KERNEL), "cuModuleGetFunction")
+        _ck(drv.cuModuleGetFunction(C.byref(self.fn), self.mod, self.kernel), "cuModuleGetFunction")
         self.X, self.Y, self.Z = X, Y, Z
         # pitches as cudaMalloc3D would choose them (512-byte aligned rows)
         self.pitch = -(-(X + 2) * BLOCK_PSIS // 512) * 512
@@ -139,5 +143,50 @@ class ReferenceUpdate:
                 args = (C.c_void_p * 7)(*[C.cast(C.pointer(v), C.c_void_p) for v in
                                           (nxt, prv, pot, lap, facs, gg, dims)])
                 _ck(drv.cuLaunchKernel(self.fn, gx, gy, gz, 8, 8, 12, 0, C.c_void_p(stream), args, None),
+                    "cuLaunchKernel")
+        _ck(drv.cuCtxSynchronize(), "cuCtxSynchronize")
+
+
+MULTI_CUBIN = os.path.join(ROOT, "oracle", "_ref", "ref_multi.cubin")
+
+
+def multi_available():
+    return os.path.exists(MULTI_CUBIN)
+
+
+class ReferenceHodgeUpdate(ReferenceUpdate):
+    """The Hodge-form update of the reference's multi-GPU program
+    (koodit/GrossPitaevskii/GPUGrossPitaevskii_BCC_multi.cu:329-397), compiled
+    unmodified for sm_103a by oracle/Makefile into oracle/_ref/ref_multi.cubin,
+    on one GPU: the same pitched arrays, its own face tables (blockDirs,
+    valueInds, hodges) scaled as its integrateInTime does (:476-483), and its
+    launch shape, CTAs of 16 blocks x 12 values along x (:649-658)."""
+
+    cubin = MULTI_CUBIN
+    # update(PitchedPtr, PitchedPtr, PitchedPtr, int3*, int*, double*, double, uint3)
+    kernel = b"_Z6update10PitchedPtrS_S_P4int3PiPdd5uint3"
+
+    def step_faces(self, steps, table, block_scale, dt, g, stream=0):
+        """`steps` leapfrog steps (odd <- even, then even <- odd, :816-881) with the
+        48 face rows (dx, dy, dz, slot, hodge)."""
+        import torch
+        dirs = np.array([r[:3] for r in table], dtype=np.int32)
+        slots = np.array([r[3] for r in table], dtype=np.int32)
+        hodges = np.array([-0.5 * float(r[4]) / (block_scale * block_scale) * dt for r in table], dtype=np.float64)
+        d_dirs = torch.from_numpy(dirs.reshape(-1)).cuda()
+        d_slots = torch.from_numpy(slots).cuda()
+        d_h = torch.from_numpy(hodges).cuda()
+        drv = _driver()
+        pot = PitchedPtr(self.pot.data_ptr() + self.pslice + self.ppitch + BLOCK_POTS, self.ppitch, self.pslice)
+        pd, ps, ph = C.c_void_p(d_dirs.data_ptr()), C.c_void_p(d_slots.data_ptr()), C.c_void_p(d_h.data_ptr())
+        gg = C.c_double(g * dt)
+        dims = UInt3(self.X, self.Y, self.Z)
+        ev, od = self._psi_ptr(self.even), self._psi_ptr(self.odd)
+        gx, gy, gz = (self.X + 15) // 16, self.Y, self.Z
+        for _ in range(steps):
+            for nxt, prv in ((od, ev), (ev, od)):
+                args = (C.c_void_p * 8)(*[C.cast(C.pointer(v), C.c_void_p) for v in
+                                          (nxt, prv, pot, pd, ps, ph, gg, dims)])
+                _ck(drv.cuLaunchKernel(self.fn, gx, gy, gz, 16 * 12, 1, 1, 0, C.c_void_p(stream), args, None),
                     "cuLaunchKernel")
         _ck(drv.cuCtxSynchronize(), "cuCtxSynchronize")

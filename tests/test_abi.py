@@ -38,7 +38,7 @@ def test_every_declared_symbol_is_exported():
 
 def test_version_and_status_strings():
     lib = gpe.load_library()
-    assert lib.gpe_abi_version() == 1
+    assert lib.gpe_abi_version() == 2
     for s in Status:
         assert lib.gpe_status_string(int(s))
     assert lib.gpe_status_string(999) == b"unknown status"

@@ -125,6 +125,7 @@ struct gpe_handle_ {
     std::vector<std::pair<int, int>> zlinks;  // (lower, upper): upper continues lower along +z
     uint32_t slots_from_above = 0, slots_from_below = 0;  // slots the stencil reads at z+1 / z-1
     bool imag_ready = false;
+    bool faces = false;  // TETRA12 stepped in the face form (gpe_config.faces)
     double tol = 0.0;
     long long launches = 0;
 };
@@ -139,6 +140,43 @@ void *field_buf(const gpe_handle_ *h, int f)
     if (h->cfg.mode == GPE_IMAGINARY_TIME) return h->buf[f == 0 ? h->parity : 1 - h->parity];
     return h->buf[(h->two_step ? 2 * h->parity : 0) + f];
 }
+
+// Summation order of a value's four faces in the face form: position k of slot
+// s takes face 4 s + kFacePerm[s][k] of the caller's table.  This is the order
+// of the reference's multi-GPU kernel (perms, GPUGrossPitaevskii_BCC_multi.cu:
+// 314-327), so that the FP64 sums round as its do.
+const int kFacePerm[12][4] = {{3, 2, 0, 1}, {2, 0, 1, 3}, {1, 0, 2, 3}, {1, 0, 2, 3}, {2, 0, 1, 3}, {3, 1, 0, 2},
+                              {0, 1, 2, 3}, {0, 1, 2, 3}, {3, 1, 0, 2}, {2, 3, 0, 1}, {2, 3, 0, 1}, {3, 2, 0, 1}};
+
+// A face table must describe the TETRA12 graph: the four faces of each slot are
+// its four lattice neighbours in some order, each with a finite weight.
+gpe_status check_face_table(const gpe_face_table &t)
+{
+    gpe_lattice_info lat;
+    gpe_status st = build_lattice(GPE_LATTICE_TETRA12, &lat);
+    if (st != GPE_OK) return fail(st, "gpe_create: lattice construction failed its self-check");
+    for (int s = 0; s < 12; s++) {
+        bool used[4] = {false, false, false, false};
+        for (int k = 0; k < 4; k++) {
+            const int f = 4 * s + k;
+            if (!std::isfinite(t.hodge[f]))
+                return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: face " + std::to_string(f) + " has a non-finite weight");
+            int match = -1;
+            for (int j = 0; j < 4 && match < 0; j++)
+                if (!used[j] && lat.entry[s][j][0] == t.dir[f][0] && lat.entry[s][j][1] == t.dir[f][1] &&
+                    lat.entry[s][j][2] == t.dir[f][2] && lat.entry[s][j][3] == t.slot[f])
+                    match = j;
+            if (match < 0)
+                return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: face " + std::to_string(f) +
+                                                          " is not a TETRA12 neighbour of slot " + std::to_string(s));
+            used[match] = true;
+        }
+    }
+    return GPE_OK;
+}
+
+// The lattice code the step kernels run.
+int step_lattice(const gpe_handle_ *h) { return h->faces ? kStepTetra12Faces : h->cfg.lattice; }
 
 gpe_status check_handle(gpe_handle h)
 {
@@ -224,7 +262,7 @@ gpe_status enqueue_halo(gpe_handle h, int field)
 PlainBatchLaunch plain_batch(gpe_handle h, int mode, void *prev, void *next)
 {
     PlainBatchLaunch l{};
-    l.lattice = h->cfg.lattice;
+    l.lattice = step_lattice(h);
     l.precision = h->cfg.precision;
     l.mode = mode;
     l.potential = h->cfg.potential;
@@ -302,7 +340,7 @@ gpe_status enqueue_step_real(gpe_handle h)
         } else {
             for (int i = 0; i < h->cfg.num_instances; i++) {
                 StepLaunch l{};
-                l.lattice = h->cfg.lattice;
+                l.lattice = step_lattice(h);
                 l.precision = h->cfg.precision;
                 l.mode = GPE_REAL_TIME;
                 l.potential = h->cfg.potential;
@@ -395,7 +433,7 @@ gpe_status enqueue_step_imag(gpe_handle h, int parity)
     }
     for (int i = 0; i < h->cfg.num_instances; i++) {
         StepLaunch l{};
-        l.lattice = h->cfg.lattice;
+        l.lattice = step_lattice(h);
         l.precision = h->cfg.precision;
         l.mode = GPE_IMAGINARY_TIME;
         l.potential = h->cfg.potential;
@@ -611,6 +649,13 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: need at least one instance");
     if (cfg->kernel == GPE_KERNEL_FUSED && cfg->lattice != GPE_LATTICE_BCC2)
         return fail(GPE_ERR_UNSUPPORTED, "gpe_create: the fused kernel is built for the BCC2 lattice only");
+    if (cfg->faces) {
+        if (cfg->lattice != GPE_LATTICE_TETRA12 || cfg->kernel == GPE_KERNEL_FUSED || cfg->precision == GPE_FP32C)
+            return fail(GPE_ERR_UNSUPPORTED, "gpe_create: a face table needs the TETRA12 lattice, the plain kernel "
+                                             "and GPE_FP64 or GPE_FP32");
+        gpe_status fst = check_face_table(*cfg->faces);
+        if (fst != GPE_OK) return fst;
+    }
     if (cfg->precision == GPE_FP32C &&
         (cfg->lattice != GPE_LATTICE_BCC2 || cfg->kernel == GPE_KERNEL_PLAIN || cfg->mode != GPE_REAL_TIME ||
          (cfg->tile > 0 && cfg->tile < fused_tile_count() && fused_half_steps(cfg->tile) != 1)))
@@ -635,6 +680,8 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
     h->cfg = *cfg;
     h->inst.assign(cfg->instances, cfg->instances + cfg->num_instances);
     h->cfg.instances = h->inst.data();
+    h->faces = cfg->faces != nullptr;
+    h->cfg.faces = nullptr;  // copied into the per-instance data below
     gpe_status st = build_lattice(gpe_lattice(cfg->lattice), &h->lat);
     if (st != GPE_OK) {
         free_handle(h);
@@ -711,6 +758,18 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
         d.dt = in.dt;
         d.g = in.g;
         d.vol = h->lat.cell_volume * in.block_scale * in.block_scale * in.block_scale;
+        if (cfg->faces) {
+            const gpe_face_table &t = *cfg->faces;
+            d.face = 1;
+            for (int sl = 0; sl < 12; sl++)
+                for (int k = 0; k < 4; k++) {
+                    const int f = 4 * sl + kFacePerm[sl][k], j = 4 * sl + k;
+                    d.fe[j] = (t.dir[f][0] + 1) | ((t.dir[f][1] + 1) << 2) | ((t.dir[f][2] + 1) << 4) | (t.slot[f] << 6);
+                    d.hf[j] = -0.5 * t.hodge[f] / s2 * in.dt;  // GPUGrossPitaevskii_BCC_multi.cu:483
+                    d.hf32[j] = float(d.hf[j]);
+                    d.hw[j] = t.hodge[f] / s2;
+                }
+        }
         h->idev_host.push_back(d);
         max_vals = std::max(max_vals, size_t(in.nx) * in.ny * in.nz * h->ns);
         // the output kernels stage a padded block grid of uint16 / a padded plane of RGB

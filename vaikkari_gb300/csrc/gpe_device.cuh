@@ -33,6 +33,15 @@ struct InstDev {
     double dt, g;
     double vol;        // volume per value
     double w[2];       // unscaled class weights
+    // TETRA12 in the face form (gpe_config.faces), per slot s its faces k = 0..3 in
+    // summation order at [4 s + k]: packed neighbour (as the lattice tables), the
+    // update weight -0.5 hodge / bs^2 * dt in FP64 and FP32, and hodge / bs^2 for
+    // the kinetic energy.
+    int face;
+    int fe[48];
+    float hf32[48];
+    double hf[48];
+    double hw[48];
 };
 
 struct WorkItem {

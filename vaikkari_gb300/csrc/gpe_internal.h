@@ -48,9 +48,13 @@ gpe_status exception_status(const char *where) noexcept;
 // Uploads a lattice's neighbour table to constant memory (gpe_plain.cu).
 cudaError_t set_plain_table(const gpe_lattice_info &info);
 
+// The step kernels' lattice code for a TETRA12 handle created with a face
+// table (gpe_config.faces): the same layout and graph, the face-form update.
+constexpr int kStepTetra12Faces = 2;
+
 // Kernel launchers; each returns cudaGetLastError() after the launch.
 struct StepLaunch {
-    int lattice;          // gpe_lattice
+    int lattice;          // gpe_lattice, or kStepTetra12Faces
     int precision;        // gpe_precision
     int mode;             // gpe_time_mode
     int potential;        // gpe_potential_kind

@@ -30,6 +30,62 @@ template <> struct Lat<GPE_LATTICE_BCC2> {
     static constexpr int NS = 2, NB = 14, NC = 2, N0 = 8;
     __device__ static int entry(int k) { return c_tab_bcc2[k]; }
 };
+// TETRA12 stepped in the face form: the faces and weights come from InstDev.
+template <> struct Lat<kStepTetra12Faces> {
+    static constexpr int NS = 12, NB = 4, NC = 1, N0 = 4;
+    __device__ static int entry(int k) { return c_tab_tetra12[k]; }
+};
+
+// The face (Hodge) form of the reference's multi-GPU update
+// (GPUGrossPitaevskii_BCC_multi.cu:329-397) for planes z0..z1-1 of one value:
+//   sum = h_k (psi_k - psi) added over the four faces in summation order,
+//   sum += (V dt + g dt |psi|^2) psi,   next += -i sum   (real time)
+//                                       next = psi - sum (imaginary time).
+// Each rounding is that kernel's as nvcc compiles it (fused multiply-add on by
+// default): every h_k (psi_k - psi) is added with one fma, |psi|^2 is
+// fma(x, x, y*y), V dt + g dt |psi|^2 one fma, and c psi is added with one fma.
+template <typename T, int MODE, int POT>
+__device__ __forceinline__ void face_values(const InstDev &d, const typename Cplx<T>::type *__restrict__ prev,
+                                            typename Cplx<T>::type *__restrict__ next, const T *__restrict__ vpot,
+                                            T sig, int s, int x, int y, int z0, int z1)
+{
+    using T2 = typename Cplx<T>::type;
+    const long long base0 = field_index(d, s, x, y, 0);
+    long long off[4];
+    T h[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int e = d.fe[4 * s + k];
+        const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
+        off[k] = field_index(d, sl, x + dx, y + dy, dz) - base0;
+        if constexpr (sizeof(T) == 8) h[k] = d.hf[4 * s + k];
+        else h[k] = d.hf32[4 * s + k];
+    }
+    const T gdt = T(d.gdt);
+    const long long voff = d.vbase - d.base;
+    for (int z = z0; z < z1; z++) {
+        const long long self = base0 + (long long)z * d.zstride;
+        T2 p = prev[self];
+        if (MODE == 1) p = c_scale<T>(sig, p);
+        T sx = T(0), sy = T(0);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            T2 v = prev[self + off[k]];
+            if (MODE == 1) v = c_scale<T>(sig, v);
+            sx = d_fma(h[k], d_sub(v.x, p.x), sx);
+            sy = d_fma(h[k], d_sub(v.y, p.y), sy);
+        }
+        T vdt;
+        if (POT == GPE_POTENTIAL_ARRAY) vdt = vpot[self + voff];
+        else vdt = trap_vdt<T>(vpot, d, s, x, y, z);
+        const T c = d_fma(gdt, d_fma(p.x, p.x, d_mul(p.y, p.y)), vdt);
+        sx = d_fma(c, p.x, sx);
+        sy = d_fma(c, p.y, sy);
+        T2 n;
+        if (MODE == 0) n = next[self];
+        next[self] = integrate<T, MODE>(n, p, sx, sy);
+    }
+}
 
 cudaError_t set_plain_table(const gpe_lattice_info &info)
 {
@@ -68,6 +124,10 @@ __device__ __forceinline__ void plain_step_body(const InstDev *__restrict__ inst
     const int z0 = (bz / L::NS) * zc;
     if (x >= d.nx || y >= d.ny) return;
     const T sig = (MODE == 1) ? T(imag[ii].sigma) : T(1);
+    if constexpr (LAT == kStepTetra12Faces) {
+        face_values<T, MODE, POT>(d, prev, next, vpot, sig, s, x, y, z0, min(z0 + zc, d.nz));
+        return;
+    }
     if constexpr (sizeof(T) == 8) {
         // FP64 is bound by the FP64 pipe: one value per thread (zc == 1), indices
         // formed directly, fewest registers and most values in flight.
@@ -197,7 +257,7 @@ static cudaError_t plain_dispatch_mode(const StepLaunch &l, cudaStream_t st)
     dim3 grid((l.nx + 31) / 32, (l.ny + 7) / 8, ((l.nz + zc - 1) / zc) * Lat<LAT>::NS);
     const T2 *prev = (const T2 *)l.prev;
     T2 *next = (T2 *)l.next;
-    const T *v = (const T *)(l.potential == GPE_POTENTIAL_ARRAY ? l.vbase : l.vpot);
+    const T *v = (const T *)(l.potential == GPE_POTENTIAL_ARRAY && LAT != kStepTetra12Faces ? l.vbase : l.vpot);
     if (l.mode == GPE_REAL_TIME) {
         if (l.potential == GPE_POTENTIAL_ARRAY)
             plain_step_kernel<T, LAT, 0, 0><<<grid, block, 0, st>>>(l.inst, l.inst_index, prev, next, v, l.imag, zc);
@@ -254,7 +314,7 @@ static cudaError_t plain_batch_mode(const PlainBatchLaunch &l, cudaStream_t st)
     using T2 = typename Cplx<T>::type;
     const T2 *prev = (const T2 *)l.prev;
     T2 *next = (T2 *)l.next;
-    const T *v = (const T *)(l.potential == GPE_POTENTIAL_ARRAY ? l.vbase : l.vpot);
+    const T *v = (const T *)(l.potential == GPE_POTENTIAL_ARRAY && LAT != kStepTetra12Faces ? l.vbase : l.vpot);
 #define GPE_PB(MODE, POT) \
     plain_step_batch_kernel<T, LAT, MODE, POT><<<l.blocks, dim3(32, 8, 1), 0, st>>>(l.inst, l.blk_inst, l.blk_begin, \
                                                                                  l.zcs, prev, next, v, l.imag)
@@ -269,20 +329,28 @@ cudaError_t launch_plain_step_batch(const PlainBatchLaunch &l, cudaStream_t s)
 {
     if (l.precision == GPE_FP64) {
         if (l.lattice == GPE_LATTICE_TETRA12) return plain_batch_mode<double, GPE_LATTICE_TETRA12>(l, s);
-        return plain_batch_mode<double, GPE_LATTICE_BCC2>(l, s);
+        if (l.lattice == kStepTetra12Faces) return plain_batch_mode<double, kStepTetra12Faces>(l, s);
+        if (l.lattice == GPE_LATTICE_BCC2) return plain_batch_mode<double, GPE_LATTICE_BCC2>(l, s);
+        return cudaErrorInvalidValue;
     }
     if (l.lattice == GPE_LATTICE_TETRA12) return plain_batch_mode<float, GPE_LATTICE_TETRA12>(l, s);
-    return plain_batch_mode<float, GPE_LATTICE_BCC2>(l, s);
+    if (l.lattice == kStepTetra12Faces) return plain_batch_mode<float, kStepTetra12Faces>(l, s);
+    if (l.lattice == GPE_LATTICE_BCC2) return plain_batch_mode<float, GPE_LATTICE_BCC2>(l, s);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_plain_step(const StepLaunch &l, cudaStream_t s)
 {
     if (l.precision == GPE_FP64) {
         if (l.lattice == GPE_LATTICE_TETRA12) return plain_dispatch_mode<double, GPE_LATTICE_TETRA12>(l, s);
-        return plain_dispatch_mode<double, GPE_LATTICE_BCC2>(l, s);
+        if (l.lattice == kStepTetra12Faces) return plain_dispatch_mode<double, kStepTetra12Faces>(l, s);
+        if (l.lattice == GPE_LATTICE_BCC2) return plain_dispatch_mode<double, GPE_LATTICE_BCC2>(l, s);
+        return cudaErrorInvalidValue;
     }
     if (l.lattice == GPE_LATTICE_TETRA12) return plain_dispatch_mode<float, GPE_LATTICE_TETRA12>(l, s);
-    return plain_dispatch_mode<float, GPE_LATTICE_BCC2>(l, s);
+    if (l.lattice == kStepTetra12Faces) return plain_dispatch_mode<float, kStepTetra12Faces>(l, s);
+    if (l.lattice == GPE_LATTICE_BCC2) return plain_dispatch_mode<float, GPE_LATTICE_BCC2>(l, s);
+    return cudaErrorInvalidValue;
 }
 
 // ---------------------------------------------------------------------------
@@ -341,6 +409,23 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
         r /= d.ny;
         const int s = int(r % L::NS);
         const int z = int(r / L::NS);
+        const long long self = field_index(d, s, x, y, z);
+        const T2 pt = f[self];
+        const double px = double(pt.x), py = double(pt.y);
+        double lx, ly;
+        if (LAT == GPE_LATTICE_TETRA12 && d.face) {
+            // face form: Lap psi = sum_k (hodge_k / bs^2) (psi_k - psi)
+            lx = 0.0;
+            ly = 0.0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int e = d.fe[4 * s + k];
+                const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
+                const T2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
+                lx += d.hw[4 * s + k] * (double(q.x) - px);
+                ly += d.hw[4 * s + k] * (double(q.y) - py);
+            }
+        } else {
         double sx[2] = {0.0, 0.0}, sy[2] = {0.0, 0.0};
         if constexpr (sizeof(T) == 4) {
             // FP32 values: each class sum kept as an unevaluated float pair
@@ -379,11 +464,9 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
                 sy[c] += double(q.y);
             }
         }
-        const long long self = field_index(d, s, x, y, z);
-        const T2 pt = f[self];
-        const double px = double(pt.x), py = double(pt.y);
-        const double lx = d.w[0] * sx[0] + d.w[1] * sx[1] - wsum * px;
-        const double ly = d.w[0] * sy[0] + d.w[1] * sy[1] - wsum * py;
+        lx = d.w[0] * sx[0] + d.w[1] * sx[1] - wsum * px;
+        ly = d.w[0] * sy[0] + d.w[1] * sy[1] - wsum * py;
+        }
         double vdt;
         if (POT == GPE_POTENTIAL_ARRAY) vdt = double(vpot[self - d.base + d.vbase]);
         else vdt = double(trap_vdt<T>(vpot, d, s, x, y, z));

@@ -94,7 +94,36 @@ class _Config(C.Structure):
         ("lattice", C.c_int32), ("precision", C.c_int32), ("mode", C.c_int32), ("kernel", C.c_int32),
         ("potential", C.c_int32), ("num_instances", C.c_int32), ("instances", C.POINTER(_Instance)),
         ("graph_steps", C.c_int32), ("tile", C.c_int32), ("zchunk", C.c_int32), ("device", C.c_int32),
+        ("faces", C.c_void_p),
     ]
+
+
+class _FaceTable(C.Structure):
+    _fields_ = [("dir", (C.c_int32 * 3) * 48), ("slot", C.c_int32 * 48), ("hodge", C.c_double * 48)]
+
+
+def face_table(rows):
+    """gpe_face_table from 48 rows (dx, dy, dz, slot, hodge), face f = 4*slot + k:
+    the reference multi-GPU program's getLaplacian output
+    (GPUGrossPitaevskii_BCC_multi.cu:73-271)."""
+    rows = list(rows)
+    if len(rows) != 48:
+        raise ValueError("a face table has 48 rows (dx, dy, dz, slot, hodge)")
+    t = _FaceTable()
+    for f, r in enumerate(rows):
+        for a in range(3):
+            t.dir[f][a] = int(r[a])
+        t.slot[f] = int(r[3])
+        t.hodge[f] = float(r[4])
+    return t
+
+
+def default_face_table(weight=None):
+    """The TETRA12 graph as a face table in this library's neighbour order, every
+    weight the lattice's Hodge weight (1.5) unless `weight` is given."""
+    info = lattice_info(Lattice.TETRA12)
+    w = float(info["class_weight"][0]) if weight is None else float(weight)
+    return [(*(int(v) for v in info["entry"][s][k][:4]), w) for s in range(12) for k in range(4)]
 
 
 class _Observables(C.Structure):
@@ -348,7 +377,9 @@ class Stepper:
 
     def __init__(self, instances: List[Instance], lattice=Lattice.BCC2, precision=Precision.FP32,
                  mode=Mode.REAL, kernel=Kernel.AUTO, potential=Potential.ARRAY, graph_steps=0, tile=0,
-                 zchunk=0, device=0):
+                 zchunk=0, device=0, faces=None):
+        """faces: TETRA12 only, 48 rows (dx, dy, dz, slot, hodge) of the reference
+        multi-GPU program's table; the update then takes its face (Hodge) form."""
         self.lib = load_library()
         self.instances = list(instances)
         self.lattice, self.precision, self.mode = Lattice(lattice), Precision(precision), Mode(mode)
@@ -362,6 +393,10 @@ class Stepper:
         cfg.num_instances = len(self.instances)
         cfg.instances = C.cast(self._carr, C.POINTER(_Instance))
         cfg.graph_steps, cfg.tile, cfg.zchunk, cfg.device = graph_steps, tile, zchunk, device
+        self.faces = None if faces is None else [tuple(r) for r in faces]
+        if faces is not None:
+            self._faces = face_table(faces)
+            cfg.faces = C.cast(C.pointer(self._faces), C.c_void_p)
         h = C.c_void_p()
         _check(self.lib.gpe_create(C.byref(cfg), C.byref(h)), "gpe_create")
         self.h = h
