@@ -880,9 +880,9 @@ def run_tetra12(args):
     discretisation, 12 values per block), plain kernel, array potential, one
     instance of 87 x 87 x 302 blocks (main()'s grid at block scale 0.06997) with
     seeded random fields.  FP64 (bit-identical to the reference's kernel) and FP32,
-    each timed with CUDA events over --steps steps (best of three) after a graph
-    of 100 steps."""
-    from vaikkari_gb300.gpe import Instance, Kernel, Lattice, Potential, Precision, Stepper
+    then both again in the face (Hodge) form of the multi-GPU program, each timed
+    with CUDA events over --steps steps (best of three) after a graph of 100 steps."""
+    from vaikkari_gb300.gpe import Instance, Kernel, Lattice, Potential, Precision, Stepper, default_face_table
     rng = np.random.default_rng(5)
     inst = Instance(87, 87, 302, 0.06997, 1e-4, 100.0, origin=(-3.0, -3.0, -10.0))
     shp = (inst.nz, inst.ny, inst.nx, 12)
@@ -891,9 +891,11 @@ def run_tetra12(args):
     V = rng.uniform(0.0, 10.0, shp)
     vals = inst.nx * inst.ny * inst.nz * 12
     rates = {}
-    for name, prec in (("fp64", Precision.FP64), ("fp32", Precision.FP32)):
+    faces = default_face_table()
+    for name, prec, fc in (("fp64", Precision.FP64, None), ("fp32", Precision.FP32, None),
+                           ("fp64_faces", Precision.FP64, faces), ("fp32_faces", Precision.FP32, faces)):
         st = Stepper([inst], lattice=Lattice.TETRA12, precision=prec, kernel=Kernel.PLAIN,
-                     potential=Potential.ARRAY, graph_steps=100)
+                     potential=Potential.ARRAY, graph_steps=100, faces=fc)
         st.upload(0, e, o, V)
         st.time_steps(100)
         ms = min(st.time_steps(args.steps) for _ in range(3))
@@ -904,6 +906,8 @@ def run_tetra12(args):
             "config": {"workload": "tetra12_plain_production_grid", "values": vals, "blocks": [87, 87, 302],
                        "lattice": "TETRA12", "kernel": "plain", "potential": "array"},
             "fp32": rates["fp32"],
+            "faces": {"fp64": rates["fp64_faces"], "fp32": rates["fp32_faces"],
+                      "form": "Hodge (face) form of GPUGrossPitaevskii_BCC_multi.cu:329-397, weights 1.5"},
             "note": "FP64 performs the reference kernel's rounded operations and equals its results bit for "
                     "bit; the per-value constant L0 + V*dt is added once per potential upload, leaving 15 FP64 "
                     "operations per value and half-step; the bound is this GPU's FP64 rate"}

@@ -175,3 +175,30 @@ def test_faces_observables_and_imaginary_time():
         st.close()
     assert abs(out[0][0] - out[1][0]) <= 1e-11 * abs(out[1][0])
     assert rel_l2(out[0][1], out[1][1]) < 1e-11
+
+
+@pytest.mark.gpu
+def test_faces_slabs_equal_undivided_grid():
+    """The multi-GPU program splits one grid into z-slabs; the face form over 3
+    linked slabs of one batch equals the undivided grid bit for bit."""
+    from vaikkari_gb300.slabs import SlabStepper
+    dims = (12, 10, 11)
+    inst = Instance(*dims, 0.25, 1e-3, 40.0, origin=(-5.0, -3.0, -3.5))
+    kw = dict(lattice=Lattice.TETRA12, precision=Precision.FP64, kernel=Kernel.PLAIN, potential=Potential.ARRAY,
+              faces=TABLE)
+    shp = (dims[2], dims[1], dims[0], 12)
+    e, o = _fields(shp, 31, np.float64)
+    V = np.random.default_rng(32).uniform(0, 3, shp)
+    whole = Stepper([inst], **kw)
+    whole.upload(0, e, o, V)
+    whole.step(130)
+    we, wo = whole.download(0)
+    whole.close()
+    sl = SlabStepper(inst, 3, **kw)
+    sl.upload(e, o, V)
+    sl.step(130)
+    se, so = sl.download()
+    sl.close()
+    assert np.abs(we).max() > 0.05
+    np.testing.assert_array_equal(se, we)
+    np.testing.assert_array_equal(so, wo)
