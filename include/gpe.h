@@ -424,7 +424,9 @@ gpe_status gpe_write_bmp(const char *path, const uint8_t *rgb, uint32_t width, u
  * All calls share that array: calls that overlap on a GPU race and must be
  * serialised by the caller.  The first call on a device looks the array up and
  * should come before any stream capture.  It allocates nothing when it
- * succeeds; a failure records its message for gpe_last_error() as every call does. */
+ * succeeds; a failure records its message for gpe_last_error() as every call does.
+ * The kinetic term uses the lattice's own weights (a face table's weights are
+ * not known here). */
 #define GPE_NOALLOC_MAX_ROWS 8192
 #define GPE_NOALLOC_VALUES_PER_ROW 2048
 gpe_status gpe_observables_noalloc(int32_t lattice, int32_t precision, const gpe_instance *inst,
