@@ -115,3 +115,64 @@ def test_batched_transfer_bindings_check_arrays_first():
         st.download_many([1], outs=[(np.empty(shp0 + (2,), np.float32), None)])              # wrong shape
     with pytest.raises(ValueError):
         st.download_many([0], outs=[(np.empty(shp0 + (2,), np.float32)[..., ::-1], None)])   # not contiguous
+
+
+_C_CLIENT = r"""
+#include "gpe.h"
+#include <stdio.h>
+
+int main(void)
+{
+    gpe_integrate_desc d = {0};
+    d.block_scale = 0.5;
+    for (int k = 0; k < 3; k++) { d.minp[k] = -2.0; d.maxp[k] = 2.0; }
+    gpe_integrate_result r;
+    if (gpe_integrate_grid(&d, &r) != GPE_OK) return 1;
+    gpe_lattice_info info;
+    if (gpe_lattice_describe(GPE_LATTICE_TETRA12, &info) != GPE_OK) return 2;
+    gpe_face_table faces;
+    for (int s = 0; s < 12; s++)
+        for (int k = 0; k < 4; k++) {
+            const int f = 4 * s + k;
+            for (int a = 0; a < 3; a++) faces.dir[f][a] = info.entry[s][k][a];
+            faces.slot[f] = info.entry[s][k][3];
+            faces.hodge[f] = 1.5;
+        }
+    gpe_instance inst = {0};
+    inst.nx = inst.ny = inst.nz = 4;
+    inst.block_scale = 0.5;
+    inst.dt = 1e-3;
+    inst.g = 1.0;
+    gpe_config cfg = {0};
+    cfg.lattice = GPE_LATTICE_TETRA12;
+    cfg.precision = GPE_FP64;
+    cfg.kernel = GPE_KERNEL_PLAIN;
+    cfg.num_instances = 1;
+    cfg.instances = &inst;
+    cfg.faces = &faces;
+    gpe_handle h = 0;
+    gpe_status s = gpe_create(&cfg, &h);
+    printf("%d %u %u %u %llu\n", (int)s, r.xsize, r.ysize, r.zsize, (unsigned long long)r.values);
+    if (s == GPE_OK) gpe_destroy(h);
+    return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("lang", ["c", "c++"])
+def test_header_builds_and_links_as_c_and_cpp(tmp_path, lang):
+    """include/gpe.h is plain C and C++: a client that fills a face table and
+    asks for the solver call's grid compiles, links against the library and runs
+    (gpe_create answers with a status; without a GPU that is GPE_ERR_CUDA)."""
+    gpe.load_library()
+    src = tmp_path / ("client.c" if lang == "c" else "client.cpp")
+    src.write_text(_C_CLIENT)
+    exe = tmp_path / "client"
+    libdir = os.path.dirname(gpe.LIB_PATH)
+    cc = ["gcc", "-std=c11"] if lang == "c" else ["g++", "-std=c++17"]
+    subprocess.run(cc + ["-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                         "-L", libdir, "-lvaikkari_gpe", f"-Wl,-rpath,{libdir}"], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    status, xs, ys, zs, values = (int(v) for v in out)
+    assert status in (Status.OK, Status.CUDA)
+    assert xs == ys == zs == int(4.0 / (0.5 * np.sqrt(8.0))) + 1 and values == 12 * xs * ys * zs
