@@ -456,46 +456,46 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
                 ly += d.hw[4 * s + k] * (double(q.y) - py);
             }
         } else {
-        double sx[2] = {0.0, 0.0}, sy[2] = {0.0, 0.0};
-        if constexpr (sizeof(T) == 4) {
-            // FP32 values: each class sum kept as an unevaluated float pair
-            // (hi + lo, error-free two-sums, lo accumulated in FP32) and
-            // converted once, so the FP64 pipe (slow on this GPU) sees a few
-            // operations per value instead of a conversion and an add per
-            // neighbour.  Agrees with FP64 summation to about 1e-14.
-            float hx[2] = {0.f, 0.f}, lx_[2] = {0.f, 0.f}, hy[2] = {0.f, 0.f}, ly_[2] = {0.f, 0.f};
+            double sx[2] = {0.0, 0.0}, sy[2] = {0.0, 0.0};
+            if constexpr (sizeof(T) == 4) {
+                // FP32 values: each class sum kept as an unevaluated float pair
+                // (hi + lo, error-free two-sums, lo accumulated in FP32) and
+                // converted once, so the FP64 pipe (slow on this GPU) sees a few
+                // operations per value instead of a conversion and an add per
+                // neighbour.  Agrees with FP64 summation to about 1e-14.
+                float hx[2] = {0.f, 0.f}, lx_[2] = {0.f, 0.f}, hy[2] = {0.f, 0.f}, ly_[2] = {0.f, 0.f};
 #pragma unroll
-            for (int k = 0; k < L::NB; k++) {
-                const int e = L::entry(s * L::NB + k);
-                const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
-                const T2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
-                const int c = (k < L::N0) ? 0 : 1;
-                float t = __fadd_rn(hx[c], q.x), bb = __fsub_rn(t, hx[c]);
-                lx_[c] = __fadd_rn(lx_[c], __fadd_rn(__fsub_rn(hx[c], __fsub_rn(t, bb)), __fsub_rn(q.x, bb)));
-                hx[c] = t;
-                t = __fadd_rn(hy[c], q.y);
-                bb = __fsub_rn(t, hy[c]);
-                ly_[c] = __fadd_rn(ly_[c], __fadd_rn(__fsub_rn(hy[c], __fsub_rn(t, bb)), __fsub_rn(q.y, bb)));
-                hy[c] = t;
-            }
+                for (int k = 0; k < L::NB; k++) {
+                    const int e = L::entry(s * L::NB + k);
+                    const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
+                    const T2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
+                    const int c = (k < L::N0) ? 0 : 1;
+                    float t = __fadd_rn(hx[c], q.x), bb = __fsub_rn(t, hx[c]);
+                    lx_[c] = __fadd_rn(lx_[c], __fadd_rn(__fsub_rn(hx[c], __fsub_rn(t, bb)), __fsub_rn(q.x, bb)));
+                    hx[c] = t;
+                    t = __fadd_rn(hy[c], q.y);
+                    bb = __fsub_rn(t, hy[c]);
+                    ly_[c] = __fadd_rn(ly_[c], __fadd_rn(__fsub_rn(hy[c], __fsub_rn(t, bb)), __fsub_rn(q.y, bb)));
+                    hy[c] = t;
+                }
 #pragma unroll
-            for (int c = 0; c < L::NC; c++) {
-                sx[c] = double(hx[c]) + double(lx_[c]);
-                sy[c] = double(hy[c]) + double(ly_[c]);
-            }
-        } else {
+                for (int c = 0; c < L::NC; c++) {
+                    sx[c] = double(hx[c]) + double(lx_[c]);
+                    sy[c] = double(hy[c]) + double(ly_[c]);
+                }
+            } else {
 #pragma unroll
-            for (int k = 0; k < L::NB; k++) {
-                const int e = L::entry(s * L::NB + k);
-                const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
-                const T2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
-                const int c = (k < L::N0) ? 0 : 1;
-                sx[c] += double(q.x);
-                sy[c] += double(q.y);
+                for (int k = 0; k < L::NB; k++) {
+                    const int e = L::entry(s * L::NB + k);
+                    const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
+                    const T2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
+                    const int c = (k < L::N0) ? 0 : 1;
+                    sx[c] += double(q.x);
+                    sy[c] += double(q.y);
+                }
             }
-        }
-        lx = d.w[0] * sx[0] + d.w[1] * sx[1] - wsum * px;
-        ly = d.w[0] * sy[0] + d.w[1] * sy[1] - wsum * py;
+            lx = d.w[0] * sx[0] + d.w[1] * sx[1] - wsum * px;
+            ly = d.w[0] * sy[0] + d.w[1] * sy[1] - wsum * py;
         }
         double vdt;
         if (POT == GPE_POTENTIAL_ARRAY) vdt = double(vpot[self - d.base + d.vbase]);
