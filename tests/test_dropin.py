@@ -67,6 +67,27 @@ def test_integrate_grid_equals_setup():
     assert grid["maxpot"] == 0.0 and grid["steps_per_iteration"] == 0
 
 
+def test_integrate_calls_refuse_bad_arguments():
+    """The solver call and the grid query check their arguments before any GPU
+    work: a non-positive block scale, a domain that does not fit, a precision the
+    solver call does not take."""
+    from vaikkari_gb300.gpe import GpeError, Status
+    ref = golden("ref_setup_small.json")
+    st = _state()
+    with pytest.raises(GpeError) as e:
+        st.grid(0.0, ref["minp"], ref["maxp"])
+    assert e.value.status == Status.INVALID_ARGUMENT
+    with pytest.raises(GpeError) as e:
+        st.grid(ref["block_scale"], ref["maxp"], ref["minp"])          # max below min
+    assert e.value.status == Status.INVALID_ARGUMENT
+    with pytest.raises(GpeError) as e:
+        st.integrate_in_time(ref["block_scale"], ref["minp"], ref["maxp"], 1.0, 0, precision=Precision.FP32C)
+    assert e.value.status == Status.INVALID_ARGUMENT
+    with pytest.raises(GpeError) as e:
+        st.integrate_in_time(ref["block_scale"], ref["minp"], ref["maxp"], 0.0, 1)
+    assert e.value.status == Status.INVALID_ARGUMENT
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", [Precision.FP64, Precision.FP32])
 def test_integrate_setup_on_gpu_equals_reference(prec):
