@@ -57,7 +57,17 @@ def _slab_worker(rank, world, port, out):
     import oracle.oracle as orc
     dist.init_process_group("gloo", rank=rank, world_size=world)
     steps = 7
-    for lattice_name, dims in (("BCC2", (5, 4, 9)), ("TETRA12", (3, 3, 7))):
+    import json
+    with open(os.path.join(here, "golden", "ref_multi_tables.json")) as fh:
+        table = [tuple(r) for r in json.load(fh)["faces"]]
+
+    def make_grid(name, info, nx, ny, nz):
+        if name == "FACES":   # the multi-GPU program's face form, its own table
+            return orc.Faces(nx, ny, nz, table, 0.3, 1e-3, 50.0)
+        return orc.Grid(nx, ny, nz, info["entry"], info["class_weight"], 0.3, 1e-3, 50.0)
+
+    for name, dims in (("BCC2", (5, 4, 9)), ("TETRA12", (3, 3, 7)), ("FACES", (3, 3, 7))):
+        lattice_name = "TETRA12" if name == "FACES" else name
         info, e, o, v = _case(lattice_name, dims, 11)
         nx, ny, nz = dims
         counts = split_z(nz, world)
@@ -70,7 +80,7 @@ def _slab_worker(rank, world, port, out):
             return g
         fields = [ext(e), ext(o)]
         vext = ext(v)
-        grid = orc.Grid(nx, ny, n + 2, info["entry"], info["class_weight"], 0.3, 1e-3, 50.0)
+        grid = make_grid(name, info, nx, ny, n + 2)
 
         def exchange(f):
             # send my boundary planes, receive the neighbours' into my ghosts
@@ -98,12 +108,11 @@ def _slab_worker(rank, world, port, out):
         gathered = [None] * world
         dist.all_gather_object(gathered, mine)
         if rank == 0:
-            ref = orc.Grid(nx, ny, nz, info["entry"], info["class_weight"], 0.3, 1e-3, 50.0)
+            ref = make_grid(name, info, nx, ny, nz)
             ref.leapfrog(e, o, v, steps)
             got_e = np.concatenate([g[0] for g in gathered])
             got_o = np.concatenate([g[1] for g in gathered])
-            out[lattice_name] = (bool(np.array_equal(got_e, e)), bool(np.array_equal(got_o, o)),
-                                 float(np.abs(e).max()))
+            out[name] = (bool(np.array_equal(got_e, e)), bool(np.array_equal(got_o, o)), float(np.abs(e).max()))
     dist.barrier()
     dist.destroy_process_group()
 
@@ -114,7 +123,7 @@ def test_slab_halo_exchange_on_cpu_ranks_is_exact():
         out = m.dict()
         mp.start_processes(_slab_worker, args=(2, port, out), nprocs=2, join=True, start_method="spawn")
         res = dict(out)
-    for name in ("BCC2", "TETRA12"):
+    for name in ("BCC2", "TETRA12", "FACES"):
         same_e, same_o, scale = res[name]
         assert scale > 0.1          # the state did not decay to nothing
         assert same_e and same_o, name
