@@ -1,20 +1,22 @@
 """Helpers shared by the parity tests: oracle grids and potential arrays that
-mirror what the library feeds its kernels."""
+mirror what the library feeds its kernels.  The stencil tables, volumes and
+value positions come from the oracle's own copy of the reference's tables
+(oracle/lattice.py, read from tests/golden), never from the library under test."""
 import numpy as np
 
 import oracle.oracle as orc
-from vaikkari_gb300.gpe import Potential, Precision, value_positions
+from oracle.lattice import tables
+from vaikkari_gb300.gpe import Potential, Precision
 
 
 def grid_for(stepper, i):
     inst = stepper.instances[i]
-    info = stepper.info
-    return orc.Grid(inst.nx, inst.ny, inst.nz, info["entry"], info["class_weight"], inst.block_scale, inst.dt,
-                    inst.g)
+    t = tables(stepper.lattice)
+    return orc.Grid(inst.nx, inst.ny, inst.nz, t["entry"], t["class_weight"], inst.block_scale, inst.dt, inst.g)
 
 
 def vol_for(stepper, i):
-    return stepper.info["cell_volume"] * stepper.instances[i].block_scale ** 3
+    return tables(stepper.lattice)["cell_volume"] * stepper.instances[i].block_scale ** 3
 
 
 def vdt_for(stepper, i, V=None):
@@ -25,8 +27,8 @@ def vdt_for(stepper, i, V=None):
     T = np.float64 if stepper.precision == Precision.FP64 else np.float32
     if stepper.potential == Potential.ARRAY:
         return np.ascontiguousarray((np.asarray(V, dtype=T).astype(np.float64) * inst.dt).astype(T))
-    info = stepper.info
-    bw, pos = info["block_width"], info["position"]
+    t = tables(stepper.lattice)
+    bw, pos = t["block_width"], t["position"]
     n = (inst.nx, inst.ny, inst.nz)
     tabs = []
     for axis in range(3):

@@ -56,8 +56,9 @@ def test_split_join_keeps_32_bits():
 
 def _gaussian_case(n=16, g=2000.0, dt=1e-4):
     from vaikkari_gb300 import workloads
-    from vaikkari_gb300.gpe import lattice_info, value_positions
-    info = lattice_info(Lattice.BCC2)
+    from oracle.lattice import tables
+    from vaikkari_gb300.gpe import value_positions
+    info = tables(Lattice.BCC2)
     inst = workloads.bcc2_instance(n, dt, g, trap=(1.0, 2.0, 0.7))
     rng = np.random.default_rng(4)
     psi = workloads.gaussian_state(inst, info, rng, 1e-3)

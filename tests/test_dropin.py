@@ -135,10 +135,11 @@ def test_integrate_in_time_matches_reference_kernel():
         re, ro = rk.download()
         np.testing.assert_array_equal(even, re)
         np.testing.assert_array_equal(odd, ro)
-    # the oracle, with the geometry-derived table as the library uses it
+    # the oracle, with the reference's own table (tests/golden)
     import oracle.oracle as orc
-    from vaikkari_gb300.gpe import Lattice, lattice_info
-    info = lattice_info(Lattice.TETRA12)
+    from oracle.lattice import tables
+    from vaikkari_gb300.gpe import Lattice
+    info = tables(Lattice.TETRA12)
     g = orc.Grid(X, Y, Z, info["entry"], info["class_weight"], ref["block_scale"], res["dt"],
                  _state().describe()["g"])
     e, o = np.ascontiguousarray(even0), np.ascontiguousarray(odd0)

@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 import oracle.oracle as orc
+from oracle.lattice import tables
 from conftest import golden
 from helpers import random_state, rel_l2, vdt_for
 from vaikkari_gb300.gpe import (GpeError, Instance, Kernel, Lattice, Mode, Potential, Precision, Stepper,
@@ -68,7 +69,7 @@ def test_face_oracle_equals_lattice_form_to_rounding():
     """With every weight 1.5 the face form is the lattice form of
     GPUGrossPitaevskii_BCC.cu:213 rearranged: after 20 steps the two oracles
     agree to rounding."""
-    info = lattice_info(Lattice.TETRA12)
+    info = tables(Lattice.TETRA12)
     nx, ny, nz, bs, dt, g = 6, 5, 4, 0.35, 1e-3, 60.0
     e, o = _fields((nz, ny, nx, 12), 3, np.float64)
     V = np.random.default_rng(4).uniform(0, 2, (nz, ny, nx, 12))

@@ -128,3 +128,22 @@ def test_vortex_fixture_header_consistent():
     assert v["block_scale"] == pytest.approx(0.0699674, abs=5e-8)
     assert v["maxr"] == pytest.approx(8.53991, abs=5e-6)
     assert v["maxz"] == pytest.approx(29.79, abs=1e-12)
+
+
+@pytest.mark.parametrize("lattice", [Lattice.TETRA12, Lattice.BCC2])
+def test_library_tables_equal_the_oracles(lattice):
+    """The oracle builds its grids from its own copy of the reference's tables
+    (oracle/lattice.py, from tests/golden), not from the library.  The library's
+    tables must equal those: the same neighbours in the same summation order, the
+    same weight doubles and the same value positions bit for bit (the trap
+    potential is formed from them).  The TETRA12 tetrahedron volume is derived
+    from the geometry and agrees with the reference's sqrt(32/9) to 2 ulp; it only
+    scales the observables."""
+    from oracle.lattice import tables
+    ours, ref = lattice_info(lattice), tables(lattice)
+    assert (ours["slots"], ours["neighbours"], ours["classes"]) == (ref["slots"], ref["neighbours"], ref["classes"])
+    np.testing.assert_array_equal(np.asarray(ours["entry"]), ref["entry"])
+    assert list(ours["class_weight"]) == list(ref["class_weight"])
+    assert ours["block_width"] == ref["block_width"]
+    np.testing.assert_array_equal(np.asarray(ours["position"]), ref["position"])
+    assert ours["cell_volume"] == pytest.approx(ref["cell_volume"], rel=1e-15, abs=0)

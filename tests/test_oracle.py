@@ -8,12 +8,13 @@ import pytest
 import oracle.oracle as orc
 from conftest import golden
 from helpers import interleave, random_state, rel_l2
-from vaikkari_gb300.gpe import Instance, Lattice, lattice_info, value_positions
+from oracle.lattice import tables
+from vaikkari_gb300.gpe import Instance, Lattice, value_positions
 from vaikkari_gb300 import workloads
 
 
 def _grid(lattice, dims, bs=0.3, dt=1e-3, g=50.0, entry=None):
-    info = lattice_info(lattice)
+    info = tables(lattice)
     nx, ny, nz = dims
     return orc.Grid(nx, ny, nz, info["entry"] if entry is None else entry, info["class_weight"], bs, dt, g)
 
@@ -56,7 +57,7 @@ def test_fp32_scheme_accuracy_small():
     """FP32 against FP64 of the same scheme on a Gaussian condensate (16^3 cells,
     300 steps): relative L2 well under 1e-5."""
     c = workloads.config1(n=16)
-    info = lattice_info(Lattice.BCC2)
+    info = tables(Lattice.BCC2)
     inst = c.inst
     g = _grid(Lattice.BCC2, (16, 16, 16), bs=inst.block_scale, dt=inst.dt, g=inst.g)
     vdt64 = np.ascontiguousarray(c.V * inst.dt)
@@ -80,7 +81,7 @@ def test_imaginary_time_harmonic_ground_state():
     mu ~ 3/2 (discretisation error O(a^2))."""
     n, L = 16, 5.0
     a = 2 * L / n
-    info = lattice_info(Lattice.BCC2)
+    info = tables(Lattice.BCC2)
     inst = Instance(n, n, n, a, 5e-3, 0.0, origin=(-L, -L, -L))
     g = _grid(Lattice.BCC2, (n, n, n), bs=a, dt=5e-3, g=0.0)
     rng = np.random.default_rng(3)
@@ -97,7 +98,7 @@ def test_leapfrog_conserves_norm_approximately():
     """The staggered leapfrog conserves the norm up to O(dt) oscillations."""
     c = workloads.config1(n=12)
     inst = c.inst
-    info = lattice_info(Lattice.BCC2)
+    info = tables(Lattice.BCC2)
     g = _grid(Lattice.BCC2, (12, 12, 12), bs=inst.block_scale, dt=inst.dt, g=inst.g)
     vdt = np.ascontiguousarray(c.V * inst.dt)
     vol = info["cell_volume"] * inst.block_scale ** 3

@@ -38,8 +38,9 @@ def _free_port():
 
 
 def _case(lattice_name, dims, seed):
-    from vaikkari_gb300.gpe import Lattice, lattice_info
-    info = lattice_info(Lattice[lattice_name])
+    from oracle.lattice import tables
+    from vaikkari_gb300.gpe import Lattice
+    info = tables(Lattice[lattice_name])
     nx, ny, nz = dims
     shp = (nz, ny, nx, info["slots"])
     e = interleave(random_state(shp, seed, 0.3), np.float64)

@@ -232,8 +232,12 @@ gpe_status build_tetra12(gpe_lattice_info *info)
     info->block_width = std::sqrt(8.0);
     // tetrahedron volume: vol units of (sqrt(8)/8)^3 block_scale^3
     info->cell_volume = vol * std::pow(std::sqrt(8.0) / 8.0, 3);
+    // position = (eighths of the block) * block edge / 8, rounded as the reference
+    // rounds it: (1/sqrt(8)) * eighths (GPUGrossPitaevskii_BCC.cu:75-88), so the
+    // doubles equal its getPositions output
+    const double inv_sqrt8 = 1.0 / std::sqrt(8.0);
     for (int s = 0; s < 12; s++)
-        for (int k = 0; k < 3; k++) info->position[s][k] = order[s][k] * std::sqrt(8.0) / 8.0;
+        for (int k = 0; k < 3; k++) info->position[s][k] = inv_sqrt8 * double(order[s][k]);
     finish(info, tab);
     // Summation order of the four neighbours: the order in which the reference's
     // getLaplacian lists them (GPUGrossPitaevskii_BCC.cu:90-142), which its kernel

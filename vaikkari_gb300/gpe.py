@@ -17,18 +17,14 @@ from __future__ import annotations
 import ctypes as C
 import enum
 import os
-from dataclasses import dataclass, field
-from typing import List, Optional, Sequence
+from typing import List, Optional
 
 import numpy as np
 
+from .instance import Instance, Lattice, value_positions  # noqa: F401  (re-exported)
+
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libvaikkari_gpe.so")
-
-
-class Lattice(enum.IntEnum):
-    TETRA12 = 0  # reference discretisation: 12 circumcentre values per block, 4 faces
-    BCC2 = 1     # 2 lattice-point values per block, 14 Hodge-weighted edges
 
 
 class Precision(enum.IntEnum):
@@ -333,43 +329,6 @@ def write_bmp(path: str, rgb: np.ndarray) -> None:
     rgb = np.ascontiguousarray(rgb, dtype=np.uint8)
     _check(lib.gpe_write_bmp(path.encode(), rgb.ctypes.data_as(C.c_void_p), rgb.shape[1], rgb.shape[0]),
            "gpe_write_bmp")
-
-
-@dataclass
-class Instance:
-    """One condensate: nx*ny*nz blocks of the lattice; see include/gpe.h."""
-    nx: int
-    ny: int
-    nz: int
-    block_scale: float
-    dt: float
-    g: float
-    origin: Sequence[float] = (0.0, 0.0, 0.0)
-    trap: Sequence[float] = (1.0, 1.0, 1.0)
-
-    def c(self) -> _Instance:
-        s = _Instance()
-        s.nx, s.ny, s.nz = self.nx, self.ny, self.nz
-        s.block_scale, s.dt, s.g = self.block_scale, self.dt, self.g
-        for k in range(3):
-            s.origin[k] = self.origin[k]
-            s.trap[k] = self.trap[k]
-        return s
-
-
-def value_positions(inst: Instance, info: dict) -> np.ndarray:
-    """Positions of every value of an instance, shape (nz, ny, nx, slots, 3), in
-    the reference's block order (GPUGrossPitaevskii_BCC.cu:258)."""
-    bw = info["block_width"]
-    i = np.arange(inst.nx)[None, None, :, None]
-    j = np.arange(inst.ny)[None, :, None, None]
-    k = np.arange(inst.nz)[:, None, None, None]
-    pos = info["position"]
-    out = np.empty((inst.nz, inst.ny, inst.nx, info["slots"], 3))
-    out[..., 0] = inst.origin[0] + inst.block_scale * (i * bw + pos[None, None, None, :, 0])
-    out[..., 1] = inst.origin[1] + inst.block_scale * (j * bw + pos[None, None, None, :, 1])
-    out[..., 2] = inst.origin[2] + inst.block_scale * (k * bw + pos[None, None, None, :, 2])
-    return out
 
 
 class Stepper:

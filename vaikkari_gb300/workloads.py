@@ -18,7 +18,13 @@ in the reference's TETRA12 lattice uses block_scale = a / sqrt(8).
 The leapfrog's second field is the first rotated by half a step of the
 chemical potential, odd = even * exp(+i mu dt / 2), as the reference does with
 VortexState::getPhase(-dt/2) (GPUGrossPitaevskii_BCC.cu:325,342); mu is the
-discrete chemical potential of the initial field computed by the library.
+discrete chemical potential of the initial field.
+
+Every builder takes the lattice's geometry (block width, value positions, cell
+volume: the dict gpe.lattice_info returns) as `geometry`; by default it asks the
+library.  This module imports no native code itself, so a caller that must not
+load the library (the CPU baseline) can pass the oracle's tables instead and
+get the same seeded condensates.
 """
 from __future__ import annotations
 
@@ -28,7 +34,7 @@ from typing import List, Sequence, Optional
 
 import numpy as np
 
-from .gpe import Instance, Lattice, value_positions, lattice_info
+from .instance import Instance, Lattice, value_positions
 
 L_HALF = 8.0
 
@@ -38,6 +44,13 @@ class Condensate:
     inst: Instance
     psi: np.ndarray          # complex128, (nz, ny, nx, slots)
     V: Optional[np.ndarray]  # float64 potential per value (None when the trap form is used)
+
+
+def _geom(lattice: Lattice, geometry: Optional[dict]) -> dict:
+    if geometry is not None:
+        return geometry
+    from .gpe import lattice_info
+    return lattice_info(lattice)
 
 
 def bcc2_instance(n: int, dt: float, g: float, trap=(1.0, 1.0, 1.0)) -> Instance:
@@ -90,8 +103,8 @@ def thomas_fermi(inst: Instance, info: dict, V: np.ndarray) -> np.ndarray:
     return normalise(psi, vol)
 
 
-def config1(lattice: Lattice = Lattice.BCC2, n: int = 32) -> Condensate:
-    info = lattice_info(lattice)
+def config1(lattice: Lattice = Lattice.BCC2, geometry: Optional[dict] = None, n: int = 32) -> Condensate:
+    info = _geom(lattice, geometry)
     mk = bcc2_instance if lattice == Lattice.BCC2 else tetra12_instance
     inst = mk(n, dt=1e-4, g=500.0)
     rng = np.random.default_rng(0)
@@ -100,8 +113,8 @@ def config1(lattice: Lattice = Lattice.BCC2, n: int = 32) -> Condensate:
     return Condensate(inst, psi, V)
 
 
-def config2(lattice: Lattice = Lattice.BCC2, n: int = 128) -> Condensate:
-    info = lattice_info(lattice)
+def config2(lattice: Lattice = Lattice.BCC2, geometry: Optional[dict] = None, n: int = 128) -> Condensate:
+    info = _geom(lattice, geometry)
     mk = bcc2_instance if lattice == Lattice.BCC2 else tetra12_instance
     inst = mk(n, dt=5e-4, g=2000.0, trap=(1.0, 1.0, 4.0))
     rng = np.random.default_rng(1)
@@ -111,8 +124,8 @@ def config2(lattice: Lattice = Lattice.BCC2, n: int = 128) -> Condensate:
     return Condensate(inst, psi, V)
 
 
-def config3(lattice: Lattice = Lattice.BCC2, n: int = 192) -> Condensate:
-    info = lattice_info(lattice)
+def config3(lattice: Lattice = Lattice.BCC2, geometry: Optional[dict] = None, n: int = 192) -> Condensate:
+    info = _geom(lattice, geometry)
     mk = bcc2_instance if lattice == Lattice.BCC2 else tetra12_instance
     inst = mk(n, dt=5e-5, g=3000.0)
     p = value_positions(inst, info)
@@ -128,11 +141,11 @@ def config3(lattice: Lattice = Lattice.BCC2, n: int = 192) -> Condensate:
 
 
 def config4(lattice: Lattice = Lattice.BCC2, count: int = 64, sizes=(24, 32, 48, 64, 96),
-            dt: float = 1e-4, shard: int = 0) -> List[Condensate]:
+            dt: float = 1e-4, shard: int = 0, geometry: Optional[dict] = None) -> List[Condensate]:
     """The 64-condensate batch (seed 2).  shard > 0 gives another batch of the
     same sizes with its own g, traps and noise: one rank's part of a job of
     64 x ranks condensates, as heavy as shard 0."""
-    info = lattice_info(lattice)
+    info = _geom(lattice, geometry)
     mk = bcc2_instance if lattice == Lattice.BCC2 else tetra12_instance
     rng = np.random.default_rng(2)
     ns = rng.choice(np.asarray(sizes), size=count)
@@ -148,8 +161,8 @@ def config4(lattice: Lattice = Lattice.BCC2, count: int = 64, sizes=(24, 32, 48,
     return out
 
 
-def config5(lattice: Lattice = Lattice.BCC2, n: int = 512) -> Condensate:
-    info = lattice_info(lattice)
+def config5(lattice: Lattice = Lattice.BCC2, geometry: Optional[dict] = None, n: int = 512) -> Condensate:
+    info = _geom(lattice, geometry)
     mk = bcc2_instance if lattice == Lattice.BCC2 else tetra12_instance
     inst = mk(n, dt=2e-5, g=1e4)
     p = value_positions(inst, info)
