@@ -35,6 +35,7 @@ METRIC = "vertex-updates/s"
 BYTES_PER_VERTEX_STEP = 48  # FP32, trap potential in-kernel: 2 half-steps x (read prev 8 B + RMW next 16 B)
 BYTES_PER_VERTEX_STEP_COMP = 64  # FP32C: plus the next field's bf16x2 residual, read and written (2 x 8 B)
 L2_BYTES = 129e6
+HEADLINE_WORKLOAD = "batch64_bcc2_trap_realtime"
 
 
 def _peaks():
@@ -46,22 +47,48 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _profile_traffic(name="fused_bcc2_batch64.md"):
-    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+def _profile_traffic(name):
+    """DRAM bytes per launch of a kernel from a committed ncu summary under
+    profiles/, with the kernel variant the capture ran (lines
+    `traffic_bytes_per_launch_full_batch:` and `traffic_variant:`)."""
     p = os.path.join(ROOT, "profiles", name)
+    out = {"bytes": None, "variant": None, "source": f"profiles/{name}"}
     if not os.path.exists(p):
-        return None
+        return out
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch_full_batch:"):
-            try:
-                return float(line.split(":", 1)[1].strip())
-            except ValueError:
-                return None
-    return None
+        key, _, val = line.partition(":")
+        try:
+            if key == "traffic_bytes_per_launch_full_batch":
+                out["bytes"] = float(val.strip())
+            elif key == "traffic_variant":
+                out["variant"] = int(val.strip())
+        except ValueError:
+            pass
+    return out
+
+
+def roofline_block(verts, bytes_per_vertex_launch, per_launch_s, kernel, profile, variant):
+    """Roofline of the dominant kernel: achieved = algorithmic bytes per launch
+    / average launch duration (CUDA events); traffic from the ncu summary of the
+    same kernel variant on this workload (null if the profiled variant differs)."""
+    peak, peak_kind = _peaks()
+    achieved = verts * bytes_per_vertex_launch / per_launch_s / 1e9
+    prof = _profile_traffic(profile)
+    same = prof["variant"] == variant
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": prof["bytes"] if same else None,
+            "traffic_source": (f"ncu capture summarised in {prof['source']} (variant {prof['variant']}, "
+                               f"full batch, one launch)" if same else
+                               f"none for variant {variant}: {prof['source']} holds variant {prof['variant']}"),
+            "algorithmic_bytes_per_vertex_step": 2 * bytes_per_vertex_launch,
+            "algorithmic_bytes_per_launch": verts * bytes_per_vertex_launch,
+            "peak_source": f"{peak_kind} hbm_gbs (of {peak_kind})", "kernel": kernel}
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle sampling during the timed region."""
+    """nvidia-smi clock/throttle sampling (every 100 ms) around the run; the
+    summary covers the samples taken inside the timed region (between
+    start_region() and end_region())."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -69,8 +96,9 @@ class ClockSampler:
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
-        self.samples = []
+        self.samples = []  # (perf_counter, fields)
         self.proc = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
@@ -87,7 +115,19 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) >= 9:
-                self.samples.append(parts)
+                self.samples.append((time.perf_counter(), parts))
+
+    def wait_first(self, timeout=10.0):
+        """Waits (bounded) until nvidia-smi has printed its first sample."""
+        end = time.perf_counter() + timeout
+        while self.proc and not self.samples and time.perf_counter() < end and self.proc.poll() is None:
+            time.sleep(0.02)
+
+    def start_region(self):
+        self.t0 = time.perf_counter()
+
+    def end_region(self):
+        self.t1 = time.perf_counter()
 
     def __exit__(self, *a):
         if self.proc:
@@ -98,14 +138,21 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        t0 = self.t0 if self.t0 is not None else -math.inf
+        t1 = self.t1 if self.t1 is not None else math.inf
+        inside = [p for t, p in self.samples if t0 <= t <= t1]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0,
+                    "samples_total": len(self.samples)}
+        num = lambda v: v.replace(".", "").isdigit()
+        sm = [float(p[1]) for p in inside if num(p[1])]
+        mx = [float(p[2]) for p in inside if num(p[2])]
+        pw = [float(p[3]) for p in inside if num(p[3])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[5 + k].lower() == "active"})
+        reasons = sorted({names[k] for p in inside for k in range(4) if p[5 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "power_w_median": statistics.median(pw) if pw else None, "reasons": reasons,
+                "samples": len(inside), "region_s": (t1 - t0) if self.t0 is not None else None}
 
 
 def _dist():
@@ -183,32 +230,53 @@ def prepare_fields(stepper, conds, precision_dtype):
     return evens, odds
 
 
-def cpu_sample(conds, evens64, odds64, budget_s, threads, lattice=None):
+def _oracle_grid(inst, lattice=1):
+    """An oracle grid and dt*V (FP64, trap form) for one condensate, from the
+    oracle's own copy of the reference's stencil tables (oracle/lattice.py);
+    nothing of the library is loaded."""
+    import oracle.oracle as orc
+    from oracle.lattice import harmonic, tables, value_positions
+    t = tables(lattice)
+    g = orc.Grid(inst.nx, inst.ny, inst.nz, t["entry"], t["class_weight"], inst.block_scale, inst.dt, inst.g)
+    pos = value_positions(inst.nx, inst.ny, inst.nz, inst.block_scale, inst.origin, lattice)
+    return g, np.ascontiguousarray(harmonic(pos, inst.trap) * inst.dt)
+
+
+def loaded_native_libraries():
+    """Shared objects under this repository mapped into this process (from
+    /proc/self/maps; empty where that file does not exist)."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if len(line.split()) >= 6 else ""
+                if path.startswith(ROOT) and ".so" in os.path.basename(path):
+                    out.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(out)
+
+
+def cpu_sample(conds, evens64, odds64, budget_s, threads, lattice=1):
     """Oracle FP64 leapfrog (the reference's update restated in C, all threads)
     over the batch, as many whole steps as fit the time budget (>= 1)."""
     import oracle.oracle as orc
-    from vaikkari_gb300.gpe import Lattice, lattice_info
-    lattice = Lattice.BCC2 if lattice is None else lattice
-    info = lattice_info(lattice)
+    from oracle.lattice import tables
     orc.set_threads(threads)
     grids, vdts, es, os_ = [], [], [], []
     for c, e, o in zip(conds, evens64, odds64):
-        inst = c.inst
-        g = orc.Grid(inst.nx, inst.ny, inst.nz, info["entry"], info["class_weight"], inst.block_scale, inst.dt,
-                     inst.g)
-        from vaikkari_gb300.gpe import value_positions
-        from vaikkari_gb300.workloads import harmonic
-        vdt = np.ascontiguousarray(harmonic(value_positions(inst, info), inst.trap) * inst.dt)
+        g, vdt = _oracle_grid(c.inst, lattice)
         grids.append(g)
         vdts.append(vdt)
         es.append(e.copy())
         os_.append(o.copy())
-    verts = sum(c.inst.nx * c.inst.ny * c.inst.nz * info["slots"] for c in conds)
+    slots = tables(lattice)["slots"]
+    verts = sum(c.inst.nx * c.inst.ny * c.inst.nz * slots for c in conds)
     t0 = time.perf_counter()
     steps = 0
     while True:
         for g, e, o, v in zip(grids, es, os_, vdts):
-            if lattice == Lattice.BCC2:
+            if int(lattice) == 1:
                 g.leapfrog_bcc2_fast(e, o, v, 1)
             else:
                 g.leapfrog(e, o, v, 1)
@@ -223,18 +291,13 @@ def cpu_single_core(conds, budget_s):
     """The same port on one thread, over the batch's instances in turn until the
     budget is used (vertex-updates/s)."""
     import oracle.oracle as orc
-    from vaikkari_gb300.gpe import Lattice, lattice_info, value_positions
-    from vaikkari_gb300.workloads import harmonic
-    info = lattice_info(Lattice.BCC2)
     orc.set_threads(1)
     done, t0 = 0, time.perf_counter()
     try:
         for c in conds:
             inst = c.inst
-            g = orc.Grid(inst.nx, inst.ny, inst.nz, info["entry"], info["class_weight"], inst.block_scale, inst.dt,
-                         inst.g)
+            g, vdt = _oracle_grid(inst)
             e = np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1))
-            vdt = np.ascontiguousarray(harmonic(value_positions(inst, info), inst.trap) * inst.dt)
             g.leapfrog_bcc2_fast(e, e.copy(), vdt, 1)
             done += inst.nx * inst.ny * inst.nz * 2
             if time.perf_counter() - t0 >= budget_s:
@@ -248,24 +311,24 @@ def run_reference(args):
     """--impl reference: the reference's update loop on the host cores.  The
     reference's stepping exists only as a CUDA kernel, so this runs the oracle
     port (its update and leapfrog restated in C, FP64, OpenMP over all host
-    threads); each step is one leapfrog step over a bounded sample of the batch."""
+    threads); each step is one leapfrog step over a bounded sample of the batch.
+    The condensates are the same seeded batch, built with the oracle's stencil
+    tables; the GPU library is never loaded (the line lists the repository's
+    shared objects this process mapped)."""
     ws, rank, local = _dist()
     if rank != 0:
         return 0
     import oracle.oracle as orc
-    from vaikkari_gb300.gpe import Lattice, lattice_info, value_positions
-    from vaikkari_gb300.workloads import harmonic
+    from oracle.lattice import tables
+    from vaikkari_gb300 import workloads
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
-    conds = build_batch()
-    info = lattice_info(Lattice.BCC2)
+    conds = workloads.config4(geometry=tables(1))
     items = []
     for c in conds:
         inst = c.inst
-        g = orc.Grid(inst.nx, inst.ny, inst.nz, info["entry"], info["class_weight"], inst.block_scale, inst.dt,
-                     inst.g)
+        g, vdt = _oracle_grid(inst)
         e = np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1))
-        vdt = np.ascontiguousarray(harmonic(value_positions(inst, info), inst.trap) * inst.dt)
         items.append((g, e, e.copy(), vdt, inst.nx * inst.ny * inst.nz * 2))
     # calibrate on one step of the whole batch, then bound the per-step sample so
     # that warmup + steps fit in about two minutes
@@ -292,18 +355,52 @@ def run_reference(args):
     el = time.perf_counter() - t0
     value = acc * args.steps / el
     desc = (f"{len(sample)} of {len(items)} instances ({acc} of {total} vertices) per step, FP64 oracle port of "
-            f"GPUGrossPitaevskii_BCC.cu:176-216,475-481 (BCC2 table, direct interior indexing), {threads} threads")
+            f"GPUGrossPitaevskii_BCC.cu:176-216,475-481 (BCC2 table from the reference's Mesh-library Hodge "
+            f"data, direct interior indexing), {threads} threads")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "batch64_bcc2_trap_realtime", "instances": len(items), "sample_instances": len(sample),
+        "config": {"workload": HEADLINE_WORKLOAD, "instances": len(items), "sample_instances": len(sample),
                    "vertices_per_step": acc, "dt": 1e-4, "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": desc},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "native_libraries": loaded_native_libraries(),
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def time_windows(st, stream, steps, dist, clk, min_seconds, min_windows=5, max_windows=5000):
+    """Times windows of exactly `steps` steps with CUDA events on the library's
+    stream, each bracketed by a barrier (N > 1) and a device synchronisation on
+    both sides, until at least `min_windows` windows and `min_seconds` of wall
+    time (so the clock sampler sees the region).  Returns the per-window times
+    (ms) and the kernel launches of one window."""
+    import torch
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times, launches = [], 0
+    clk.start_region()
+    end = time.perf_counter() + min_seconds
+    while len(times) < max_windows and (len(times) < min_windows or time.perf_counter() < end):
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        n0 = st.launch_count()
+        ev0.record(stream)
+        st.step(steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        launches = st.launch_count() - n0
+        times.append(ev0.elapsed_time(ev1))
+    clk.end_region()
+    return times, launches
+
+
+def graph_steps_for(steps):
+    """A step graph of exactly `steps` steps (up to 1000), so the timed region
+    is graph replays, never the direct launches a shorter call falls back to."""
+    return steps if steps <= 1000 else 100
 
 
 def run_ours(args):
@@ -311,61 +408,56 @@ def run_ours(args):
     import torch
     torch.cuda.set_device(local)
     dist = _init_pg(ws, "nccl")
-    from vaikkari_gb300.gpe import Kernel, Lattice, Mode, Potential, Precision, Stepper
+    from vaikkari_gb300.gpe import Kernel, Lattice, Potential, Precision, Stepper
     conds = build_batch(rank, ws, args.scaling)
     insts = [c.inst for c in conds]
     verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
-    verts_job = _sum_over_ranks(dist, verts, device=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    verts_job = _sum_over_ranks(dist, verts, device=dev)
     tile, zchunk, tuned = args.tile, args.zchunk, None
     comp_main = args.precision == "fp32c"
     prec = Precision.FP32C if comp_main else Precision.FP32
     host_t = np.float64 if comp_main else np.float32
     bytes_vs = BYTES_PER_VERTEX_STEP_COMP if comp_main else BYTES_PER_VERTEX_STEP
-    if tile < 0:
-        # untimed: pick the kernel variant and z-chunk for this batch (cached per device)
-        from vaikkari_gb300.autotune import autotune
-        tuned = autotune(insts, precision=prec, potential=Potential.TRAP, device=local)
-        tile, zchunk = tuned["tile"], tuned["zchunk"]
-    st = Stepper(insts, lattice=Lattice.BCC2, precision=prec, kernel=Kernel.FUSED,
-                 potential=Potential.TRAP, graph_steps=100, tile=tile, zchunk=zchunk, device=local)
-    evens, odds = prepare_fields(st, conds, host_t)
-
-    # Warm-up: W steps, plus one replay of the 100-step graph so that the
-    # graph is instantiated before the timed region.
-    st.step(args.warmup)
-    st.step(100)
-    st.synchronize()
-    stream = torch.cuda.ExternalStream(st.stream_handle(), device=local)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    n0 = st.launch_count()
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
+    clk = ClockSampler(local).__enter__()
+    try:
+        if tile < 0:
+            # untimed: pick the kernel variant and z-chunk for this batch (cached per device)
+            from vaikkari_gb300.autotune import autotune
+            tuned = autotune(insts, precision=prec, potential=Potential.TRAP, device=local)
+            tile, zchunk = tuned["tile"], tuned["zchunk"]
+        gsteps = graph_steps_for(args.steps)
+        st = Stepper(insts, lattice=Lattice.BCC2, precision=prec, kernel=Kernel.FUSED,
+                     potential=Potential.TRAP, graph_steps=gsteps, tile=tile, zchunk=zchunk, device=local)
+        evens, odds = prepare_fields(st, conds, host_t)
+        # Warm-up: W steps, then one call of K steps, which instantiates the step
+        # graph before the timed region.
+        st.step(args.warmup)
         st.step(args.steps)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-    launches = st.launch_count() - n0
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        dist.barrier()
-    ms_max = _max_over_ranks(dist, ms, device=torch.device("cuda", local))
-    value = job_value(verts_job, args.steps, ms_max)
+        st.synchronize()
+        stream = torch.cuda.ExternalStream(st.stream_handle(), device=local)
+        clk.wait_first()
+        times, launches = time_windows(st, stream, args.steps, dist, clk, args.window_seconds)
+        ms = statistics.median(times)
+        ms_max = _max_over_ranks(dist, ms, device=dev)
+        value = job_value(verts_job, args.steps, ms_max)
+        per_launch_s = (ms * 1e-3) / max(launches, 1)
+        roof = roofline_block(verts, bytes_vs / 2, per_launch_s,
+                              "fused_bcc2_kernel<float, MODE 2 (compensated)>" if comp_main
+                              else "fused_bcc2_kernel<float, MODE 0>",
+                              "fused_bcc2_fp32c_batch64.md" if comp_main else "fused_bcc2_batch64.md", tile)
+        clocks = clk.summary()
+    finally:
+        clk.__exit__()
 
-    # Roofline of the fused kernel: it is the only kernel in the timed region
-    # (two launches per step), so the average launch lasts ms / launches.
-    peak, peak_kind = _peaks()
-    per_launch_s = (ms * 1e-3) / max(launches, 1)
-    achieved = verts * (bytes_vs / 2) / per_launch_s / 1e9
-    traffic = _profile_traffic("fused_bcc2_fp32c_batch64.md" if comp_main else "fused_bcc2_batch64.md")
-
-    # End to end through the public API with pinned host buffers: upload every
-    # instance (one batched call), run the steps, read the observables, download
-    # every field (one batched call).
+    # End to end through the public API with pinned host buffers.  One call
+    # uploads every instance (one batched call), runs the K steps, reads the
+    # observables and downloads every field (one batched call).  One untimed
+    # call first: the handle allocates the transfers' device staging, copy
+    # stream and events on first use.  e2e = the median of several calls.
     pinned_e, pinned_o = [], []
+    tt = torch.float64 if comp_main else torch.float32
     for e, o in zip(evens, odds):
-        tt = torch.float64 if comp_main else torch.float32
         pe = torch.empty(e.shape, dtype=tt, pin_memory=True).numpy()
         po = torch.empty(o.shape, dtype=tt, pin_memory=True).numpy()
         pe[...] = e
@@ -373,35 +465,42 @@ def run_ours(args):
         pinned_e.append(pe)
         pinned_o.append(po)
     h2d = sum(a.nbytes for a in pinned_e) + sum(a.nbytes for a in pinned_o)
-    # Warm-up of the batched transfers, untimed: the handle allocates their device
-    # staging, copy stream and events on first use.  Downloading right after the
-    # upload returns the same values into the same pinned buffers.
-    st.upload_many([(i, pinned_e[i], pinned_o[i], None) for i in range(len(insts))])
-    st.download_many(range(len(insts)), outs=list(zip(pinned_e, pinned_o)))
-    st.synchronize()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    st.upload_many([(i, pinned_e[i], pinned_o[i], None) for i in range(len(insts))])
-    st.step(args.steps)
-    obs = st.observables(0)
-    st.download_many(range(len(insts)), outs=list(zip(pinned_e, pinned_o)))
-    st.synchronize()
-    e2e_s = time.perf_counter() - t0
-    e2e_s = _max_over_ranks(dist, e2e_s, device=torch.device("cuda", local))
+    d2h = h2d + len(insts) * 56  # both fields back, plus one gpe_observables record per instance
+
+    def one_call():
+        t0 = time.perf_counter()
+        st.upload_many([(i, pinned_e[i], pinned_o[i], None) for i in range(len(insts))])
+        st.step(args.steps)
+        obs_ = st.observables(0)
+        st.download_many(range(len(insts)), outs=list(zip(pinned_e, pinned_o)))
+        st.synchronize()
+        return time.perf_counter() - t0, obs_
+
+    one_call()
+    calls = []
+    for _ in range(max(5, args.e2e_calls)):
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        el, obs = one_call()
+        calls.append(el)
+    e2e_s = _max_over_ranks(dist, statistics.median(calls), device=dev)
     e2e_value = verts_job * args.steps / e2e_s
-    h2d_job = int(_sum_over_ranks(dist, h2d, device=torch.device("cuda", local)))
+    h2d_job = _sum_over_ranks(dist, h2d, device=dev)
+    d2h_job = _sum_over_ranks(dist, d2h, device=dev)
     finite = all(o["finite"] for o in obs)
     st.close()
 
-    # Accuracy at this workload: FP32 vs FP64 (same scheme) after 1000 steps.
+    # Accuracy at this workload after 1000 steps: FP32, FP32C and FP64 (same scheme).
     acc = None
     if rank == 0 and not args.skip_accuracy:
-        acc = accuracy_block(conds, insts, local)
+        acc = accuracy_block(conds, insts, local, timed="fp32c" if comp_main else "fp32")
 
-    # The same batch with compensated FP32 storage (accuracy in `accuracy`).
-    comp = None
-    if rank == 0 and not args.skip_comp and not comp_main:
-        comp = compensated_block(conds, insts, local, args.steps, args.warmup, tune=args.tile < 0)
+    # The batch in the other FP32 storage (plain FP32 when the headline is FP32C).
+    other = None
+    if rank == 0 and not args.skip_comp:
+        other = storage_block(conds, insts, local, args.steps, args.warmup, args.window_seconds,
+                              Precision.FP32 if comp_main else Precision.FP32C, tune=args.tile < 0)
 
     # The FP64 plain path, one instance at a time (the drop-in denominator).
     fp64 = None
@@ -417,7 +516,8 @@ def run_ours(args):
         v1 = cpu_single_core(conds, 3.0)
         cpu = {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
                "sample": f"{steps} leapfrog step(s) of the whole batch ({nv} vertices), FP64 oracle port "
-                         f"(GPUGrossPitaevskii_BCC.cu:176-216,475-481 restated, BCC2 table), {el:.1f} s",
+                         f"(GPUGrossPitaevskii_BCC.cu:176-216,475-481 restated, BCC2 table from the "
+                         f"reference's Mesh-library Hodge data), {el:.1f} s",
                "value_1core": v1}
 
     if rank == 0:
@@ -425,28 +525,31 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": args.scaling, "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batch64_bcc2_trap_realtime" + ("_compensated" if comp_main else ""),
-                       "storage": "fp32 + bf16 residual" if comp_main else "fp32", "instances": len(insts),
-                       "vertices": verts, "vertices_all_ranks": verts_job,
+            "config": {"workload": HEADLINE_WORKLOAD,
+                       "storage": "fp32 + bf16 residual (GPE_FP32C)" if comp_main else "fp32",
+                       "instances": len(insts), "vertices": verts, "vertices_all_ranks": verts_job,
                        "sizes": sorted({i.nx for i in insts}), "dt": 1e-4,
-                       "graph_steps": 100, "kernel": "fused", "variant": tile, "zchunk": zchunk,
+                       "graph_steps": gsteps, "kernel": "fused", "variant": tile, "zchunk": zchunk,
                        "autotuned": tuned is not None,
                        "parallelism": (f"condensate shards x{ws} ({args.scaling}), no collective"
                                        if ws > 1 else "single"),
-                       "l2": f"inputs larger than L2 (fields {2 * 8 * verts / 1e6:.0f} MB vs {L2_BYTES / 1e6:.0f} MB)"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "algorithmic_bytes_per_vertex_step": bytes_vs,
-                         "peak_source": f"{peak_kind} hbm_gbs", "kernel": "fused_bcc2_kernel"},
+                       "l2": f"inputs larger than L2 (fields {2 * 8 * verts / 1e6:.0f} MB vs {L2_BYTES / 1e6:.0f} MB)",
+                       "timing": (f"median of {len(times)} windows of {args.steps} steps (one graph replay each), "
+                                  f"CUDA events on the library stream"),
+                       "window_ms": {"min": min(times), "median": ms, "max": max(times)}},
+            "roofline": roof,
             "gpu_launches": launches,
-            "clocks": clk.summary(),
-            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d_job,
-                    "d2h_bytes_per_step": h2d_job,
-                    "steps_per_call": args.steps, "seconds": e2e_s, "finite": finite},
+            "clocks": clocks,
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d_job / args.steps,
+                    "d2h_bytes_per_step": d2h_job / args.steps, "h2d_bytes_per_call": h2d_job,
+                    "d2h_bytes_per_call": d2h_job, "steps_per_call": args.steps,
+                    "seconds_median": e2e_s, "seconds_all": calls, "calls": len(calls), "finite": finite,
+                    "call": "gpe_upload_many (pinned host) + gpe_step + gpe_observables_get + gpe_download_many"},
             "cpu_baseline": cpu,
             "accuracy": acc,
-            "compensated": comp,
+            ("plain_fp32" if comp_main else "compensated"): other,
             "fp64_plain": fp64,
+            "native_libraries": loaded_native_libraries(),
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -454,10 +557,13 @@ def run_ours(args):
     return 0
 
 
-def accuracy_block(conds, insts, device):
+def accuracy_block(conds, insts, device, timed="fp32c"):
+    """FP32 and FP32C against FP64 of the same scheme after 1000 real-time steps
+    of the whole batch: aggregate and worst-instance relative L2, and the worst
+    norm and energy drift.  `timed` names the storage the headline timed; its
+    figures are repeated under "timed"."""
     from vaikkari_gb300.gpe import Kernel, Lattice, Potential, Precision, Stepper
     steps = 1000
-    res = {}
     outs = {}
     for prec, dt_ in ((Precision.FP32, np.float32), (Precision.FP64, np.float64), (Precision.FP32C, np.float64)):
         st = Stepper(insts, lattice=Lattice.BCC2, precision=prec, kernel=Kernel.FUSED, potential=Potential.TRAP,
@@ -469,75 +575,67 @@ def accuracy_block(conds, insts, device):
         fields = [st.download(i, odd=False)[0].astype(np.float64) for i in range(len(insts))]
         st.close()
         outs[prec] = (o0, o1, fields)
-    num = sum(float(np.sum((a - b) ** 2)) for a, b in zip(outs[Precision.FP32][2], outs[Precision.FP64][2]))
-    den = sum(float(np.sum(b ** 2)) for b in outs[Precision.FP64][2])
-    n32 = [o["norm"] for o in outs[Precision.FP32][1]]
+    f64 = outs[Precision.FP64][2]
+    den = sum(float(np.sum(b ** 2)) for b in f64)
     n64 = [o["norm"] for o in outs[Precision.FP64][1]]
-    e32 = [o["energy"] for o in outs[Precision.FP32][1]]
     e64 = [o["energy"] for o in outs[Precision.FP64][1]]
     n0 = [o["norm"] for o in outs[Precision.FP64][0]]
-    res["steps"] = steps
-    res["rel_l2_fp32_vs_fp64"] = math.sqrt(num / den)
-    res["max_norm_drift_fp32_vs_fp64"] = max(abs(a - b) / b for a, b in zip(n32, n64))
-    res["max_energy_drift_fp32_vs_fp64"] = max(abs(a - b) / abs(b) for a, b in zip(e32, e64))
-    res["max_norm_drift_fp64_scheme"] = max(abs(a - b) / b for a, b in zip(n64, n0))
-    # per-instance relative L2 (each condensate weighted alike)
-    per32 = [math.sqrt(float(np.sum((a - b) ** 2)) / float(np.sum(b ** 2)))
-             for a, b in zip(outs[Precision.FP32][2], outs[Precision.FP64][2])]
-    res["max_instance_rel_l2_fp32"] = max(per32)
-    res["instances_over_1e-5_fp32"] = sum(1 for v in per32 if v > 1e-5)
-    # compensated storage (Precision.FP32C)
-    cf = outs[Precision.FP32C][2]
-    numc = sum(float(np.sum((a - b) ** 2)) for a, b in zip(cf, outs[Precision.FP64][2]))
-    perc = [math.sqrt(float(np.sum((a - b) ** 2)) / float(np.sum(b ** 2)))
-            for a, b in zip(cf, outs[Precision.FP64][2])]
-    nc = [o["norm"] for o in outs[Precision.FP32C][1]]
-    ec = [o["energy"] for o in outs[Precision.FP32C][1]]
-    res["rel_l2_fp32c_vs_fp64"] = math.sqrt(numc / den)
-    res["max_instance_rel_l2_fp32c"] = max(perc)
-    res["max_norm_drift_fp32c_vs_fp64"] = max(abs(a - b) / b for a, b in zip(nc, n64))
-    res["max_energy_drift_fp32c_vs_fp64"] = max(abs(a - b) / abs(b) for a, b in zip(ec, e64))
+    res = {"steps": steps, "reference": "FP64 run of the same scheme (fused kernel, same inputs)",
+           "max_norm_drift_fp64_scheme": max(abs(a - b) / b for a, b in zip(n64, n0))}
+    for tag, prec in (("fp32", Precision.FP32), ("fp32c", Precision.FP32C)):
+        f = outs[prec][2]
+        num = sum(float(np.sum((a - b) ** 2)) for a, b in zip(f, f64))
+        per = [math.sqrt(float(np.sum((a - b) ** 2)) / float(np.sum(b ** 2))) for a, b in zip(f, f64)]
+        nn = [o["norm"] for o in outs[prec][1]]
+        ee = [o["energy"] for o in outs[prec][1]]
+        res[f"rel_l2_{tag}_vs_fp64"] = math.sqrt(num / den)
+        res[f"max_instance_rel_l2_{tag}"] = max(per)
+        res[f"instances_over_1e-5_{tag}"] = sum(1 for v in per if v > 1e-5)
+        res[f"max_norm_drift_{tag}_vs_fp64"] = max(abs(a - b) / b for a, b in zip(nn, n64))
+        res[f"max_energy_drift_{tag}_vs_fp64"] = max(abs(a - b) / abs(b) for a, b in zip(ee, e64))
+    res["timed"] = {"storage": timed, "rel_l2_vs_fp64": res[f"rel_l2_{timed}_vs_fp64"],
+                    "max_instance_rel_l2": res[f"max_instance_rel_l2_{timed}"],
+                    "max_norm_drift_vs_fp64": res[f"max_norm_drift_{timed}_vs_fp64"],
+                    "max_energy_drift_vs_fp64": res[f"max_energy_drift_{timed}_vs_fp64"],
+                    "meets_l2_1e-5": res[f"rel_l2_{timed}_vs_fp64"] <= 1e-5,
+                    "meets_norm_drift_1e-6": res[f"max_norm_drift_{timed}_vs_fp64"] <= 1e-6}
     return res
 
 
-def compensated_block(conds, insts, device, steps, warmup, tune=True):
-    """The batch in Precision.FP32C (compensated FP32 storage): its own
-    autotuned variant, K timed steps after W + 100 warm-up steps, and the
-    roofline at 64 B per vertex-step."""
+def storage_block(conds, insts, device, steps, warmup, window_seconds, prec, tune=True):
+    """The batch in another storage (Precision.FP32 or FP32C): its own autotuned
+    variant, timed like the headline (median of windows of K steps after W + K
+    warm-up steps), with its roofline."""
     import torch
     from vaikkari_gb300.gpe import Kernel, Lattice, Potential, Precision, Stepper
+    comp = prec == Precision.FP32C
     tile, zchunk = 0, 0
     if tune:
         from vaikkari_gb300.autotune import autotune
-        t = autotune(insts, precision=Precision.FP32C, potential=Potential.TRAP, device=device)
+        t = autotune(insts, precision=prec, potential=Potential.TRAP, device=device)
         tile, zchunk = t["tile"], t["zchunk"]
-    st = Stepper(insts, lattice=Lattice.BCC2, precision=Precision.FP32C, kernel=Kernel.FUSED,
-                 potential=Potential.TRAP, graph_steps=100, tile=tile, zchunk=zchunk, device=device)
-    prepare_fields(st, conds, np.float64)
+    st = Stepper(insts, lattice=Lattice.BCC2, precision=prec, kernel=Kernel.FUSED,
+                 potential=Potential.TRAP, graph_steps=graph_steps_for(steps), tile=tile, zchunk=zchunk,
+                 device=device)
+    prepare_fields(st, conds, np.float64 if comp else np.float32)
     st.step(warmup)
-    st.step(100)
+    st.step(steps)
     st.synchronize()
     stream = torch.cuda.ExternalStream(st.stream_handle(), device=device)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    n0 = st.launch_count()
-    ev0.record(stream)
-    st.step(steps)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    launches = st.launch_count() - n0
-    ms = ev0.elapsed_time(ev1)
+    clk = ClockSampler(device)
+    times, launches = time_windows(st, stream, steps, None, clk, min(window_seconds, 0.5))
+    ms = statistics.median(times)
     verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
     st.close()
-    peak, kind = _peaks()
-    achieved = verts * (BYTES_PER_VERTEX_STEP_COMP / 2) / ((ms * 1e-3) / max(launches, 1)) / 1e9
+    bytes_vs = BYTES_PER_VERTEX_STEP_COMP if comp else BYTES_PER_VERTEX_STEP
+    roof = roofline_block(verts, bytes_vs / 2, (ms * 1e-3) / max(launches, 1),
+                          "fused_bcc2_kernel<float, MODE 2 (compensated)>" if comp else
+                          "fused_bcc2_kernel<float, MODE 0>",
+                          "fused_bcc2_fp32c_batch64.md" if comp else "fused_bcc2_batch64.md", tile)
     return {"value": verts * steps / (ms * 1e-3), "unit": METRIC, "ms_per_step": ms / steps, "steps": steps,
-            "variant": tile, "zchunk": zchunk, "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": _profile_traffic("fused_bcc2_fp32c_batch64.md"),
-                         "algorithmic_bytes_per_vertex_step": BYTES_PER_VERTEX_STEP_COMP,
-                         "peak_source": f"{kind} hbm_gbs"},
-            "storage": "FP32 value + bf16 residual per component (12 B per value and field)"}
+            "windows": len(times), "variant": tile, "zchunk": zchunk, "gpu_launches": launches, "roofline": roof,
+            "storage": ("FP32 value + bf16 residual per component (12 B per value and field)" if comp
+                        else "FP32 (8 B per value and field)")}
 
 
 def fp64_plain_rate(conds, insts, device, steps):
@@ -605,7 +703,8 @@ def _cpu_config_rate(conds, budget_s=5.0, lattice=None):
     """FP64 oracle port on all host threads: whole leapfrog steps of every
     condensate for about `budget_s` seconds (at least one step)."""
     e64 = [np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1)) for c in conds]
-    v, n, el, nv = cpu_sample(conds, e64, [a.copy() for a in e64], budget_s, os.cpu_count() or 1, lattice)
+    v, n, el, nv = cpu_sample(conds, e64, [a.copy() for a in e64], budget_s, os.cpu_count() or 1,
+                              1 if lattice is None else int(lattice))
     return {"value": v, "unit": METRIC, "cores": os.cpu_count() or 1, "kind": "port",
             "sample": f"{n} leapfrog step(s), {nv} vertices, FP64 oracle port, {el:.2f} s"}
 
@@ -658,26 +757,70 @@ def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1, latt
             row["norm_drift_fp64_vs_initial"] = max(abs(a["norm"] - b["norm"]) / b["norm"] for a, b in zip(o64, o64_0))
             row["energy_fp64"] = [o["energy"] for o in o64]
         acc.append(row)
-    # throughput: FP32 fused and FP64 plain, device time of 200 steps after warm-up
-    rates = {}
+    # throughput, device time: windows of 200 steps (one graph replay each) after
+    # warm-up, median, with the clocks sampled over the FP32 windows
+    rates, rooflines, clocks = {}, {}, None
     cases = ((("fp32_plain", Precision.FP32, Kernel.PLAIN), ("fp64_plain", Precision.FP64, Kernel.PLAIN)) if ref_mode
-             else (("fp32_fused", Precision.FP32, Kernel.FUSED), ("fp64_fused", Precision.FP64, Kernel.FUSED),
-                   ("fp64_plain", Precision.FP64, Kernel.PLAIN)))
+             else (("fp32_fused", Precision.FP32, Kernel.FUSED), ("fp32c_fused", Precision.FP32C, Kernel.FUSED),
+                   ("fp64_fused", Precision.FP64, Kernel.FUSED), ("fp64_plain", Precision.FP64, Kernel.PLAIN)))
+    head = "fp32_plain" if ref_mode else "fp32_fused"
     for key, prec, kern_ in cases:
-        st = _stepper(conds, prec, kern_, Mode.REAL, tile=tile if kern_ == kern else 0, lattice=lattice,
-                      zchunk=zchunk if kern_ == Kernel.FUSED else 0)
-        prepare_fields(st, conds, np.float64 if prec == Precision.FP64 else np.float32)
-        st.time_steps(103)
-        ms = min(st.time_steps(200) for _ in range(2))
-        rates[key] = verts * 200 / (ms * 1e-3)
+        tk, zk = (tile, zchunk) if kern_ == kern and prec != Precision.FP32C else (0, 0)
+        if prec == Precision.FP32C:
+            from vaikkari_gb300.autotune import autotune
+            tc = autotune(insts, precision=Precision.FP32C)
+            tk, zk = tc["tile"], tc["zchunk"]
+        st = _stepper(conds, prec, kern_, Mode.REAL, tile=tk, lattice=lattice, zchunk=zk, graph_steps=200)
+        prepare_fields(st, conds, np.float64 if prec in (Precision.FP64, Precision.FP32C) else np.float32)
+        rates[key], rooflines[key], clk = _windowed_rate(st, verts, 200, key == head, prec, kern_, tk)
+        if clk is not None:
+            clocks = clk
         st.close()
-    return {"metric": METRIC, "value": rates["fp32_plain" if ref_mode else "fp32_fused"], "unit": METRIC,
-            "dtype": "f32",
+    return {"metric": METRIC, "value": rates[head], "unit": METRIC, "dtype": "f32",
             "config": {"workload": name, "lattice": lattice.name, "instances": len(insts), "vertices": verts,
                        "dt": insts[0].dt, "variant": tile, "zchunk": zchunk,
+                       "timing": "median of windows of 200 steps (one graph replay each), CUDA events",
                        "mode": "ref-mode (12 values per block, block scale a/sqrt(8))" if ref_mode
                        else "config-mode (2 values per cell)"},
-            "rates": rates, "accuracy": acc, "cpu_baseline": _cpu_config_rate(conds, lattice=lattice)}
+            "roofline": rooflines[head], "clocks": clocks, "rates": rates, "rooflines": rooflines,
+            "accuracy": acc, "cpu_baseline": _cpu_config_rate(conds, lattice=lattice)}
+
+
+def _windowed_rate(st, verts, steps, sample_clocks, prec, kern, tile, seconds=1.0):
+    """Vertex-updates/s of a prepared stepper: median of windows of `steps`
+    steps after one untimed call; the roofline at the algorithmic bytes of the
+    trap form (24 B per value and half-step in FP32, 32 B in FP32C, 48 B in
+    FP64; the two-step variants move 16 / 32 B per value and half-step)."""
+    import torch
+    from vaikkari_gb300.gpe import Precision, variants
+    st.step(3)
+    st.step(steps)
+    st.synchronize()
+    stream = torch.cuda.ExternalStream(st.stream_handle(), device=torch.cuda.current_device())
+    clk = ClockSampler(torch.cuda.current_device())
+    if sample_clocks:
+        clk.__enter__()
+        clk.wait_first()
+    try:
+        times, launches = time_windows(st, stream, steps, None, clk, seconds)
+    finally:
+        if sample_clocks:
+            clk.__exit__()
+    ms = statistics.median(times)
+    half_steps = 2 * steps
+    per_value_half = {Precision.FP32: 24, Precision.FP32C: 32, Precision.FP64: 48}[prec]
+    vinfo = {v["tile"]: v for v in variants()}
+    if kern.name == "FUSED" and tile in vinfo and vinfo[tile]["half_steps"] == 2:
+        per_value_half = per_value_half * 2 // 3  # both fields read once and written once per step
+    peak, kind = _peaks()
+    # the stepping kernel is the only kernel in the window: its average launch
+    # moves the window's algorithmic bytes / launches in window time / launches
+    achieved = verts * per_value_half * half_steps / (ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "traffic_source": "not captured for this workload",
+            "algorithmic_bytes_per_vertex_step": 2 * per_value_half, "launches_per_window": launches,
+            "peak_source": f"{kind} hbm_gbs (of {kind})"}
+    return verts * steps / (ms * 1e-3), roof, (clk.summary() if sample_clocks else None)
 
 
 def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1, lattice=None):
@@ -740,22 +883,20 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1, latti
 def _cpu_imag_rate(conds, budget_s=5.0, lattice=None):
     """FP64 oracle imaginary-time steps (observables, then the normalised Euler
     step, all host threads for the step) of every condensate for about
-    `budget_s` seconds."""
+    `budget_s` seconds; stencil tables from the oracle's own copy."""
     import oracle.oracle as orc
-    from vaikkari_gb300.gpe import Lattice, lattice_info, value_positions
-    from vaikkari_gb300.workloads import harmonic
-    info = lattice_info(Lattice.BCC2 if lattice is None else lattice)
+    from oracle.lattice import tables
+    lat = 1 if lattice is None else int(lattice)
+    t = tables(lat)
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
     jobs = []
     for c in conds:
         inst = c.inst
-        g = orc.Grid(inst.nx, inst.ny, inst.nz, info["entry"], info["class_weight"], inst.block_scale, inst.dt,
-                     inst.g)
-        vdt = np.ascontiguousarray(harmonic(value_positions(inst, info), inst.trap) * inst.dt)
+        g, vdt = _oracle_grid(inst, lat)
         psi = np.ascontiguousarray(np.stack([c.psi.real, c.psi.imag], -1), dtype=np.float64)
-        jobs.append((g, psi, vdt, info["cell_volume"] * inst.block_scale ** 3))
-    verts = sum(c.inst.nx * c.inst.ny * c.inst.nz * info["slots"] for c in conds)
+        jobs.append((g, psi, vdt, t["cell_volume"] * inst.block_scale ** 3))
+    verts = sum(c.inst.nx * c.inst.ny * c.inst.nz * t["slots"] for c in conds)
     steps, t0 = 0, time.perf_counter()
     while True:
         for g, psi, vdt, vol in jobs:
@@ -1017,9 +1158,13 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=200)
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
-    ap.add_argument("--skip-comp", action="store_true", help="skip the compensated-storage (FP32C) timing")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp32c"],
-                    help="batch64: storage of the timed path (fp32c = FP32 + bf16 residual)")
+    ap.add_argument("--skip-comp", action="store_true", help="skip the timing of the other FP32 storage")
+    ap.add_argument("--precision", default="fp32c", choices=["fp32", "fp32c"],
+                    help="batch64: storage of the timed path (fp32c = FP32 + bf16 residual, the storage that "
+                         "meets relative L2 <= 1e-5 after 1000 steps; fp32 = plain FP32)")
+    ap.add_argument("--window-seconds", type=float, default=2.0,
+                    help="keep timing windows of --steps steps for at least this long (median reported)")
+    ap.add_argument("--e2e-calls", type=int, default=5, help="timed end-to-end calls (median reported)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--workload", default="batch64",
                     help="batch64 (the headline), config1/config2/config3/config5 (accuracy cases), relax "

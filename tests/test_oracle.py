@@ -123,3 +123,19 @@ def test_bcc2_fast_path_bit_identical(dims):
     g.leapfrog_bcc2_fast(e2, o2, v, 3)
     np.testing.assert_array_equal(e1, e2)
     np.testing.assert_array_equal(o1, o2)
+
+
+def test_workloads_same_with_oracle_geometry():
+    """The CPU baseline builds the seeded batch with the oracle's stencil tables
+    (so it never loads the library); the condensates must be the very ones the
+    GPU path builds with the library's tables."""
+    from vaikkari_gb300.gpe import lattice_info
+    a = workloads.config4(geometry=tables(Lattice.BCC2), count=6)
+    b = workloads.config4(geometry=lattice_info(Lattice.BCC2), count=6)
+    for x, y in zip(a, b):
+        assert x.inst == y.inst
+        np.testing.assert_array_equal(x.psi, y.psi)
+    c1 = workloads.config1(Lattice.TETRA12, geometry=tables(Lattice.TETRA12), n=6)
+    c2 = workloads.config1(Lattice.TETRA12, n=6)
+    np.testing.assert_array_equal(c1.V, c2.V)
+    np.testing.assert_allclose(c1.psi, c2.psi, rtol=1e-14, atol=0)
