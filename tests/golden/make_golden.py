@@ -5,7 +5,7 @@ copied): builds ``oracle/_ref/ref_fixtures`` with ``make -C oracle ref`` (the
 reference's GPUGrossPitaevskii_BCC.cu host code, VortexState, Mesh library and
 MT19937, compiled from their sources) and records what it prints.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref DIR]     (DIR: $VAIKKARI_REFERENCE, else /root/reference)
 
 Outputs (committed):
   ref_tables.json        getPositions/getLaplacian (GPUGrossPitaevskii_BCC.cu:73-142)
@@ -45,7 +45,8 @@ def run(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("VAIKKARI_REFERENCE", "/root/reference"),
+                    help="reference source tree (default: $VAIKKARI_REFERENCE, else /root/reference)")
     a = ap.parse_args()
     gp = os.path.join(a.ref, "koodit", "GrossPitaevskii")
     if not os.path.isdir(gp):

@@ -22,9 +22,13 @@
 // Set-up: host code cannot use the array's name as a device address, so the
 // first call on each device (with that device current) looks the address up
 // with cudaGetSymbolAddress and caches it; that first call should therefore be
-// made before any stream capture begins.  The stencil tables are computed when
-// the library is loaded.
+// made before any stream capture begins.  The cache is keyed on the device's
+// current CUDA context by its process-unique id (cuCtxGetId), so after a
+// cudaDeviceReset, or any other change of context, the next call looks the
+// address up again instead of using one from a destroyed context.  The stencil
+// tables are computed when the library is loaded.
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -44,9 +48,48 @@ constexpr int kMaxDevices = 64;
 // rows [0, kRows): one row of 6 partial sums per CTA; row kRows: the final sums
 static __device__ __align__(256) double g_noalloc_scratch[(kRows + 1) * 6];
 
-// Host-side cache of the array's device address, per device ordinal.
-double *g_scratch_addr[kMaxDevices] = {};
+// Host-side cache of the array's device address, per device ordinal, valid for
+// the context whose id it records.
+struct ScratchAddr {
+    unsigned long long ctx_id = 0;
+    double *ptr = nullptr;
+};
+ScratchAddr g_scratch_addr[kMaxDevices];
 std::mutex g_scratch_mutex;
+
+// cuCtxGetCurrent and cuCtxGetId through the runtime's driver entry point (the
+// library links only the CUDA runtime); looked up once.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+struct CtxFns {
+    CtxGetCurrentFn current = nullptr;
+    CtxGetIdFn id = nullptr;
+    CtxFns()
+    {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            current = (CtxGetCurrentFn)fn;
+        fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            id = (CtxGetIdFn)fn;
+    }
+};
+
+// Id of the calling thread's current context; 0 if there is none or it cannot
+// be told (then the address is looked up on every call).
+unsigned long long current_context_id()
+{
+    static const CtxFns fns;
+    if (!fns.current || !fns.id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (fns.current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    if (fns.id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 // Stencil of each lattice, packed for the kernel and passed by value.
 struct NoallocStencil {
@@ -172,7 +215,8 @@ __global__ void __launch_bounds__(kThreads) noalloc_observables_kernel(const Noa
     if (t < 6) rows[6ll * blockIdx.x + t] = t < 4 ? sm[t][0] : 0.0;
 }
 
-// The array's device address for the current device (first call: look it up).
+// The array's device address for the current device and context (first call
+// in a context: look it up).
 gpe_status scratch_for_current_device(double **out)
 {
     int dev = -1;
@@ -180,13 +224,16 @@ gpe_status scratch_for_current_device(double **out)
     if (e != cudaSuccess) return cuda_fail(e, "gpe_observables_noalloc: cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices) return fail(GPE_ERR_UNSUPPORTED, "gpe_observables_noalloc: device ordinal too high");
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[dev]) {
+    ScratchAddr &c = g_scratch_addr[dev];
+    const unsigned long long id = current_context_id();
+    if (id == 0 || c.ptr == nullptr || c.ctx_id != id) {
         void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // makes the device's primary context current if needed
         if (e != cudaSuccess) return cuda_fail(e, "gpe_observables_noalloc: cudaGetSymbolAddress");
-        g_scratch_addr[dev] = (double *)p;
+        c.ptr = (double *)p;
+        c.ctx_id = current_context_id();
     }
-    *out = g_scratch_addr[dev];
+    *out = c.ptr;
     return GPE_OK;
 }
 
@@ -250,6 +297,9 @@ static gpe_status gpe_observables_noalloc_impl(int32_t lattice, int32_t precisio
     out->mu = (out->kinetic + out->potential + 2.0 * out->interaction) / out->norm;
     out->finite = std::isfinite(out->norm) && std::isfinite(out->energy) && std::isfinite(out->mu);
     out->pad_ = 0;
+    if (out->norm == 0.0)
+        return fail(GPE_ERR_NOT_FINITE, "gpe_observables_noalloc: the field is zero everywhere (norm 0), so mu is "
+                                        "undefined");
     if (!out->finite) return fail(GPE_ERR_NOT_FINITE, "gpe_observables_noalloc: NaN or Inf in the field");
     return GPE_OK;
 }
