@@ -255,6 +255,15 @@ gpe_status gpe_variant_describe(int32_t variant, int32_t *tile_x, int32_t *tile_
  * second set of fields and refuse gpe_link_z).  0 for no such variant. */
 int32_t gpe_variant_half_steps(int32_t variant);
 
+/* How a variant advances time: 0 = one half-step per launch; 1 = a whole
+ * leapfrog step per launch (the two-step variants above); 2 = persistent: one
+ * cooperative launch per gpe_step call advances every instance by all its
+ * steps, each work item starting a half-step as soon as the neighbouring items
+ * it reads have finished the previous one (BCC2, real time, FP64, FP32 or
+ * GPE_FP32C; refuses gpe_link_z).  -1 for no such variant.  The reference
+ * launches twice per step from a host loop (GPUGrossPitaevskii_BCC.cu:475-481). */
+int32_t gpe_variant_kind(int32_t variant);
+
 /* Kernel launches the handle has issued (for accounting). */
 int64_t gpe_launch_count(gpe_handle h);
 

@@ -93,7 +93,8 @@ def autotune(instances: List[Instance], fields=None, lattice=Lattice.BCC2, preci
     """Best (tile, zchunk) for this batch.  Every variant is timed with the
     automatic z-chunk, then the three fastest with each z-chunk in `zchunks`.
     Imaginary time and compensated storage (Precision.FP32C) skip the variants
-    that advance whole real-time steps."""
+    that advance whole real-time steps; imaginary time also skips the persistent
+    variants (real time only)."""
     name = _device_name(device)
     sig = signature(instances, lattice, precision, potential, name, mode)
     db = _load() if cache else {}
@@ -102,6 +103,8 @@ def autotune(instances: List[Instance], fields=None, lattice=Lattice.BCC2, preci
     results = []
     for v in variants():
         if (mode != Mode.REAL or Precision(precision) == Precision.FP32C) and v["half_steps"] != 1:
+            continue
+        if mode != Mode.REAL and v["persistent"]:  # real time only
             continue
         r = measure(instances, v["tile"], 0, fields, lattice, precision, potential, steps, device, mode)
         results.append({"tile": v["tile"], "zchunk": 0, "vups": r})

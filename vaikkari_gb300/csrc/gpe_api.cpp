@@ -126,6 +126,13 @@ struct gpe_handle_ {
     uint32_t slots_from_above = 0, slots_from_below = 0;  // slots the stencil reads at z+1 / z-1
     bool imag_ready = false;
     bool faces = false;  // TETRA12 stepped in the face form (gpe_config.faces)
+    // persistent variants: one launch per gpe_step call; per work item its
+    // neighbouring items (CSR) and an epoch word, the half-steps it has completed
+    bool persistent = false;
+    int *nbr_begin_dev = nullptr, *nbr_dev = nullptr;
+    unsigned int *done = nullptr;
+    unsigned int epoch = 0;      // done[] of every item after the launches queued so far
+    bool epoch_reset = false;    // a launch timed out: zero done[] before the next one
     double tol = 0.0;
     long long launches = 0;
 };
@@ -193,6 +200,7 @@ gpe_status sync_and_check(gpe_handle h)
     if (err != 0) {
         cudaMemsetAsync(h->err, 0, sizeof(int), h->stream);
         cudaStreamSynchronize(h->stream);
+        h->epoch_reset = true;  // the persistent kernel's epoch words stopped part-way
         return fail(GPE_ERR_TIMEOUT, "a bounded wait in the fused kernel ran out; the step was abandoned");
     }
     return GPE_OK;
@@ -499,8 +507,53 @@ gpe_status enqueue_steps(gpe_handle h, long long steps)
     return GPE_OK;
 }
 
+// Persistent variants: one cooperative launch per call advances every instance
+// by `steps` leapfrog steps (no graphs: there is one launch to replay).
+gpe_status run_persistent(gpe_handle h, long long steps)
+{
+    constexpr long long kMaxSteps = 1ll << 24;  // per launch, so the epoch arithmetic stays far from wrapping
+    while (steps > 0) {
+        const long long n = std::min(steps, kMaxSteps);
+        if (h->epoch_reset) {
+            GPE_CUDA_TRY(cudaMemsetAsync(h->done, 0, sizeof(unsigned int) * h->items.size(), h->stream));
+            h->epoch = 0;
+            h->epoch_reset = false;
+        }
+        PersistLaunch l{};
+        l.precision = h->cfg.precision;
+        l.potential = h->cfg.potential;
+        l.variant = fused_persistent_index(h->tile);
+        l.comp = h->comp ? 1 : 0;
+        l.device = h->cfg.device;
+        l.inst = h->idev;
+        l.items = h->items_dev;
+        l.num_items = int(h->items.size());
+        l.maps = h->maps;
+        l.lo_maps = h->lo_maps;
+        l.field[0] = h->buf[0];
+        l.field[1] = h->buf[1];
+        l.lo[0] = h->lo[0];
+        l.lo[1] = h->lo[1];
+        l.vpot = h->vpot;
+        l.nbr_begin = h->nbr_begin_dev;
+        l.nbr = h->nbr_dev;
+        l.done = h->done;
+        l.epoch0 = h->epoch;
+        l.half_steps = int(2 * n);
+        l.err = h->err;
+        l.inject_skip_plane = h->inject;
+        int grid = 0;
+        GPE_CUDA_TRY(launch_persistent(l, h->stream, &grid));
+        h->launches++;
+        h->epoch += unsigned(2 * n);
+        steps -= n;
+    }
+    return GPE_OK;
+}
+
 gpe_status run_steps(gpe_handle h, long long steps)
 {
+    if (h->persistent) return run_persistent(h, steps);
     const long long G = h->cfg.graph_steps == 0 ? 100 : h->cfg.graph_steps;
     if (h->cfg.graph_steps < 0 || steps < G) return enqueue_steps(h, steps);
     long long done = 0;
@@ -555,6 +608,9 @@ void free_handle(gpe_handle h)
     cudaFree(h->pb_zcs);
     cudaFree(h->items_dev);
     cudaFree(h->item_begin_dev);
+    cudaFree(h->nbr_begin_dev);
+    cudaFree(h->nbr_dev);
+    cudaFree(h->done);
     cudaFree(h->imag);
     cudaFree(h->partials);
     cudaFree(h->counter);
@@ -880,6 +936,14 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
     if (h->fused) {
         h->tile = cfg->tile > 0 && cfg->tile < fused_tile_count() ? cfg->tile : 0;
         fused_tile_shape(h->tile, &h->tx, &h->ty);
+        if (fused_variant_kind(h->tile) == kVariantPersistent) {
+            if (cfg->mode != GPE_REAL_TIME) {
+                free_handle(h);
+                return fail(GPE_ERR_UNSUPPORTED, "gpe_create: the persistent kernel variants advance real time; "
+                                                 "imaginary time needs a one-launch-per-half-step variant");
+            }
+            h->persistent = true;
+        }
         if (fused_half_steps(h->tile) == 2) {
             if (cfg->mode != GPE_REAL_TIME) {
                 free_handle(h);
@@ -948,6 +1012,40 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
         for (int oi : order) {
             first[oi] = int(h->items.size());
             h->items.insert(h->items.end(), per[oi].begin(), per[oi].end());
+        }
+        if (h->persistent) {
+            // Each item depends on the items of its instance within one tile and
+            // one z-chunk (itself included): the halo it reads, and the reads of
+            // the field it rewrites.  Items of instance i are numbered
+            // first[i] + (zi * nty + yi) * ntx + xi.
+            std::vector<int> nb_begin(1, 0), nb;
+            std::vector<int> owner(h->items.size());
+            for (int i = 0; i < cfg->num_instances; i++)
+                for (size_t k = 0; k < per[i].size(); k++) owner[first[i] + k] = i;
+            for (size_t it = 0; it < h->items.size(); it++) {
+                const int i = owner[it];
+                const gpe_instance &in = h->inst[i];
+                const int ntx = (in.nx + h->tx - 1) / h->tx, nty = (in.ny + h->ty - 1) / h->ty;
+                const int nzc = (in.nz + zc - 1) / zc;
+                const WorkItem &w = h->items[it];
+                const int xi = w.x0 / h->tx, yi = w.y0 / h->ty, zi = w.z0 / zc;
+                for (int dz = -1; dz <= 1; dz++)
+                    for (int dy = -1; dy <= 1; dy++)
+                        for (int dx = -1; dx <= 1; dx++) {
+                            const int X = xi + dx, Y = yi + dy, Z = zi + dz;
+                            if (X < 0 || X >= ntx || Y < 0 || Y >= nty || Z < 0 || Z >= nzc) continue;
+                            nb.push_back(first[i] + (Z * nty + Y) * ntx + X);
+                        }
+                nb_begin.push_back(int(nb.size()));
+            }
+            GPE_CREATE_TRY(cudaMalloc(&h->nbr_begin_dev, sizeof(int) * nb_begin.size()));
+            GPE_CREATE_TRY(cudaMemcpyAsync(h->nbr_begin_dev, nb_begin.data(), sizeof(int) * nb_begin.size(),
+                                           cudaMemcpyHostToDevice, h->stream));
+            GPE_CREATE_TRY(cudaMalloc(&h->nbr_dev, sizeof(int) * nb.size()));
+            GPE_CREATE_TRY(cudaMemcpyAsync(h->nbr_dev, nb.data(), sizeof(int) * nb.size(), cudaMemcpyHostToDevice,
+                                           h->stream));
+            GPE_CREATE_TRY(cudaMalloc(&h->done, sizeof(unsigned int) * h->items.size()));
+            GPE_CREATE_TRY(cudaMemsetAsync(h->done, 0, sizeof(unsigned int) * h->items.size(), h->stream));
         }
         // Items of instance i occupy rows [first[i], first[i] + per[i].size()).
         std::vector<int> ranges(2 * cfg->num_instances);
@@ -1501,7 +1599,7 @@ static gpe_status gpe_link_z_impl(gpe_handle h, int32_t lower, int32_t upper)
     if (h->cfg.mode != GPE_REAL_TIME)
         return fail(GPE_ERR_UNSUPPORTED, "gpe_link_z: slabs are supported in real time (imaginary time "
                                          "normalises each instance on its own)");
-    if (h->two_step)
+    if (h->two_step || h->persistent)
         return fail(GPE_ERR_UNSUPPORTED, "gpe_link_z: slabs exchange halos between half-steps; use a kernel "
                                          "variant that advances a half-step per launch");
     const int n = h->cfg.num_instances;
@@ -1536,6 +1634,11 @@ int32_t gpe_variant_count(void) { return fused_tile_count(); }
 int32_t gpe_variant_half_steps(int32_t variant)
 {
     return (variant >= 0 && variant < fused_tile_count()) ? fused_half_steps(variant) : 0;
+}
+
+int32_t gpe_variant_kind(int32_t variant)
+{
+    return (variant >= 0 && variant < fused_tile_count()) ? fused_variant_kind(variant) : -1;
 }
 
 static gpe_status gpe_variant_describe_impl(int32_t variant, int32_t *tile_x, int32_t *tile_y, int32_t *stages,

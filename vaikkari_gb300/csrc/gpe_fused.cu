@@ -60,6 +60,7 @@
 
 #include <string>
 
+#include "gpe_fused_core.cuh"
 #include "gpe_internal.h"
 
 namespace gpe {
@@ -86,224 +87,6 @@ struct FusedArgs {
     int inject_skip_plane;  // test hook: plane the producer of work item 0 withholds (-1 = none)
 };
 
-template <typename T> struct Acc;
-template <> struct Acc<double> {
-    double s = 0.0;
-    __device__ void add(double v) { s += v; }
-    __device__ double value() const { return s; }
-};
-template <> struct Acc<float> {  // compensated FP32
-    float s = 0.f, c = 0.f;
-    __device__ void add(float v)
-    {
-        const float y = __fsub_rn(v, c);
-        const float t = __fadd_rn(s, y);
-        c = __fsub_rn(__fsub_rn(t, s), y);
-        s = t;
-    }
-    __device__ double value() const { return double(s) - double(c); }
-};
-
-// ---- PTX helpers -----------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ uint64_t global_ns()
-{
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Bounded wait: gives up after about one second of wall time.
-constexpr uint64_t kWaitLimitNs = 1000000000ull;
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
-{
-    if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = global_ns();
-    while (true) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (global_ns() - t0 > kWaitLimitNs) return false;
-    }
-}
-
-__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
-                                            uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-        "[%6];" ::"r"(dst),
-        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
-        : "memory");
-}
-
-constexpr int kErrTimeout = 1;
-
-template <typename T, int TX, int TY, bool COMP = false>
-struct FusedShape {
-    using T2 = typename Cplx<T>::type;
-    static constexpr int NT = TX * TY;       // consumer threads
-    static constexpr int NTHREADS = NT + 32; // plus the producer warp
-    static constexpr int BW = TX + 4;        // x0-2 .. x0+TX+1
-    static constexpr int BH = TY + 2;        // y0-1 .. y0+TY
-    static constexpr int SLOT = BW * BH;
-    static constexpr int HALO_BYTES = 2 * SLOT * (int)sizeof(T2);
-    static constexpr int NEXT_BYTES = 2 * TX * TY * (int)sizeof(T2);
-    static constexpr int NEXT_OFF = ((HALO_BYTES + 127) / 128) * 128;
-    // compensated storage: the residual tile, columns x0-2 .. x0+TX+1 (its copy
-    // starts on the 16-byte boundary of column x0-2), TY rows, both slots
-    static constexpr int LO_W = TX + 4;
-    static constexpr int LO_BYTES = COMP ? 2 * TY * LO_W * 4 : 0;
-    static constexpr int LO_OFF = ((NEXT_OFF + NEXT_BYTES + 127) / 128) * 128;
-    static constexpr int STAGE_BYTES = ((LO_OFF + LO_BYTES + 127) / 128) * 128;
-    static constexpr int XE = (int)sizeof(T2) / 8;  // 8-byte TMA elements per complex
-};
-
-template <typename T, int TX, int TY, int STAGES, bool COMP = false>
-int fused_smem_bytes(int zcmax)
-{
-    return STAGES * FusedShape<T, TX, TY, COMP>::STAGE_BYTES + 128 /* align */ + 16 * STAGES /* barriers */ +
-           2 * zcmax * (int)sizeof(T) + 16;
-}
-
-// FP64 values need twice the registers: ask for half the resident CTAs.
-template <typename T, int MINB> struct MinBlocks {
-    static constexpr int value = sizeof(T) == 8 ? (MINB + 1) / 2 : MINB;
-};
-
-// Programmatic dependent launch (sm_90 and later).
-__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-
-// Launch with programmatic stream serialisation: the kernel may begin while the
-// previous kernel on the stream drains, and waits for it in grid_dependency_wait.
-template <typename Kern, typename Args>
-static cudaError_t launch_pdl(Kern kern, int grid, int threads, int bytes, cudaStream_t s, const Args &a)
-{
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.gridDim = dim3(unsigned(grid));
-    cfg.blockDim = dim3(unsigned(threads));
-    cfg.dynamicSmemBytes = size_t(bytes);
-    cfg.stream = s;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kern, a);
-}
-
-// Packed FP32 pairs (add / mul / fma .rn.f32x2, sm_100 and later): each lane is
-// the IEEE operation of that lane, so a complex sum, or a complex times a real
-// factor, rounds exactly as the two scalar operations do, in one instruction.
-__device__ __forceinline__ float2 f2_add(float2 a, float2 b)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
-        "add.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-
-__device__ __forceinline__ float2 f2_mul(float2 a, float2 b)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
-        "mul.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-
-__device__ __forceinline__ float2 f2_sub(float2 a, float2 b)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
-        "sub.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-
-__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 a, b, c, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
-        "mov.b64 c, {%6, %7};\n\tfma.rn.f32x2 d, a, b, c;\n\tmov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-    return r;
-}
-
-// Complex sums and dt*H psi (gpe_device.cuh's hpsi, two classes) with the same
-// rounded operations, packed for FP32.
-template <typename T> struct Ops;
-template <> struct Ops<double> {
-    static __device__ __forceinline__ double2 add(double2 a, double2 b) { return c_add<double>(a, b); }
-    static __device__ __forceinline__ void hpsi(double2 p, const double2 *S, const double *L, double L0, double vdt,
-                                                double gdt, double &hx, double &hy, double &nrm)
-    {
-        gpe::hpsi<double, 2>(p, S, L, L0, vdt, gdt, hx, hy, nrm);
-    }
-};
-template <> struct Ops<float> {
-    static __device__ __forceinline__ float2 add(float2 a, float2 b) { return f2_add(a, b); }
-    static __device__ __forceinline__ void hpsi(float2 p, const float2 *S, const float *L, float L0, float vdt,
-                                                float gdt, float &hx, float &hy, float &nrm)
-    {
-        nrm = d_fma(p.x, p.x, d_mul(p.y, p.y));
-        const float c = d_fma(gdt, nrm, d_add(L0, vdt));
-        float2 a = f2_mul(make_float2(L[0], L[0]), S[0]);
-        a = f2_fma(make_float2(L[1], L[1]), S[1], a);
-        const float2 h = f2_fma(make_float2(c, c), p, a);
-        hx = h.x;
-        hy = h.y;
-    }
-};
-
-// Compensated update of one value (MODE 2): returns the new stored value and
-// replaces *lo (bf16 pair, x in the low half) with the new residual.
-__device__ __forceinline__ float2 integrate_comp(float2 n, float hx, float hy, uint32_t &lo)
-{
-    __nv_bfloat162 lb;
-    memcpy(&lb, &lo, 4);
-    const float2 t = f2_add(__bfloat1622float2(lb), make_float2(hy, -hx));
-    const float2 s = f2_add(n, t);
-    const float2 b = f2_sub(s, n);
-    const float2 r = f2_add(f2_sub(n, f2_sub(s, b)), f2_sub(t, b));
-    lb = __floats2bfloat162_rn(r.x, r.y);
-    memcpy(&lo, &lb, 4);
-    return s;
-}
-
 template <typename T, int TX, int TY, int MODE, int POT, int STAGES, int MINB>
 __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_bcc2_kernel(const FusedArgs a)
 {
@@ -320,7 +103,7 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
     const uint32_t full = base + STAGES * S::STAGE_BYTES;
     const uint32_t empty = full + 8 * STAGES;
     T *const ztab = (T *)(gbase + STAGES * S::STAGE_BYTES + 16 * STAGES);
-    __shared__ int abort_flag;
+    __shared__ volatile int abort_flag;
     __shared__ double row_sums[4];  // imaginary time: this work item's four sums
 
     const int tid = threadIdx.x;
@@ -328,7 +111,6 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
     const int it = blockIdx.x;
     const WorkItem w = a.items[it];
     const InstDev &d = a.inst[w.inst];
-    const int nplanes = w.z1 - w.z0 + 2;  // planes z0-1 .. z1
     const int nz = d.nz;
 
     if (tid == 0) {
@@ -356,174 +138,20 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
     if (warp == NWARPS - 1) {
         // ---- producer warp ------------------------------------------------
         if (lane == 0) {
-            const CUtensorMap *halo = a.maps + 4 * w.inst + 2 * a.src;
-            const CUtensorMap *inner = a.maps + 4 * w.inst + 2 * (1 - a.src) + 1;
             int issued = 0;
-            for (int k = 0; k < nplanes; k++) {
-                const int st = k % STAGES;
-                if (k >= STAGES) {
-                    bool ok = mbar_try_wait(empty + 8 * st, ((k / STAGES) - 1) & 1);
-                    const uint64_t t0 = global_ns();
-                    while (!ok && !*(volatile int *)&abort_flag && global_ns() - t0 <= kWaitLimitNs)
-                        ok = mbar_try_wait(empty + 8 * st, ((k / STAGES) - 1) & 1);
-                    if (!ok) {
-                        atomicExch(a.err, kErrTimeout);
-                        abort_flag = 1;
-                        break;
-                    }
-                }
-                if (a.inject_skip_plane == k && it == 0) {
-                    // test hook (gpe_debug_inject): withhold this plane's copy so that
-                    // the consumers' bounded wait runs out
-                    issued = k;
-                    break;
-                }
-                const bool with_next = REAL && (k >= 2);
-                mbar_arrive_expect_tx(full + 8 * st, S::HALO_BYTES + (with_next ? S::NEXT_BYTES + S::LO_BYTES : 0));
-                // padded coordinates: x0-2 -> x0, y0-1 -> y0, plane q -> q+1
-                tma_load_4d(base + st * S::STAGE_BYTES, halo, w.x0 * S::XE, w.y0, 0, w.z0 + k, full + 8 * st);
-                if (with_next)  // next field, interior tile of plane q-1 = z0+k-2
-                    tma_load_4d(base + st * S::STAGE_BYTES + S::NEXT_OFF, inner, (w.x0 + 2) * S::XE, w.y0 + 1, 0,
-                                w.z0 + k - 1, full + 8 * st);
-                if (MODE == 2 && with_next)  // its residuals, from padded column x0 (16-byte aligned)
-                    tma_load_4d(base + st * S::STAGE_BYTES + S::LO_OFF, a.lo_maps + 2 * w.inst + (1 - a.src), w.x0,
-                                w.y0 + 1, 0, w.z0 + k - 1, full + 8 * st);
-                issued = k + 1;
-            }
-            if (abort_flag) {
-                // let the copies this CTA issued land (bounded) before it exits
-                for (int k = (issued > STAGES ? issued - STAGES : 0); k < issued; k++)
-                    mbar_wait_bounded(full + 8 * (k % STAGES), (k / STAGES) & 1);
-            }
+            produce_item<T, TX, TY, MODE, STAGES, false>(w, 0, a.src, a.maps, a.lo_maps, base, full, empty,
+                                                        it == 0 ? a.inject_skip_plane : -1, a.err, &abort_flag,
+                                                        issued);
+            if (abort_flag) drain_ring<STAGES>(issued, full);  // let this CTA's copies land before it exits
         }
     } else {
         // ---- consumer warps ----------------------------------------------
-        const int tx = tid % TX, ty = tid / TX;
-        const int x = w.x0 + tx, y = w.y0 + ty;
-        const bool valid = (x < d.nx) && (y < d.ny);
-        const long long zstride = d.zstride, plane = d.plane;
-        const long long col = field_index(d, 0, x, y, 0);
-        const long long voff = d.vbase - d.base;
         const T sig = (MODE == 1) ? T(a.imag[w.inst].sigma) : T(1);
-        const T Lw[2] = {T(d.Lc[0]), T(d.Lc[1])};
-        const T L0 = T(d.L0), gdt = T(d.gdt);
-        T2 *__restrict__ nxt = (T2 *)a.next;
-        uint32_t *__restrict__ nlo = a.next_lo;
-        uint32_t lo0 = 0u, lo1 = 0u;  // MODE 2: residuals of the output plane
-        const T *__restrict__ vpot = (const T *)a.vpot;
-        T vxy0 = T(0), vxy1 = T(0);
-        if (POT == GPE_POTENTIAL_TRAP && valid) {
-            const T *tx_ = vpot + d.vbase;
-            const T *ty_ = tx_ + 2ll * d.nx;
-            vxy0 = d_add(tx_[x], ty_[y]);
-            vxy1 = d_add(tx_[d.nx + x], ty_[d.ny + y]);
-        }
-        const int zl = w.z1 - w.z0;
-
-        // carried state (see the summation order above)
-        const T2 zero2 = {T(0), T(0)};
-        T2 cm = zero2, cc = zero2, bm = zero2, bc = zero2;  // own C, B at planes z-1, z
-        T2 axyC = zero2, axyB = zero2;                        // in-plane axial sums at plane z
-        T2 bBp = zero2, sd0 = zero2, bCc = zero2;             // bB(z), Sd of slot 0 at z, bC(z)
-        Acc<T> s0, s1, s2, s3;
-        const int lx = tx + 2, ly = ty + 1;
-        for (int k = 0; k < nplanes; k++) {
-            const int st = k % STAGES;
-            if (!mbar_wait_bounded(full + 8 * st, (k / STAGES) & 1)) {
-                atomicExch(a.err, kErrTimeout);
-                abort_flag = 1;
-                break;
-            }
-            const unsigned char *sb = gbase + st * S::STAGE_BYTES;
-            const T2 *Cp = (const T2 *)sb;
-            const T2 *Bp = Cp + S::SLOT;
-            auto at = [&](const T2 *P, int dx, int dy) -> T2 {
-                T2 v = P[(ly + dy) * S::BW + lx + dx];
-                if (MODE == 1) v = c_scale<T>(sig, v);
-                return v;
-            };
-            const T2 qC = at(Cp, 0, 0), qCxm = at(Cp, -1, 0), qCxp = at(Cp, 1, 0), qCym = at(Cp, 0, -1),
-                     qCyp = at(Cp, 0, 1), qCpp = at(Cp, 1, 1);
-            const T2 qB = at(Bp, 0, 0), qBxm = at(Bp, -1, 0), qBxp = at(Bp, 1, 0), qBym = at(Bp, 0, -1),
-                     qByp = at(Bp, 0, 1), qBmm = at(Bp, -1, -1);
-            T2 n0 = zero2, n1 = zero2;
-            if (REAL && k >= 2) {
-                const T2 *Np = (const T2 *)(sb + S::NEXT_OFF);
-                n0 = Np[ty * TX + tx];
-                n1 = Np[TX * TY + ty * TX + tx];
-                if (MODE == 2) {
-                    const uint32_t *Lp = (const uint32_t *)(sb + S::LO_OFF);
-                    lo0 = Lp[ty * S::LO_W + tx + 2];
-                    lo1 = Lp[(TY + ty) * S::LO_W + tx + 2];
-                }
-            }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(empty + 8 * st);  // this warp is done with stage st
-
-            // sums of plane q = z0-1+k
-            const T2 bBq = Ops<T>::add(Ops<T>::add(qBmm, qBym), Ops<T>::add(qBxm, qB));
-            const T2 bCq = Ops<T>::add(Ops<T>::add(qC, qCxp), Ops<T>::add(qCyp, qCpp));
-            const T2 axyCq = Ops<T>::add(Ops<T>::add(qCxm, qCxp), Ops<T>::add(qCym, qCyp));
-            const T2 axyBq = Ops<T>::add(Ops<T>::add(qBxm, qBxp), Ops<T>::add(qBym, qByp));
-            const T2 sd0q = Ops<T>::add(bBp, bBq);  // Sd of slot 0 at plane q
-
-            if (k >= 2 && valid) {
-                const int z = w.z0 + k - 2;  // output plane (q - 1)
-                T2 S2[2];
-                T hx, hy, nrm;
-                T v0, v1;
-                if (POT == GPE_POTENTIAL_TRAP) {
-                    v0 = d_add(vxy0, ztab[z - w.z0]);
-                    v1 = d_add(vxy1, ztab[zl + z - w.z0]);
-                } else {
-                    const long long i0 = col + z * zstride;
-                    v0 = vpot[i0 + voff];
-                    v1 = vpot[i0 + plane + voff];
-                }
-                // slot 0 (cube corner)
-                S2[0] = sd0;
-                S2[1] = Ops<T>::add(Ops<T>::add(cm, qC), axyC);
-                Ops<T>::hpsi(cc, S2, Lw, L0, v0, gdt, hx, hy, nrm);
-                T2 o0;
-                if constexpr (MODE == 2) o0 = integrate_comp(n0, hx, hy, lo0);
-                else o0 = integrate<T, MODE>(n0, cc, hx, hy);
-                if (MODE == 1) {
-                    s0.add(nrm);
-                    s1.add(d_fma(cc.x, hx, d_mul(cc.y, hy)));
-                    s2.add(d_mul(nrm, nrm));
-                    s3.add(d_fma(o0.x, o0.x, d_mul(o0.y, o0.y)));
-                }
-                // slot 1 (cube centre)
-                S2[0] = Ops<T>::add(bCc, bCq);
-                S2[1] = Ops<T>::add(Ops<T>::add(bm, qB), axyB);
-                Ops<T>::hpsi(bc, S2, Lw, L0, v1, gdt, hx, hy, nrm);
-                T2 o1;
-                if constexpr (MODE == 2) o1 = integrate_comp(n1, hx, hy, lo1);
-                else o1 = integrate<T, MODE>(n1, bc, hx, hy);
-                if (MODE == 1) {
-                    s0.add(nrm);
-                    s1.add(d_fma(bc.x, hx, d_mul(bc.y, hy)));
-                    s2.add(d_mul(nrm, nrm));
-                    s3.add(d_fma(o1.x, o1.x, d_mul(o1.y, o1.y)));
-                }
-                const long long i0 = col + z * zstride;
-                nxt[i0] = o0;
-                nxt[i0 + plane] = o1;
-                if (MODE == 2) {
-                    nlo[i0] = lo0;
-                    nlo[i0 + plane] = lo1;
-                }
-            }
-            cm = cc;
-            cc = qC;
-            bm = bc;
-            bc = qB;
-            axyC = axyCq;
-            axyB = axyBq;
-            bBp = bBq;
-            sd0 = sd0q;
-            bCc = bCq;
-        }
+        Acc<T> acc[4];
+        consume_item<T, TX, TY, MODE, POT, STAGES, false>(w, d, 0, gbase, full, empty, a.next, a.next_lo, a.vpot,
+                                                          ztab, w.z1 - w.z0, w.z0, sig, acc, tid, lane, a.err,
+                                                          &abort_flag);
+        Acc<T> &s0 = acc[0], &s1 = acc[1], &s2 = acc[2], &s3 = acc[3];
         if (MODE == 1) {
             double v[4] = {s0.value(), s1.value(), s2.value(), s3.value()};
 #pragma unroll
@@ -678,21 +306,6 @@ struct TwoStepArgs {
     int *err;
     int inject_skip_plane;
 };
-
-// Barrier of threads 0..n-1 on barrier id, returning whether any of them passed v.
-__device__ __forceinline__ bool bar_any(int id, int n, bool v)
-{
-    uint32_t r;
-    asm volatile(
-        "{\n\t.reg .pred q, p;\n\t"
-        "setp.ne.u32 q, %1, 0;\n\t"
-        "bar.red.or.pred p, %2, %3, q;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(r)
-        : "r"(v ? 1u : 0u), "r"(id), "r"(n)
-        : "memory");
-    return r != 0;
-}
 
 template <typename T, int TX, int TY, int POT, int STAGES, int MINB>
 __global__ void __launch_bounds__(TwoStepShape<T, TX, TY>::NTHREADS, MinBlocks<T, MINB>::value)
@@ -953,28 +566,36 @@ static const Variant kTwoVariants[] = {
 };
 constexpr int kOneCount = int(sizeof(kVariants) / sizeof(kVariants[0]));
 constexpr int kTwoCount = int(sizeof(kTwoVariants) / sizeof(kTwoVariants[0]));
+// The persistent kernel's variants (gpe_persistent.cu) follow the two-step ones.
 
-static const Variant &variant_of(int tile)
+int fused_tile_count() { return kOneCount + kTwoCount + persistent_variant_count(); }
+int fused_variant_kind(int tile)
 {
-    if (tile < 0 || tile >= kOneCount + kTwoCount) tile = 0;
-    return tile < kOneCount ? kVariants[tile] : kTwoVariants[tile - kOneCount];
+    if (tile >= kOneCount && tile < kOneCount + kTwoCount) return kVariantTwoStep;
+    if (tile >= kOneCount + kTwoCount && tile < fused_tile_count()) return kVariantPersistent;
+    return kVariantHalfStep;
 }
-
-int fused_tile_count() { return kOneCount + kTwoCount; }
-int fused_half_steps(int tile) { return (tile >= kOneCount && tile < kOneCount + kTwoCount) ? 2 : 1; }
-void fused_tile_shape(int tile, int *tx, int *ty)
-{
-    *tx = variant_of(tile).tx;
-    *ty = variant_of(tile).ty;
-}
+int fused_persistent_index(int tile) { return tile - kOneCount - kTwoCount; }
+int fused_half_steps(int tile) { return fused_variant_kind(tile) == kVariantTwoStep ? 2 : 1; }
 
 void fused_variant(int tile, int *tx, int *ty, int *stages, int *minb)
 {
-    const Variant &v = variant_of(tile);
+    if (tile < 0 || tile >= fused_tile_count()) tile = 0;
+    if (fused_variant_kind(tile) == kVariantPersistent) {
+        persistent_variant(fused_persistent_index(tile), tx, ty, stages, minb);
+        return;
+    }
+    const Variant &v = tile < kOneCount ? kVariants[tile] : kTwoVariants[tile - kOneCount];
     *tx = v.tx;
     *ty = v.ty;
     *stages = v.stages;
     *minb = v.minb;
+}
+
+void fused_tile_shape(int tile, int *tx, int *ty)
+{
+    int st, mb;
+    fused_variant(tile, tx, ty, &st, &mb);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (the library

@@ -125,6 +125,34 @@ void fused_variant(int tile, int *tx, int *ty, int *stages, int *minb);
 gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *field_arena, int tile);
 // GPE_FP32C: the 4-D map of one field's residual array (32-bit words).
 gpe_status make_residual_map(void *out_map, const InstDev &d, void *lo_arena, int tile);
+// Variant kinds of gpe_config.tile: one half-step per launch, a whole leapfrog
+// step per launch (two-step), or the persistent kernel (many half-steps per launch).
+enum VariantKind { kVariantHalfStep = 0, kVariantTwoStep = 1, kVariantPersistent = 2 };
+int fused_variant_kind(int tile);
+int fused_persistent_index(int tile);  // index into the persistent kernel's own variant list
+
+// The persistent real-time kernel (gpe_persistent.cu): one cooperative launch
+// advances every instance by half_steps half-steps (odd <- even first), each
+// work item waiting only for its neighbouring items' epoch words.
+struct PersistLaunch {
+    int precision, potential, variant, comp, device;
+    const InstDev *inst;
+    const WorkItem *items;
+    int num_items;
+    const void *maps, *lo_maps;
+    void *field[2];
+    void *lo[2];
+    const void *vpot;
+    const int *nbr_begin, *nbr;
+    unsigned int *done;
+    unsigned int epoch0;
+    int half_steps;
+    int *err;
+    int inject_skip_plane;
+};
+cudaError_t launch_persistent(const PersistLaunch &l, cudaStream_t s, int *grid);
+int persistent_variant_count();
+void persistent_variant(int k, int *tx, int *ty, int *stages, int *minb);
 
 struct ObsLaunch {
     int lattice, precision, potential;

@@ -208,6 +208,8 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_time_steps.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]
     lib.gpe_variant_half_steps.restype = C.c_int32
     lib.gpe_variant_half_steps.argtypes = [C.c_int32]
+    lib.gpe_variant_kind.restype = C.c_int32
+    lib.gpe_variant_kind.argtypes = [C.c_int32]
     lib.gpe_link_z.restype = st
     lib.gpe_link_z.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
     lib.gpe_debug_inject.restype = st
@@ -309,7 +311,8 @@ def variants() -> List[dict]:
         t = [C.c_int32() for _ in range(4)]
         _check(lib.gpe_variant_describe(v, *[C.byref(x) for x in t]), "gpe_variant_describe")
         out.append({"tile": v, "tx": t[0].value, "ty": t[1].value, "stages": t[2].value, "min_blocks": t[3].value,
-                    "half_steps": lib.gpe_variant_half_steps(v)})
+                    "half_steps": lib.gpe_variant_half_steps(v), "kind": lib.gpe_variant_kind(v),
+                    "persistent": lib.gpe_variant_kind(v) == 2})
     return out
 
 
