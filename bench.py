@@ -67,12 +67,17 @@ def _profile_traffic(name):
     return out
 
 
-def roofline_block(verts, bytes_per_vertex_launch, per_launch_s, kernel, profile, variant):
-    """Roofline of the dominant kernel: achieved = algorithmic bytes per launch
-    / average launch duration (CUDA events); traffic from the ncu summary of the
-    same kernel variant on this workload (null if the profiled variant differs)."""
+def roofline_block(verts, bytes_per_vertex_step, steps, window_s, launches, kernel, profile, variant):
+    """Roofline of the dominant kernel, the only kernel in the timed window:
+    achieved = algorithmic bytes per launch / average launch duration, i.e. the
+    window's algorithmic bytes (vertices x bytes per vertex-step x steps) over
+    the window's device time (CUDA events), whether the window holds two
+    launches per step or one persistent launch; traffic from the ncu summary of
+    the same kernel variant on this workload (null if the profiled variant
+    differs)."""
     peak, peak_kind = _peaks()
-    achieved = verts * bytes_per_vertex_launch / per_launch_s / 1e9
+    window_bytes = verts * bytes_per_vertex_step * steps
+    achieved = window_bytes / window_s / 1e9
     prof = _profile_traffic(profile)
     same = prof["variant"] == variant
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -80,8 +85,8 @@ def roofline_block(verts, bytes_per_vertex_launch, per_launch_s, kernel, profile
             "traffic_source": (f"ncu capture summarised in {prof['source']} (variant {prof['variant']}, "
                                f"full batch, one launch)" if same else
                                f"none for variant {variant}: {prof['source']} holds variant {prof['variant']}"),
-            "algorithmic_bytes_per_vertex_step": 2 * bytes_per_vertex_launch,
-            "algorithmic_bytes_per_launch": verts * bytes_per_vertex_launch,
+            "algorithmic_bytes_per_vertex_step": bytes_per_vertex_step,
+            "algorithmic_bytes_per_launch": window_bytes / max(launches, 1), "launches_per_window": launches,
             "peak_source": f"{peak_kind} hbm_gbs (of {peak_kind})", "kernel": kernel}
 
 
@@ -441,8 +446,7 @@ def run_ours(args):
         ms = statistics.median(times)
         ms_max = _max_over_ranks(dist, ms, device=dev)
         value = job_value(verts_job, args.steps, ms_max)
-        per_launch_s = (ms * 1e-3) / max(launches, 1)
-        roof = roofline_block(verts, bytes_vs / 2, per_launch_s,
+        roof = roofline_block(verts, bytes_vs, args.steps, ms * 1e-3, launches,
                               "fused_bcc2_kernel<float, MODE 2 (compensated)>" if comp_main
                               else "fused_bcc2_kernel<float, MODE 0>",
                               "fused_bcc2_fp32c_batch64.md" if comp_main else "fused_bcc2_batch64.md", tile)
@@ -455,8 +459,13 @@ def run_ours(args):
     # observables and downloads every field (one batched call).  One untimed
     # call first: the handle allocates the transfers' device staging, copy
     # stream and events on first use.  e2e = the median of several calls.
+    # Host fields are float in both storages (a GPE_FP32C handle takes float
+    # with gpe_set_host_precision; its residual starts at zero, and the
+    # accuracy block measures that path too).
+    if comp_main:
+        st.set_host_precision(Precision.FP32)
     pinned_e, pinned_o = [], []
-    tt = torch.float64 if comp_main else torch.float32
+    tt = torch.float32
     for e, o in zip(evens, odds):
         pe = torch.empty(e.shape, dtype=tt, pin_memory=True).numpy()
         po = torch.empty(o.shape, dtype=tt, pin_memory=True).numpy()
@@ -544,6 +553,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h_job / args.steps, "h2d_bytes_per_call": h2d_job,
                     "d2h_bytes_per_call": d2h_job, "steps_per_call": args.steps,
                     "seconds_median": e2e_s, "seconds_all": calls, "calls": len(calls), "finite": finite,
+                    "host_format": "float32 complex (8 B per value and field)",
                     "call": "gpe_upload_many (pinned host) + gpe_step + gpe_observables_get + gpe_download_many"},
             "cpu_baseline": cpu,
             "accuracy": acc,
@@ -565,29 +575,34 @@ def accuracy_block(conds, insts, device, timed="fp32c"):
     from vaikkari_gb300.gpe import Kernel, Lattice, Potential, Precision, Stepper
     steps = 1000
     outs = {}
-    for prec, dt_ in ((Precision.FP32, np.float32), (Precision.FP64, np.float64), (Precision.FP32C, np.float64)):
+    runs = ((Precision.FP32, np.float32, "fp32"), (Precision.FP64, np.float64, "fp64"),
+            (Precision.FP32C, np.float64, "fp32c"), (Precision.FP32C, np.float32, "fp32c_host_fp32"))
+    for prec, dt_, tag in runs:
         st = Stepper(insts, lattice=Lattice.BCC2, precision=prec, kernel=Kernel.FUSED, potential=Potential.TRAP,
                      graph_steps=100, device=device)
+        if prec == Precision.FP32C and dt_ == np.float32:
+            st.set_host_precision(Precision.FP32)  # the e2e call's host format
         prepare_fields(st, conds, dt_)
         o0 = st.observables(0)
         st.step(steps)
         o1 = st.observables(0)
         fields = [st.download(i, odd=False)[0].astype(np.float64) for i in range(len(insts))]
         st.close()
-        outs[prec] = (o0, o1, fields)
-    f64 = outs[Precision.FP64][2]
+        outs[tag] = (o0, o1, fields)
+    f64 = outs["fp64"][2]
     den = sum(float(np.sum(b ** 2)) for b in f64)
-    n64 = [o["norm"] for o in outs[Precision.FP64][1]]
-    e64 = [o["energy"] for o in outs[Precision.FP64][1]]
-    n0 = [o["norm"] for o in outs[Precision.FP64][0]]
+    n64 = [o["norm"] for o in outs["fp64"][1]]
+    e64 = [o["energy"] for o in outs["fp64"][1]]
+    n0 = [o["norm"] for o in outs["fp64"][0]]
     res = {"steps": steps, "reference": "FP64 run of the same scheme (fused kernel, same inputs)",
-           "max_norm_drift_fp64_scheme": max(abs(a - b) / b for a, b in zip(n64, n0))}
-    for tag, prec in (("fp32", Precision.FP32), ("fp32c", Precision.FP32C)):
-        f = outs[prec][2]
+           "max_norm_drift_fp64_scheme": max(abs(a - b) / b for a, b in zip(n64, n0)),
+           "fp32c_host_fp32": "GPE_FP32C started from float fields and read back as float (the e2e host format)"}
+    for tag in ("fp32", "fp32c", "fp32c_host_fp32"):
+        f = outs[tag][2]
         num = sum(float(np.sum((a - b) ** 2)) for a, b in zip(f, f64))
         per = [math.sqrt(float(np.sum((a - b) ** 2)) / float(np.sum(b ** 2))) for a, b in zip(f, f64)]
-        nn = [o["norm"] for o in outs[prec][1]]
-        ee = [o["energy"] for o in outs[prec][1]]
+        nn = [o["norm"] for o in outs[tag][1]]
+        ee = [o["energy"] for o in outs[tag][1]]
         res[f"rel_l2_{tag}_vs_fp64"] = math.sqrt(num / den)
         res[f"max_instance_rel_l2_{tag}"] = max(per)
         res[f"instances_over_1e-5_{tag}"] = sum(1 for v in per if v > 1e-5)
@@ -628,7 +643,7 @@ def storage_block(conds, insts, device, steps, warmup, window_seconds, prec, tun
     verts = sum(i.nx * i.ny * i.nz for i in insts) * 2
     st.close()
     bytes_vs = BYTES_PER_VERTEX_STEP_COMP if comp else BYTES_PER_VERTEX_STEP
-    roof = roofline_block(verts, bytes_vs / 2, (ms * 1e-3) / max(launches, 1),
+    roof = roofline_block(verts, bytes_vs, steps, ms * 1e-3, launches,
                           "fused_bcc2_kernel<float, MODE 2 (compensated)>" if comp else
                           "fused_bcc2_kernel<float, MODE 0>",
                           "fused_bcc2_fp32c_batch64.md" if comp else "fused_bcc2_batch64.md", tile)
@@ -786,11 +801,13 @@ def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1, latt
             "accuracy": acc, "cpu_baseline": _cpu_config_rate(conds, lattice=lattice)}
 
 
-def _windowed_rate(st, verts, steps, sample_clocks, prec, kern, tile, seconds=1.0):
+def _windowed_rate(st, verts, steps, sample_clocks, prec, kern, tile, seconds=1.0, imaginary=False):
     """Vertex-updates/s of a prepared stepper: median of windows of `steps`
     steps after one untimed call; the roofline at the algorithmic bytes of the
-    trap form (24 B per value and half-step in FP32, 32 B in FP32C, 48 B in
-    FP64; the two-step variants move 16 / 32 B per value and half-step)."""
+    trap form (real time: 24 B per value and half-step in FP32, 32 B in FP32C,
+    48 B in FP64; the two-step variants move 16 / 32 B per value and half-step;
+    imaginary time: one pass per step reading psi and writing the next field,
+    16 B per value in FP32, 32 B in FP64)."""
     import torch
     from vaikkari_gb300.gpe import Precision, variants
     st.step(3)
@@ -807,8 +824,10 @@ def _windowed_rate(st, verts, steps, sample_clocks, prec, kern, tile, seconds=1.
         if sample_clocks:
             clk.__exit__()
     ms = statistics.median(times)
-    half_steps = 2 * steps
+    half_steps = steps if imaginary else 2 * steps
     per_value_half = {Precision.FP32: 24, Precision.FP32C: 32, Precision.FP64: 48}[prec]
+    if imaginary:
+        per_value_half = {Precision.FP32: 16, Precision.FP64: 32}[prec]
     vinfo = {v["tile"]: v for v in variants()}
     if kern.name == "FUSED" and tile in vinfo and vinfo[tile]["half_steps"] == 2:
         per_value_half = per_value_half * 2 // 3  # both fields read once and written once per step
@@ -846,10 +865,10 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1, latti
         for i, c in enumerate(conds):
             st.upload(i, c.psi)
         t0 = time.perf_counter()
-        # FP64 runs to the criterion.  The FP32 field stops changing once the
-        # per-step update drops below its rounding, which freezes mu and trips a
-        # 1e-9 criterion spuriously, so FP32 runs the same number of steps.
-        lim, crit = (max_steps, tol) if prec == Precision.FP64 else (steps64, 0.0)
+        # Both run to the criterion: FP64 tests |dmu| < tol every step; FP32
+        # tests the mean |dmu| per step over each chunk of 100 steps with mu from
+        # the FP64 observables (gpe_imaginary_time).
+        lim, crit = max_steps, tol
         steps, conv, mu = st.imaginary_time(lim, crit)
         st.synchronize()
         wall = time.perf_counter() - t0
@@ -866,14 +885,14 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1, latti
            "rel_mu_fp32_vs_fp64": max(abs(a - b) / abs(b) for a, b in zip(r32["mu_obs"], r64["mu_obs"])),
            "rel_energy_fp32_vs_fp64": max(abs(a - b) / abs(b) for a, b in zip(r32["energy"], r64["energy"])),
            "rel_l2_fp32_vs_fp64": _rel_l2_phase(r32["fields"], r64["fields"])}
-    # throughput of the imaginary-time step (FP32), device time
+    # throughput of the imaginary-time step (FP32), device time: median of
+    # windows of 1000 steps (ten graph replays), clocks sampled over them
     st = _stepper(conds, Precision.FP32, kern, Mode.IMAGINARY, tile=tile, zchunk=zchunk, lattice=lattice)
     for i, c in enumerate(conds):
         st.upload(i, c.psi)
-    st.time_steps(100)
-    ms = min(st.time_steps(1000) for _ in range(2))
+    rate, roof, clocks = _windowed_rate(st, verts, 1000, True, Precision.FP32, kern, tile, imaginary=True)
     st.close()
-    return {"metric": METRIC, "value": verts * 1000 / (ms * 1e-3), "unit": METRIC, "dtype": "f32",
+    return {"metric": METRIC, "value": rate, "unit": METRIC, "dtype": "f32", "roofline": roof, "clocks": clocks,
             "config": {"workload": name, "lattice": lattice.name, "instances": len(insts), "vertices": verts,
                        "dt": insts[0].dt, "tol": tol, "max_steps": max_steps, "mode": "imaginary", "variant": tile,
                        "zchunk": zchunk, "kernel": kern.name.lower()},

@@ -207,6 +207,16 @@ gpe_status gpe_upload_many(gpe_handle h, int32_t count, const int32_t *instances
 gpe_status gpe_download_many(gpe_handle h, int32_t count, const int32_t *instances, void *const *even,
                              void *const *odd);
 
+/* Element type of the host field arrays of gpe_upload/gpe_download and their
+ * batched forms.  A GPE_FP32C handle exchanges double by default (each value
+ * split into its FP32 value and bf16 residual on upload, recombined on
+ * download); with GPE_FP32 it exchanges float: an upload sets the residual to
+ * zero, a download rounds value + residual to float once.  That halves the host
+ * link traffic for callers whose data are single precision; the residual still
+ * keeps the time integration's rounding errors from accumulating.  Other
+ * handles accept only their own precision.  No counterpart in the reference. */
+gpe_status gpe_set_host_precision(gpe_handle h, int32_t precision);
+
 /* Real time: advances every instance by `steps` leapfrog steps (odd <- even,
  * then even <- odd; GPUGrossPitaevskii_BCC.cu:475-481).  Imaginary time:
  * `steps` normalised Euler steps.  Asynchronous on the handle's stream. */
@@ -218,8 +228,14 @@ gpe_status gpe_synchronize(gpe_handle h);
 gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out);
 
 /* Imaginary time until |mu_k - mu_{k-1}| < tol for every instance or max_steps.
- * Steps run in graph-sized chunks; convergence is checked on the device each step
- * and the host polls between chunks.  Outputs may be NULL. */
+ * Steps run in graph-sized chunks of G steps (gpe_config.graph_steps, 100 by
+ * default).  GPE_FP64: mu comes from the reductions fused into every step and
+ * the test runs on the device each step; the host polls between chunks.
+ * GPE_FP32: mu of the normalised field is taken from the FP64 observables after
+ * each chunk, and the test is |mu_k - mu_{k-G}| < G * tol (the mean change per
+ * step over the chunk), because the per-step change of an FP32 field's mu is
+ * below the resolution of sums over FP32 values.  Outputs may be NULL; mu_out
+ * receives the last mu of each instance. */
 gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64_t *steps_done,
                               int32_t *converged, double *mu_out);
 

@@ -219,3 +219,42 @@ def test_batch_runs_are_identical():
         diff = [i for i in range(len(insts)) if not (np.array_equal(a[i][0], b[i][0]) and
                                                      np.array_equal(a[i][1], b[i][1]))]
         assert not diff, (prec.name, diff)
+
+
+@pytest.mark.gpu
+def test_fp32_host_format_of_compensated_storage():
+    """gpe_set_host_precision(GPE_FP32) on a GPE_FP32C handle: float fields in
+    (residual zero), float fields out (value + residual rounded once), through
+    the single and the batched transfers; equal to the oracle's compensated run
+    from the same float start, bit for bit."""
+    import oracle.oracle as orc
+    from helpers import grid_for, interleave, random_state, vdt_for
+    from vaikkari_gb300.gpe import Instance, Kernel, Lattice, Potential, Precision, Stepper
+    insts = [Instance(9, 7, 11, 0.35, 1e-3, 80.0, origin=(-1.5, -1.2, -1.9)),
+             Instance(16, 5, 6, 0.3, 1.5e-3, 40.0, origin=(-2.4, -0.8, -0.9))]
+    for batched in (False, True):
+        st = Stepper(insts, lattice=Lattice.BCC2, precision=Precision.FP32C, kernel=Kernel.FUSED,
+                     potential=Potential.TRAP)
+        st.set_host_precision(Precision.FP32)
+        fields, want = [], []
+        for i in range(len(insts)):
+            shp = st.shape(i)
+            e = interleave(random_state(shp, 90 + i, 0.3), np.float32)
+            o = interleave(random_state(shp, 95 + i, 0.3), np.float32)
+            fields.append((e, o))
+            eh, oh = e.copy(), o.copy()
+            el, ol = np.zeros(e.shape, np.uint16), np.zeros(o.shape, np.uint16)
+            grid_for(st, i).leapfrog_bcc2_comp(eh, oh, el, ol, vdt_for(st, i), 5)
+            want.append((orc.join_comp(eh, el).astype(np.float32), orc.join_comp(oh, ol).astype(np.float32)))
+        if batched:
+            st.upload_many([(i, e, o, None) for i, (e, o) in enumerate(fields)])
+        else:
+            for i, (e, o) in enumerate(fields):
+                st.upload(i, e, o)
+        st.step(5)
+        got = st.download_many(range(len(insts))) if batched else [st.download(i) for i in range(len(insts))]
+        st.close()
+        for (ge, go), (we, wo) in zip(got, want):
+            assert ge.dtype == np.float32
+            np.testing.assert_array_equal(ge, we)
+            np.testing.assert_array_equal(go, wo)

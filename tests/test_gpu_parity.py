@@ -290,3 +290,25 @@ def test_imaginary_time_converges_to_harmonic_ground_state(kernel):
     assert mu[0] == pytest.approx(1.5, rel=3e-2)
     assert obs["norm"] == pytest.approx(1.0, rel=1e-12)
     assert obs["mu"] == pytest.approx(mu[0], rel=1e-8)
+
+
+@pytest.mark.parametrize("lattice,kernel", [(Lattice.TETRA12, Kernel.PLAIN), (Lattice.BCC2, Kernel.FUSED)])
+def test_observables_fp32_smooth_field_trap(lattice, kernel):
+    """FP32 fields take the float-pair observables: a smooth Gaussian on a fine
+    grid makes each value's Laplacian a small difference of large neighbour
+    sums (the hardest case for reduced-precision arithmetic); with the trap
+    potential, every sum still agrees with the FP64 oracle to 1e-12."""
+    bw = 8 ** 0.5 if lattice == Lattice.TETRA12 else 1.0
+    n, L = 24, 4.0
+    bs = 2 * L / n / bw
+    inst = Instance(n, n, n, bs, 1e-3, 700.0, origin=(-L, -L, -L), trap=(1.0, 1.7, 0.6))
+    st = Stepper([inst], lattice=lattice, precision=Precision.FP32, kernel=kernel, potential=Potential.TRAP)
+    from oracle.lattice import value_positions
+    p = value_positions(n, n, n, bs, inst.origin, lattice)
+    psi = np.exp(-0.5 * np.sum(p * p, axis=-1)) * np.exp(0.3j * p[..., 0])
+    st.upload(0, psi, psi)
+    want = grid_for(st, 0).observables(interleave(psi, np.float32), vdt_for(st, 0), vol_for(st, 0))
+    got = st.observables(0)[0]
+    st.close()
+    for k in ("norm", "kinetic", "potential", "interaction", "energy", "mu"):
+        assert got[k] == pytest.approx(want[k], rel=1e-12), k

@@ -78,7 +78,8 @@ struct gpe_handle_ {
     gpe_lattice_info lat{};
     int ns = 0;
     size_t esize = 0;  // bytes per real element on the device
-    size_t hsize = 0;  // bytes per real element of a host field array (8 for GPE_FP32C)
+    size_t hsize = 0;  // bytes per real element of a host field array (8 for GPE_FP32C unless host_fp32)
+    bool host_fp32 = false;  // GPE_FP32C: host fields are float (gpe_set_host_precision)
     bool comp = false;                   // GPE_FP32C: compensated real-time storage
     void *lo[2] = {nullptr, nullptr};    // GPE_FP32C: bf16x2 residual per value of fields 0 and 1
     std::vector<InstDev> idev_host;
@@ -131,6 +132,7 @@ struct gpe_handle_ {
     bool persistent = false;
     int *nbr_begin_dev = nullptr, *nbr_dev = nullptr;
     unsigned int *done = nullptr;
+    unsigned long long *ticket = nullptr;  // the persistent launch's work counter, zeroed before each launch
     unsigned int epoch = 0;      // done[] of every item after the launches queued so far
     bool epoch_reset = false;    // a launch timed out: zero done[] before the next one
     double tol = 0.0;
@@ -519,6 +521,7 @@ gpe_status run_persistent(gpe_handle h, long long steps)
             h->epoch = 0;
             h->epoch_reset = false;
         }
+        GPE_CUDA_TRY(cudaMemsetAsync(h->ticket, 0, sizeof(unsigned long long), h->stream));
         PersistLaunch l{};
         l.precision = h->cfg.precision;
         l.potential = h->cfg.potential;
@@ -535,6 +538,7 @@ gpe_status run_persistent(gpe_handle h, long long steps)
         l.lo[0] = h->lo[0];
         l.lo[1] = h->lo[1];
         l.vpot = h->vpot;
+        l.ticket = h->ticket;
         l.nbr_begin = h->nbr_begin_dev;
         l.nbr = h->nbr_dev;
         l.done = h->done;
@@ -611,6 +615,7 @@ void free_handle(gpe_handle h)
     cudaFree(h->nbr_begin_dev);
     cudaFree(h->nbr_dev);
     cudaFree(h->done);
+    cudaFree(h->ticket);
     cudaFree(h->imag);
     cudaFree(h->partials);
     cudaFree(h->counter);
@@ -1044,6 +1049,7 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
             GPE_CREATE_TRY(cudaMalloc(&h->nbr_dev, sizeof(int) * nb.size()));
             GPE_CREATE_TRY(cudaMemcpyAsync(h->nbr_dev, nb.data(), sizeof(int) * nb.size(), cudaMemcpyHostToDevice,
                                            h->stream));
+            GPE_CREATE_TRY(cudaMalloc(&h->ticket, sizeof(unsigned long long)));
             GPE_CREATE_TRY(cudaMalloc(&h->done, sizeof(unsigned int) * h->items.size()));
             GPE_CREATE_TRY(cudaMemsetAsync(h->done, 0, sizeof(unsigned int) * h->items.size(), h->stream));
         }
@@ -1154,7 +1160,7 @@ static gpe_status gpe_upload_impl(gpe_handle h, int32_t instance, const void *ev
         if (st != GPE_OK) return st;
         if (h->comp)
             GPE_CUDA_TRY(launch_pack_split(h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->staging, field_buf(h, f),
-                                           h->lo[f], h->stream));
+                                           h->lo[f], h->host_fp32, h->stream));
         else
             GPE_CUDA_TRY(launch_pack(prec, h->idev, instance, in.nx, in.ny, in.nz, h->ns, h->staging, field_buf(h, f),
                                      1, 1.0, h->stream));
@@ -1195,7 +1201,7 @@ static gpe_status gpe_download_impl(gpe_handle h, int32_t instance, void *even, 
         if (!dsts[f]) continue;
         if (h->comp)
             GPE_CUDA_TRY(launch_unpack_join(h->idev, instance, in.nx, in.ny, in.nz, h->ns, field_buf(h, f), h->lo[f],
-                                            h->staging, h->stream));
+                                            h->staging, h->host_fp32, h->stream));
         else
             GPE_CUDA_TRY(launch_unpack(h->cfg.precision, h->idev, instance, in.nx, in.ny, in.nz, h->ns,
                                        field_buf(h, f), h->staging, nullptr, h->stream));
@@ -1291,7 +1297,7 @@ static gpe_status gpe_upload_many_impl(gpe_handle h, int32_t count, const int32_
             if ((st = copy_in(stage, srcs[f], b)) != GPE_OK) return st;
             if (h->comp)
                 GPE_CUDA_TRY(launch_pack_split(h->idev, i, in.nx, in.ny, in.nz, h->ns, stage, field_buf(h, f), h->lo[f],
-                                               h->stream));
+                                               h->host_fp32, h->stream));
             else
                 GPE_CUDA_TRY(launch_pack(prec, h->idev, i, in.nx, in.ny, in.nz, h->ns, stage, field_buf(h, f), 1, 1.0,
                                          h->stream));
@@ -1354,7 +1360,7 @@ static gpe_status gpe_download_many_impl(gpe_handle h, int32_t count, const int3
             const size_t b = vals * 2 * h->hsize;
             if (h->comp)
                 GPE_CUDA_TRY(launch_unpack_join(h->idev, i, in.nx, in.ny, in.nz, h->ns, field_buf(h, f), h->lo[f], stage,
-                                                h->stream));
+                                                h->host_fp32, h->stream));
             else
                 GPE_CUDA_TRY(launch_unpack(h->cfg.precision, h->idev, i, in.nx, in.ny, in.nz, h->ns, field_buf(h, f),
                                            stage, nullptr, h->stream));
@@ -1458,6 +1464,8 @@ gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out
     GPE_GUARD(gpe_observables_get_impl(h, field, out));
 }
 
+static gpe_status gpe_observables_get_impl(gpe_handle h, int32_t field, gpe_observables *out);
+
 static gpe_status gpe_imaginary_time_impl(gpe_handle h, int64_t max_steps, double tol, int64_t *steps_done, int32_t *converged,
                                           double *mu_out)
 {
@@ -1466,13 +1474,25 @@ static gpe_status gpe_imaginary_time_impl(gpe_handle h, int64_t max_steps, doubl
     if (h->cfg.mode != GPE_IMAGINARY_TIME)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_imaginary_time: handle is not in imaginary-time mode");
     if (max_steps < 0 || !(tol >= 0.0)) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_imaginary_time: bad arguments");
-    h->tol = tol;
+    // FP64: the per-step test |mu_k - mu_(k-1)| < tol on the device, as the
+    // reductions fused into each step compute mu.  FP32: a per-step difference
+    // of mu taken from FP32 values is not resolvable at tol (a step can change
+    // no stored value, or change it by less than the sums' rounding), so the
+    // test runs once per chunk of G steps on mu from the FP64 observables of the
+    // normalised field: converged when |mu_k - mu_(k-G)| < G * tol, i.e. the
+    // mean change per step over the chunk is below tol.
+    const bool windowed = h->cfg.precision != GPE_FP64;
+    h->tol = windowed ? 0.0 : tol;
     st = imag_prepare(h);
     if (st != GPE_OK) return st;
     const long long G = h->cfg.graph_steps == 0 ? 100 : (h->cfg.graph_steps < 0 ? 100 : h->cfg.graph_steps);
     long long done = 0;
     bool all = false;
-    std::vector<ImagScalars> sc(h->cfg.num_instances);
+    const int n_inst = h->cfg.num_instances;
+    std::vector<ImagScalars> sc(n_inst);
+    std::vector<gpe_observables> obs(n_inst);
+    std::vector<double> mu(n_inst, 0.0), mu_prev(n_inst, 0.0);
+    bool have_prev = false;
     while (done < max_steps) {
         const long long n = std::min<long long>(G, max_steps - done);
         st = run_steps(h, n);
@@ -1480,18 +1500,33 @@ static gpe_status gpe_imaginary_time_impl(gpe_handle h, int64_t max_steps, doubl
         done += n;
         st = imag_normalise(h, !h->fused);
         if (st != GPE_OK) return st;
-        GPE_CUDA_TRY(cudaMemcpyAsync(sc.data(), h->imag, sizeof(ImagScalars) * sc.size(), cudaMemcpyDeviceToHost,
-                                     h->stream));
-        st = sync_and_check(h);
-        if (st != GPE_OK) return st;
-        all = true;
-        for (auto &s : sc) all = all && (s.conv_step >= 0);
+        if (windowed) {
+            st = gpe_observables_get_impl(h, 0, obs.data());
+            if (st != GPE_OK) return st;
+            all = have_prev && n == G;
+            for (int i = 0; i < n_inst; i++) {
+                mu[i] = obs[i].mu;
+                all = all && std::fabs(mu[i] - mu_prev[i]) < double(n) * tol;
+            }
+            mu_prev = mu;
+            have_prev = true;
+        } else {
+            GPE_CUDA_TRY(cudaMemcpyAsync(sc.data(), h->imag, sizeof(ImagScalars) * sc.size(), cudaMemcpyDeviceToHost,
+                                         h->stream));
+            st = sync_and_check(h);
+            if (st != GPE_OK) return st;
+            all = true;
+            for (int i = 0; i < n_inst; i++) {
+                all = all && (sc[i].conv_step >= 0);
+                mu[i] = sc[i].mu;
+            }
+        }
         if (all) break;
     }
     if (steps_done) *steps_done = done;
     if (converged) *converged = all ? 1 : 0;
     if (mu_out)
-        for (int i = 0; i < h->cfg.num_instances; i++) mu_out[i] = sc[i].mu;
+        for (int i = 0; i < n_inst; i++) mu_out[i] = mu[i];
     return GPE_OK;
 }
 
@@ -1627,6 +1662,29 @@ static gpe_status gpe_link_z_impl(gpe_handle h, int32_t lower, int32_t upper)
 gpe_status gpe_link_z(gpe_handle h, int32_t lower, int32_t upper)
 {
     GPE_GUARD(gpe_link_z_impl(h, lower, upper));
+}
+
+static gpe_status gpe_set_host_precision_impl(gpe_handle h, int32_t precision)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (h->comp) {
+        if (precision != GPE_FP64 && precision != GPE_FP32)
+            return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_set_host_precision: GPE_FP32C exchanges fields as GPE_FP64 "
+                                                  "or GPE_FP32");
+        h->host_fp32 = precision == GPE_FP32;
+        h->hsize = h->host_fp32 ? 4 : 8;
+        return GPE_OK;
+    }
+    if (precision != h->cfg.precision)
+        return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_set_host_precision: this handle exchanges fields in its own "
+                                              "precision");
+    return GPE_OK;
+}
+
+gpe_status gpe_set_host_precision(gpe_handle h, int32_t precision)
+{
+    GPE_GUARD(gpe_set_host_precision_impl(h, precision));
 }
 
 int32_t gpe_variant_count(void) { return fused_tile_count(); }

@@ -290,13 +290,17 @@ __device__ __forceinline__ void fence_proxy_async_global()
 // Returns kItemDone, kItemWithheld (test hook: plane `withhold` of this item
 // was not issued, nor anything after it) or kItemAbort (a wait ran out or the
 // CTA is stopping; *err and *abort_flag are set).  `issued` is the ring number
-// one past the last plane issued.
+// one past the last plane issued.  With a non-null `tag`, tag[stage] = tag_value
+// is written for the item's first plane once that stage is free, before its
+// copies are issued (the persistent kernel names the item to its consumers so).
 constexpr int kItemDone = 0, kItemWithheld = 1, kItemAbort = -1;
 
 template <typename T, int TX, int TY, int MODE, int STAGES, bool WATCH>
 __device__ __forceinline__ int produce_item(const WorkItem &w, int kb, int src, const CUtensorMap *maps,
                                             const CUtensorMap *lo_maps, uint32_t base, uint32_t full, uint32_t empty,
-                                            int withhold, int *err, volatile int *abort_flag, int &issued)
+                                            int withhold, int *err, volatile int *abort_flag, int &issued,
+                                            volatile unsigned long long *tag = nullptr,
+                                            unsigned long long tag_value = 0)
 {
     using S = FusedShape<T, TX, TY, MODE == 2>;
     constexpr bool REAL = MODE != 1;
@@ -322,6 +326,7 @@ __device__ __forceinline__ int produce_item(const WorkItem &w, int kb, int src, 
             }
         }
         if (withhold == k) return kItemWithheld;
+        if (k == 0 && tag) tag[st] = tag_value;
         const bool with_next = REAL && (k >= 2);
         mbar_arrive_expect_tx(full + 8 * st, S::HALO_BYTES + (with_next ? S::NEXT_BYTES + S::LO_BYTES : 0));
         // padded coordinates: x0-2 -> x0, y0-1 -> y0, plane q -> q+1

@@ -143,6 +143,7 @@ struct PersistLaunch {
     void *field[2];
     void *lo[2];
     const void *vpot;
+    unsigned long long *ticket;
     const int *nbr_begin, *nbr;
     unsigned int *done;
     unsigned int epoch0;
@@ -194,9 +195,9 @@ cudaError_t launch_unpack(int precision, const InstDev *inst, int inst_index, in
                           cudaStream_t s);
 // GPE_FP32C: double host order <-> FP32 field plus bf16x2 residuals.
 cudaError_t launch_pack_split(const InstDev *inst, int ii, int nx, int ny, int nz, int slots, const void *host_order,
-                              void *field, void *lo, cudaStream_t s);
+                              void *field, void *lo, bool host_fp32, cudaStream_t s);
 cudaError_t launch_unpack_join(const InstDev *inst, int ii, int nx, int ny, int nz, int slots, const void *field,
-                               const void *lo, void *host_order, cudaStream_t s);
+                               const void *lo, void *host_order, bool host_fp32, cudaStream_t s);
 // Field outputs (gpe_output.cu).
 cudaError_t launch_volume(int precision, const InstDev *inst, int ii, const void *field, double unit, int quirk,
                           uint16_t *out, long long total, cudaStream_t s);

@@ -3,31 +3,40 @@
 //
 // The reference drives its leapfrog from the host, two launches per step
 // (koodit/GrossPitaevskii/GPUGrossPitaevskii_BCC.cu:475-481).  Here one
-// cooperative launch runs all the half-steps of a gpe_step call: its CTAs stay
-// resident, each takes work items blockIdx.x, blockIdx.x + gridDim.x, ... of
-// the same item list as the one-launch-per-half-step kernel, half-step after
-// half-step, and runs each item exactly as that kernel does (gpe_fused_core.cuh:
-// the producer lane's TMA issue, the consumer warps' z-march), so the results
-// are bit-identical to it.
+// cooperative launch runs all the half-steps of a gpe_step call.  Its CTAs stay
+// resident and take tickets from one counter: ticket t is work item t % N of
+// half-step t / N (N items, the same list as the one-launch-per-half-step
+// kernel), so every CTA that finishes early takes more work and the CTAs stay
+// balanced however unevenly the items divide among them.  Each item runs
+// exactly as in that kernel (gpe_fused_core.cuh: the producer lane's TMA issue,
+// the consumer warps' z-march), so the results are bit-identical to it.  The
+// producer tells its consumers which ticket a ring plane starts with through a
+// per-stage tag in shared memory, written before the plane's copies are issued
+// and read after its full barrier completes.
 //
 // Ordering without a grid barrier: item X at half-step h reads the field its
 // neighbours wrote at half-step h-1 (halo), and rewrites the field they read
 // at h-1, so it may start once every item within one tile / one z-chunk of it
-// (at most 27, itself included) has finished h-1.  Each item has an epoch word
-// done[X] = half-steps it has completed since the handle was created.
+// (at most 27, itself included) has finished h-1.  Each item has a counter
+// done[X] of consumer-warp completions since the handle was created: with W
+// consumer warps per CTA, X has finished half-step h when done[X] reaches
+// W * (epoch0 + h + 1).
 //   * publish: after the item's last plane every consumer thread fences its
-//     stores into the async proxy, the consumer warps meet at a named barrier,
-//     and thread 0 stores done[X] = epoch0 + h + 1 with release semantics at
-//     GPU scope;
+//     stores into the async proxy, the warp synchronises, and lane 0 adds 1 to
+//     done[X] with release semantics at GPU scope - each warp on its own, so no
+//     warp waits for the others at an item boundary;
 //   * wait: before issuing item X at half-step h, lane j of the producer warp
-//     polls done[neighbour j] with acquire loads until it reaches epoch0 + h;
-//     lane 0 then fences into the async proxy and issues the TMA copies.
+//     polls done[neighbour j] with acquire loads until it reaches
+//     W * (epoch0 + h); lane 0 then fences into the async proxy and issues the
+//     TMA copies.
 // The producer runs ahead of its consumers by the ring's depth across item and
 // half-step boundaries, so the pipeline does not drain between half-steps, and
 // small and large instances of a batch advance independently.  No CTA waits
 // for one that is not resident: the launch is cooperative (the grid is at most
-// the resident CTAs), and every item of half-step h depends only on items of
-// h-1, which every CTA finishes before it starts h.
+// the resident CTAs).  Nothing deadlocks: tickets are handed out in increasing
+// order, a ticket depends only on smaller ones, and each CTA runs its tickets
+// in order, so the smallest unfinished ticket always has its dependencies done
+// and its CTA working on it.
 //
 // Waits are bounded (about one second).  A wait that runs out sets the
 // handle's error word; every other wait of the launch (epoch polls, ring
@@ -50,10 +59,11 @@ struct PersistArgs {
     void *field[2];              // even, odd
     uint32_t *lo[2];             // MODE 2: their bf16x2 residuals
     const void *vpot;
+    unsigned long long *ticket;  // ticket counter, zero at launch
     const int *nbr_begin;        // [num_items + 1]: CSR rows of nbr
     const int *nbr;              // the items each item depends on (itself included)
-    unsigned int *done;          // per item: half-steps completed
-    unsigned int epoch0;         // done[] of every item when this launch starts
+    unsigned int *done;          // per item: consumer-warp completions (W per half-step)
+    unsigned int epoch0;         // half-steps every item had completed when this launch starts
     int half_steps;              // half-steps this launch advances (odd <- even first)
     int *err;
     int inject_skip_plane;       // test hook: plane the producer of item 0 withholds at half-step 0
@@ -66,9 +76,9 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p)
     return v;
 }
 
-__device__ __forceinline__ void st_release_gpu(unsigned *p, unsigned v)
+__device__ __forceinline__ void red_release_gpu_add(unsigned *p, unsigned v)
 {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 // Waits until *p has reached `need` (epochs compare modulo 2^32); gives up after
@@ -80,6 +90,7 @@ __device__ __forceinline__ bool wait_epoch(const unsigned *p, unsigned need, con
     if (int(ld_acquire_gpu(p) - need) >= 0) return true;
     const uint64_t t0 = global_ns();
     for (unsigned i = 1;; i++) {
+        __nanosleep(64);  // eases the polling load on L2 while CTAs wait for a lagging neighbour
         if (int(ld_acquire_gpu(p) - need) >= 0) return true;
         if ((i & 15u) == 0u && (*(const volatile int *)gerr != 0 || *abort_flag || global_ns() - t0 > kWaitLimitNs))
             return false;
@@ -100,6 +111,8 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) persis
     const uint32_t full = base + STAGES * S::STAGE_BYTES;
     const uint32_t empty = full + 8 * STAGES;
     __shared__ volatile int abort_flag;
+    __shared__ unsigned long long stage_tag[STAGES];  // ticket whose first plane a stage holds
+    constexpr unsigned long long kEnd = ~0ull;
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
@@ -112,71 +125,89 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) persis
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    const unsigned long long N = (unsigned long long)a.num_items;
+    const unsigned long long total = (unsigned long long)a.half_steps * N;
 
     if (warp == NWARPS - 1) {
-        // ---- producer warp: dependency polls on all lanes, TMA issue on lane 0
+        // ---- producer warp: tickets and dependency polls on all lanes, TMA issue on lane 0
         int issued = 0;
-        bool stop = false;
-        for (int h = 0; h < a.half_steps && !stop; h++) {
-            const int src = h & 1;  // odd <- even, then even <- odd
-            for (int it = blockIdx.x; it < a.num_items; it += gridDim.x) {
-                const unsigned need = a.epoch0 + unsigned(h);
-                const int nb0 = a.nbr_begin[it], nbn = a.nbr_begin[it + 1] - nb0;
-                const bool ready = lane >= nbn || wait_epoch(a.done + a.nbr[nb0 + lane], need, a.err, &abort_flag);
-                if (__any_sync(0xffffffffu, !ready)) {
-                    if (lane == 0) {
-                        atomicExch(a.err, kErrTimeout);
-                        abort_flag = 1;
+        bool ended = false;  // the end-of-work plane went out
+        while (true) {
+            unsigned long long t = 0;
+            if (lane == 0) t = atomicAdd(a.ticket, 1ull);
+            t = __shfl_sync(0xffffffffu, t, 0);
+            const bool aborting = __any_sync(0xffffffffu, abort_flag != 0);  // one decision for the warp
+            if (t >= total || aborting) {
+                // no more work: an empty plane tagged kEnd tells the consumers
+                if (lane == 0 && !aborting) {
+                    const int st = issued % STAGES;
+                    bool ok = issued < STAGES || mbar_wait_watched<true>(empty + 8 * st, ((issued / STAGES) - 1) & 1,
+                                                                         a.err);
+                    if (ok) {
+                        stage_tag[st] = kEnd;
+                        mbar_arrive(full + 8 * st);  // completes the phase with no copies
+                        ended = true;
                     }
-                    stop = true;
-                    break;
                 }
-                __syncwarp();  // orders the other lanes' acquire loads before lane 0's issue
-                int r = kItemDone;
-                if (lane == 0) {
-                    __threadfence();             // the flags the other lanes acquired come first
-                    fence_proxy_async_global();  // then this CTA's TMA reads of the neighbours' stores
-                    r = produce_item<T, TX, TY, MODE, STAGES, true>(
-                        a.items[it], issued, src, a.maps, a.lo_maps, base, full, empty,
-                        (h == 0 && it == 0) ? a.inject_skip_plane : -1, a.err, &abort_flag, issued);
-                }
-                r = __shfl_sync(0xffffffffu, r, 0);
-                if (r != kItemDone) {
-                    stop = true;
-                    break;
-                }
+                break;
             }
+            const int h = int(t / N), it = int(t % N);
+            const unsigned need = unsigned(NT / 32) * (a.epoch0 + unsigned(h));
+            const int nb0 = a.nbr_begin[it], nbn = a.nbr_begin[it + 1] - nb0;
+            const bool ready = lane >= nbn || wait_epoch(a.done + a.nbr[nb0 + lane], need, a.err, &abort_flag);
+            if (__any_sync(0xffffffffu, !ready)) {
+                if (lane == 0) {
+                    atomicExch(a.err, kErrTimeout);
+                    abort_flag = 1;
+                }
+                break;
+            }
+            __syncwarp();  // orders the other lanes' acquire loads before lane 0's issue
+            int r = kItemDone;
+            if (lane == 0) {
+                __threadfence();             // the flags the other lanes acquired come first
+                fence_proxy_async_global();  // then this CTA's TMA reads of the neighbours' stores
+                r = produce_item<T, TX, TY, MODE, STAGES, true>(
+                    a.items[it], issued, h & 1, a.maps, a.lo_maps, base, full, empty,
+                    (h == 0 && it == 0) ? a.inject_skip_plane : -1, a.err, &abort_flag, issued, stage_tag, t);
+            }
+            r = __shfl_sync(0xffffffffu, r, 0);
+            if (r != kItemDone) break;
         }
-        // every copy this CTA issued lands before it exits (instant when the
-        // consumers took them all)
-        if (lane == 0) drain_ring<STAGES>(issued, full);
+        // After an abort, the copies this CTA issued land before it exits.  A
+        // normal end needs no wait: the consumers take every plane before the
+        // end-of-work plane, and the CTA stays until they finish (the ring's
+        // phases have then moved past the ones a drain would test).
+        if (lane == 0 && !ended) drain_ring<STAGES>(issued, full);
     } else {
-        // ---- consumer warps -------------------------------------------------
+        // ---- consumer warps: each publishes its own part of an item ---------
         int kb = 0;
         Acc<T> acc[4];
-        bool ok = true;
-        for (int h = 0; h < a.half_steps && ok; h++) {
-            const int src = h & 1;
-            void *next = src ? a.field[0] : a.field[1];  // selects, so the argument arrays stay in registers
-            uint32_t *next_lo = src ? a.lo[0] : a.lo[1];
-            for (int it = blockIdx.x; it < a.num_items; it += gridDim.x) {
-                const WorkItem w = a.items[it];
-                const InstDev &d = a.inst[w.inst];
-                const T *tz = (const T *)a.vpot + d.vbase + 2ll * d.nx + 2ll * d.ny;  // trap: z-terms [slot][z]
-                const bool got = consume_item<T, TX, TY, MODE, POT, STAGES, true>(
-                    w, d, kb, gbase, full, empty, next, next_lo, a.vpot, tz, d.nz, 0, T(1), acc, tid, lane, a.err,
-                    &abort_flag);
-                kb += w.z1 - w.z0 + 2;
-                fence_proxy_async_global();  // this thread's stores, before other CTAs' TMA reads of them
-                if (bar_any(1, NT, !got)) {  // consumer warps only; all stop together
-                    ok = false;
-                    break;
-                }
-                if (tid == 0) {
-                    __threadfence();
-                    st_release_gpu(a.done + it, a.epoch0 + unsigned(h) + 1u);
-                }
+        while (true) {
+            // the ticket of the next item, from the tag of its first plane's stage
+            const int st = kb % STAGES;
+            const bool got = mbar_wait_watched<true>(full + 8 * st, (kb / STAGES) & 1, a.err);
+            if (__any_sync(0xffffffffu, !got)) {
+                atomicExch(a.err, kErrTimeout);
+                abort_flag = 1;
+                break;
             }
+            const unsigned long long t = stage_tag[st];
+            if (t == kEnd) break;
+            const int h = int(t / N), it = int(t % N);
+            void *next = (h & 1) ? a.field[0] : a.field[1];  // selects, so the argument arrays stay in registers
+            uint32_t *next_lo = (h & 1) ? a.lo[0] : a.lo[1];
+            const WorkItem w = a.items[it];
+            const InstDev &d = a.inst[w.inst];
+            const T *tz = (const T *)a.vpot + d.vbase + 2ll * d.nx + 2ll * d.ny;  // trap: z-terms [slot][z]
+            if (!consume_item<T, TX, TY, MODE, POT, STAGES, true>(w, d, kb, gbase, full, empty, next, next_lo,
+                                                                  a.vpot, tz, d.nz, 0, T(1), acc, tid, lane, a.err,
+                                                                  &abort_flag))
+                break;  // warp-uniform; the launch's error word is set, the other warps stop too
+            kb += w.z1 - w.z0 + 2;
+            fence_proxy_async_global();  // this thread's stores, before other CTAs' TMA reads of them
+            __syncwarp();
+            if (lane == 0) red_release_gpu_add(a.done + it, 1u);
         }
     }
 }
@@ -188,7 +219,7 @@ struct PVariant {
     int tx, ty, stages, minb;
 };
 static const PVariant kPersistVariants[] = {
-    {32, 4, 8, 5}, {32, 8, 6, 3}, {32, 4, 6, 6}, {32, 2, 8, 8}, {64, 4, 4, 3}, {16, 8, 6, 6},
+    {32, 4, 8, 5}, {32, 8, 6, 3}, {32, 4, 8, 4}, {32, 2, 8, 8}, {64, 4, 4, 3}, {32, 8, 6, 2},
 };
 constexpr int kPersistCount = int(sizeof(kPersistVariants) / sizeof(kPersistVariants[0]));
 
@@ -256,10 +287,10 @@ static cudaError_t launch_p_variant(const PersistLaunch &l, const PersistArgs &a
 {
     switch (l.variant) {  // must list kPersistVariants in order
     case 1: return launch_p_mode<T, 32, 8, 6, 3>(l, a, s, grid);
-    case 2: return launch_p_mode<T, 32, 4, 6, 6>(l, a, s, grid);
+    case 2: return launch_p_mode<T, 32, 4, 8, 4>(l, a, s, grid);
     case 3: return launch_p_mode<T, 32, 2, 8, 8>(l, a, s, grid);
     case 4: return launch_p_mode<T, 64, 4, 4, 3>(l, a, s, grid);
-    case 5: return launch_p_mode<T, 16, 8, 6, 6>(l, a, s, grid);
+    case 5: return launch_p_mode<T, 32, 8, 6, 2>(l, a, s, grid);
     default: return launch_p_mode<T, 32, 4, 8, 5>(l, a, s, grid);
     }
 }
@@ -277,6 +308,7 @@ cudaError_t launch_persistent(const PersistLaunch &l, cudaStream_t s, int *grid)
     a.lo[0] = (uint32_t *)l.lo[0];
     a.lo[1] = (uint32_t *)l.lo[1];
     a.vpot = l.vpot;
+    a.ticket = l.ticket;
     a.nbr_begin = l.nbr_begin;
     a.nbr = l.nbr;
     a.done = l.done;

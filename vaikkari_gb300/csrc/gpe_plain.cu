@@ -418,6 +418,102 @@ __device__ void cta_tree_store(double (&v)[W], double *out)
     if (t < W) out[t] = sm[t][0];
 }
 
+// Float pairs: a value hi + lo with |lo| <= ulp(hi)/2, carried by error-free
+// transformations on the FP32 pipe (Knuth's two-sum; the two-product through
+// fma).  Addition is the accurate form (both parts two-summed), whose error is
+// about 2^-44 of the result even when the operands cancel; multiplication
+// rounds once at about 2^-44.  On this GPU the FP32 pipe is 64 times the FP64
+// pipe, so some twenty FP32 operations per double-precision step are cheaper
+// than the FP64 instruction they replace.
+struct FPair {
+    float hi, lo;
+};
+__device__ __forceinline__ FPair fp_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ FPair fp_fast_two_sum(float a, float b)  // |a| >= |b| or a == 0
+{
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FPair fp_two_prod(float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ FPair fp_add(FPair x, FPair y)
+{
+    FPair s = fp_two_sum(x.hi, y.hi);
+    const FPair t = fp_two_sum(x.lo, y.lo);
+    s = fp_fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+    return fp_fast_two_sum(s.hi, __fadd_rn(s.lo, t.lo));
+}
+__device__ __forceinline__ FPair fp_mul(FPair x, FPair y)
+{
+    const FPair p = fp_two_prod(x.hi, y.hi);
+    return fp_fast_two_sum(p.hi, __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, p.lo)));
+}
+__device__ __forceinline__ FPair fp_scale(FPair x, float k)  // k a power of two: exact
+{
+    return {__fmul_rn(x.hi, k), __fmul_rn(x.lo, k)};
+}
+__device__ __forceinline__ FPair fp_of(double v)
+{
+    const float hi = __double2float_rn(v);
+    return {hi, __double2float_rn(__dsub_rn(v, double(hi)))};
+}
+__device__ __forceinline__ double fp_value(FPair x) { return __dadd_rn(double(x.hi), double(x.lo)); }
+
+// The observables of FP32 values, all in float-pair arithmetic: per class c
+// the neighbour sum S_c as an error-free pair, the bracket S_c - n_c psi (the
+// Laplacian's cancellation, exact up to the pair's rounding), Lap psi =
+// sum_c w_c (S_c - n_c psi), and the four terms, each added into a float-pair
+// accumulator.  Agrees with FP64 evaluation to about 1e-13 relative.
+template <int LAT, int POT>
+__device__ __forceinline__ void observables_terms_f32(const InstDev &d, const float2 *__restrict__ f,
+                                                      const float *__restrict__ vpot, int s, int x, int y, int z,
+                                                      long long self, const FPair (&w)[2], FPair rdt, FPair half_g,
+                                                      FPair (&acc)[4])
+{
+    using L = Lat<LAT>;
+    const float2 pt = f[self];
+    float hx[2] = {0.f, 0.f}, lx_[2] = {0.f, 0.f}, hy[2] = {0.f, 0.f}, ly_[2] = {0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < L::NB; k++) {
+        const int e = L::entry(s * L::NB + k);
+        const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
+        const float2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
+        const int c = (k < L::N0) ? 0 : 1;
+        const FPair tx = fp_two_sum(hx[c], q.x), ty = fp_two_sum(hy[c], q.y);
+        hx[c] = tx.hi;
+        lx_[c] = __fadd_rn(lx_[c], tx.lo);
+        hy[c] = ty.hi;
+        ly_[c] = __fadd_rn(ly_[c], ty.lo);
+    }
+    FPair lapx = {0.f, 0.f}, lapy = {0.f, 0.f};
+#pragma unroll
+    for (int c = 0; c < L::NC; c++) {
+        const float n = float(c == 0 ? L::N0 : L::NB - L::N0);
+        const FPair npx = fp_two_prod(n, pt.x), npy = fp_two_prod(n, pt.y);
+        const FPair bx = fp_add(fp_two_sum(hx[c], lx_[c]), {-npx.hi, -npx.lo});
+        const FPair by = fp_add(fp_two_sum(hy[c], ly_[c]), {-npy.hi, -npy.lo});
+        lapx = fp_add(lapx, fp_mul(w[c], bx));
+        lapy = fp_add(lapy, fp_mul(w[c], by));
+    }
+    float vdt;
+    if (POT == GPE_POTENTIAL_ARRAY) vdt = vpot[self - d.base + d.vbase];
+    else vdt = trap_vdt<float>(vpot, d, s, x, y, z);
+    const FPair n2 = fp_add(fp_two_prod(pt.x, pt.x), fp_two_prod(pt.y, pt.y));
+    const FPair kin = fp_scale(fp_add(fp_mul({pt.x, 0.f}, lapx), fp_mul({pt.y, 0.f}, lapy)), -0.5f);
+    acc[0] = fp_add(acc[0], n2);
+    acc[1] = fp_add(acc[1], kin);
+    acc[2] = fp_add(acc[2], fp_mul(fp_mul({vdt, 0.f}, rdt), n2));
+    acc[3] = fp_add(acc[3], fp_mul(half_g, fp_mul(n2, n2)));
+}
+
 // One CTA's share of one instance's sums: values first, first + stride, ...;
 // writes the CTA's row of 6 partial sums to `row`.
 template <typename T, int LAT, int POT>
@@ -431,6 +527,27 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
     Kahan k0, k1, k2, k3;
     const double wsum = L::N0 * d.w[0] + (L::NB - L::N0) * d.w[1];
     const double rdt = 1.0 / d.dt;
+    if constexpr (sizeof(T) == 4 && LAT != kStepTetra12Faces) {
+        if (!(LAT == GPE_LATTICE_TETRA12 && d.face)) {
+            const FPair w[2] = {fp_of(d.w[0]), fp_of(d.w[1])};
+            const FPair rdt2 = fp_of(rdt), half_g = fp_of(0.5 * d.g);
+            FPair acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+            for (long long v = first; v < total; v += stride) {
+                long long r = v;
+                const int x = int(r % d.nx);
+                r /= d.nx;
+                const int y = int(r % d.ny);
+                r /= d.ny;
+                const int s = int(r % L::NS);
+                const int z = int(r / L::NS);
+                observables_terms_f32<LAT, POT>(d, (const float2 *)f, (const float *)vpot, s, x, y, z,
+                                                field_index(d, s, x, y, z), w, rdt2, half_g, acc);
+            }
+            double out[6] = {fp_value(acc[0]), fp_value(acc[1]), fp_value(acc[2]), fp_value(acc[3]), 0.0, 0.0};
+            cta_tree_store<6>(out, row);
+            return;
+        }
+    }
     for (long long v = first; v < total; v += stride) {
         long long r = v;
         const int x = int(r % d.nx);
@@ -733,7 +850,8 @@ __global__ void scale_field_kernel(const InstDev *__restrict__ insts, int ii, T 
 // GPE_FP32C transfers.  Upload: a double x becomes hi = float(x) and the
 // residual lo = bf16(float(x - hi)) (x - hi is exact in double); download:
 // double(hi) + double(lo).  lo holds both components in one word, re in the low half.
-__global__ void pack_split_kernel(const InstDev *__restrict__ insts, int ii, const double *__restrict__ src,
+template <typename H>  // host element: double, or float (the residual starts at zero)
+__global__ void pack_split_kernel(const InstDev *__restrict__ insts, int ii, const H *__restrict__ src,
                                   float *__restrict__ hi, uint32_t *__restrict__ lo)
 {
     const InstDev &d = insts[ii];
@@ -748,7 +866,7 @@ __global__ void pack_split_kernel(const InstDev *__restrict__ insts, int ii, con
         const int y = int(r % d.ny);
         const int z = int(r / d.ny);
         const long long o = field_index(d, s, x, y, z);
-        const double a = src[2 * v], b = src[2 * v + 1];
+        const double a = double(src[2 * v]), b = double(src[2 * v + 1]);
         const float ha = __double2float_rn(a), hb = __double2float_rn(b);
         hi[2 * o] = ha;
         hi[2 * o + 1] = hb;
@@ -759,8 +877,9 @@ __global__ void pack_split_kernel(const InstDev *__restrict__ insts, int ii, con
     }
 }
 
+template <typename H>  // host element: double, or float (value + residual rounded once)
 __global__ void unpack_join_kernel(const InstDev *__restrict__ insts, int ii, const float *__restrict__ hi,
-                                   const uint32_t *__restrict__ lo, double *__restrict__ dst)
+                                   const uint32_t *__restrict__ lo, H *__restrict__ dst)
 {
     const InstDev &d = insts[ii];
     const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
@@ -778,8 +897,8 @@ __global__ void unpack_join_kernel(const InstDev *__restrict__ insts, int ii, co
         const uint32_t w = lo[o];
         memcpy(&l, &w, 4);
         const float2 lf = __bfloat1622float2(l);
-        dst[2 * v] = double(hi[2 * o]) + double(lf.x);
-        dst[2 * v + 1] = double(hi[2 * o + 1]) + double(lf.y);
+        dst[2 * v] = H(double(hi[2 * o]) + double(lf.x));
+        dst[2 * v + 1] = H(double(hi[2 * o + 1]) + double(lf.y));
     }
 }
 
@@ -816,18 +935,27 @@ cudaError_t launch_unpack(int precision, const InstDev *inst, int ii, int nx, in
 }
 
 cudaError_t launch_pack_split(const InstDev *inst, int ii, int nx, int ny, int nz, int slots, const void *host_order,
-                              void *field, void *lo, cudaStream_t s)
+                              void *field, void *lo, bool host_fp32, cudaStream_t s)
 {
     const int g = grid_for((long long)nx * ny * nz * slots);
-    pack_split_kernel<<<g, 256, 0, s>>>(inst, ii, (const double *)host_order, (float *)field, (uint32_t *)lo);
+    if (host_fp32)
+        pack_split_kernel<float><<<g, 256, 0, s>>>(inst, ii, (const float *)host_order, (float *)field, (uint32_t *)lo);
+    else
+        pack_split_kernel<double><<<g, 256, 0, s>>>(inst, ii, (const double *)host_order, (float *)field,
+                                                    (uint32_t *)lo);
     return cudaGetLastError();
 }
 
 cudaError_t launch_unpack_join(const InstDev *inst, int ii, int nx, int ny, int nz, int slots, const void *field,
-                               const void *lo, void *host_order, cudaStream_t s)
+                               const void *lo, void *host_order, bool host_fp32, cudaStream_t s)
 {
     const int g = grid_for((long long)nx * ny * nz * slots);
-    unpack_join_kernel<<<g, 256, 0, s>>>(inst, ii, (const float *)field, (const uint32_t *)lo, (double *)host_order);
+    if (host_fp32)
+        unpack_join_kernel<float><<<g, 256, 0, s>>>(inst, ii, (const float *)field, (const uint32_t *)lo,
+                                                    (float *)host_order);
+    else
+        unpack_join_kernel<double><<<g, 256, 0, s>>>(inst, ii, (const float *)field, (const uint32_t *)lo,
+                                                     (double *)host_order);
     return cudaGetLastError();
 }
 

@@ -208,6 +208,8 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_time_steps.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]
     lib.gpe_variant_half_steps.restype = C.c_int32
     lib.gpe_variant_half_steps.argtypes = [C.c_int32]
+    lib.gpe_set_host_precision.restype = st
+    lib.gpe_set_host_precision.argtypes = [C.c_void_p, C.c_int32]
     lib.gpe_variant_kind.restype = C.c_int32
     lib.gpe_variant_kind.argtypes = [C.c_int32]
     lib.gpe_link_z.restype = st
@@ -394,6 +396,12 @@ class Stepper:
         return a, a.ctypes.data_as(C.c_void_p)
 
     # -- API ----------------------------------------------------------------
+    def set_host_precision(self, precision):
+        """Element type of host field arrays: Precision.FP64 (default for FP32C)
+        or Precision.FP32 (FP32C only: float in, float out; gpe_set_host_precision)."""
+        _check(self.lib.gpe_set_host_precision(self.h, int(precision)), "gpe_set_host_precision")
+        self.field_dtype = np.float64 if Precision(precision) == Precision.FP64 else np.float32
+
     def upload(self, i: int, even, odd=None, potential=None):
         """even/odd: complex arrays (nz, ny, nx, slots) or real (..., 2); potential: V (unscaled)."""
         shp = self.shape(i)
