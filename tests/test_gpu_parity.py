@@ -312,3 +312,27 @@ def test_observables_fp32_smooth_field_trap(lattice, kernel):
     st.close()
     for k in ("norm", "kinetic", "potential", "interaction", "energy", "mu"):
         assert got[k] == pytest.approx(want[k], rel=1e-12), k
+
+
+def test_fp32_imaginary_time_stops_on_its_own_criterion():
+    """FP32 imaginary time tests convergence on mu from the FP64 observables,
+    once per chunk (mean change per step below tol): from a random-phase start
+    it converges at tol 1e-9 by itself, in about as many steps as the FP64 run
+    (which tests every step), and to the same mu within FP32's resolution."""
+    n = 20
+    a = 10.0 / n
+    inst = Instance(n, n, n, a, 2e-3, 300.0, origin=(-5.0, -5.0, -5.0), trap=(1.0, 1.0, 4.0))
+    rng = np.random.default_rng(31)
+    psi = np.exp(1j * rng.uniform(0, 2 * np.pi, size=(n, n, n, 2)))
+    res = {}
+    for prec in (Precision.FP64, Precision.FP32):
+        st = Stepper([inst], lattice=Lattice.BCC2, precision=prec, mode=Mode.IMAGINARY, kernel=Kernel.FUSED,
+                     potential=Potential.TRAP, graph_steps=100)
+        st.upload(0, psi)
+        res[prec] = st.imaginary_time(60000, 1e-9)
+        st.close()
+    s64, c64, mu64 = res[Precision.FP64]
+    s32, c32, mu32 = res[Precision.FP32]
+    assert c64 and c32
+    assert s32 <= 1.5 * s64 + 200
+    assert mu32[0] == pytest.approx(mu64[0], rel=1e-6)

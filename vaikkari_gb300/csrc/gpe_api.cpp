@@ -914,7 +914,7 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
         for (int i = 0; i < cfg->num_instances; i++) {
             const gpe_instance &in = h->inst[i];
             const int zc = plain_planes_per_thread((long long)in.nx * in.ny * in.nz * h->ns, cfg->precision);
-            const long long blocks = (long long)((in.nx + 31) / 32) * ((in.ny + 7) / 8) * ((in.nz + zc - 1) / zc) * h->ns;
+            const long long blocks = (long long)plain_blocks_per_plane(in.nx, in.ny) * ((in.nz + zc - 1) / zc) * h->ns;
             if ((long long)pb_begin[i] + blocks > 0x7fffffffll) {
                 pb_begin.clear();
                 break;  // too many CTAs for one launch: keep one launch per instance

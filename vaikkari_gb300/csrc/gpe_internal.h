@@ -69,6 +69,8 @@ struct StepLaunch {
 cudaError_t launch_plain_step(const StepLaunch &l, cudaStream_t s);
 // Planes each thread of the plain kernel marches for an instance of `values` values.
 int plain_planes_per_thread(long long values, int precision);
+// CTAs of the plain kernel per slot plane of an nx x ny instance.
+int plain_blocks_per_plane(int nx, int ny);
 // The plain step of every instance in one launch (tables from the handle).
 struct PlainBatchLaunch {
     int lattice, precision, mode, potential;

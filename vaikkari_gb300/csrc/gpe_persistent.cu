@@ -17,18 +17,18 @@
 // Ordering without a grid barrier: item X at half-step h reads the field its
 // neighbours wrote at half-step h-1 (halo), and rewrites the field they read
 // at h-1, so it may start once every item within one tile / one z-chunk of it
-// (at most 27, itself included) has finished h-1.  Each item has a counter
-// done[X] of consumer-warp completions since the handle was created: with W
-// consumer warps per CTA, X has finished half-step h when done[X] reaches
-// W * (epoch0 + h + 1).
+// (at most 27, itself included) has finished h-1.  Each item has an epoch
+// word done[X], the half-steps it has completed since the handle was created.
 //   * publish: after the item's last plane every consumer thread fences its
-//     stores into the async proxy, the warp synchronises, and lane 0 adds 1 to
-//     done[X] with release semantics at GPU scope - each warp on its own, so no
-//     warp waits for the others at an item boundary;
+//     stores into the async proxy and each consumer warp arrives (CTA scope) on
+//     a slot of a small publication ring in shared memory.  A publisher warp
+//     waits for all consumer warps of the slot, fences at GPU scope (making
+//     their stores visible, by cumulativity) and adds 1 to done[X] with release
+//     semantics.  The consumer warps never stall on a GPU-scope fence; they run
+//     up to kPub items ahead of the publisher;
 //   * wait: before issuing item X at half-step h, lane j of the producer warp
-//     polls done[neighbour j] with acquire loads until it reaches
-//     W * (epoch0 + h); lane 0 then fences into the async proxy and issues the
-//     TMA copies.
+//     polls done[neighbour j] with acquire loads until it reaches epoch0 + h;
+//     lane 0 then fences into the async proxy and issues the TMA copies.
 // The producer runs ahead of its consumers by the ring's depth across item and
 // half-step boundaries, so the pipeline does not drain between half-steps, and
 // small and large instances of a batch advance independently.  No CTA waits
@@ -62,7 +62,7 @@ struct PersistArgs {
     unsigned long long *ticket;  // ticket counter, zero at launch
     const int *nbr_begin;        // [num_items + 1]: CSR rows of nbr
     const int *nbr;              // the items each item depends on (itself included)
-    unsigned int *done;          // per item: consumer-warp completions (W per half-step)
+    unsigned int *done;          // per item: half-steps completed
     unsigned int epoch0;         // half-steps every item had completed when this launch starts
     int half_steps;              // half-steps this launch advances (odd <- even first)
     int *err;
@@ -97,13 +97,20 @@ __device__ __forceinline__ bool wait_epoch(const unsigned *p, unsigned need, con
     }
 }
 
+constexpr int kPub = 4;  // publication ring slots
+
+// Threads of a persistent CTA: the consumer warps, the producer warp, the publisher warp.
+template <typename T, int TX, int TY> constexpr int persistent_threads() { return TX * TY + 64; }
+
 template <typename T, int TX, int TY, int MODE, int POT, int STAGES, int MINB>
-__global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) persistent_bcc2_kernel(const PersistArgs a)
+__global__ void __launch_bounds__(persistent_threads<T, TX, TY>(), MinBlocks<T, MINB>::value)
+    persistent_bcc2_kernel(const PersistArgs a)
 {
     static_assert(MODE == 0 || (MODE == 2 && sizeof(T) == 4), "real time: plain or compensated FP32 storage");
     using S = FusedShape<T, TX, TY, MODE == 2>;
     constexpr int NT = S::NT;
-    constexpr int NWARPS = S::NTHREADS / 32;
+    constexpr int NCW = NT / 32;  // consumer warps
+    constexpr int PRODUCER = NCW, PUBLISHER = NCW + 1;
     extern __shared__ unsigned char dyn_smem[];
     const uint32_t raw = smem_u32(dyn_smem);
     const uint32_t base = (raw + 127u) & ~127u;
@@ -112,6 +119,8 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) persis
     const uint32_t empty = full + 8 * STAGES;
     __shared__ volatile int abort_flag;
     __shared__ unsigned long long stage_tag[STAGES];  // ticket whose first plane a stage holds
+    __shared__ __align__(8) unsigned long long pub_bar[2 * kPub];  // [slot] full (NCW arrivals), empty (1)
+    __shared__ int pub_item[kPub];                                  // item of the slot, -1 = no more
     constexpr unsigned long long kEnd = ~0ull;
 
     const int tid = threadIdx.x;
@@ -122,13 +131,30 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) persis
             mbar_init(full + 8 * st, 1);
             mbar_init(empty + 8 * st, NT / 32);
         }
+        for (int j = 0; j < kPub; j++) {
+            mbar_init(smem_u32(&pub_bar[2 * j]), NCW);
+            mbar_init(smem_u32(&pub_bar[2 * j + 1]), 1);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     const unsigned long long N = (unsigned long long)a.num_items;
     const unsigned long long total = (unsigned long long)a.half_steps * N;
 
-    if (warp == NWARPS - 1) {
+    if (warp == PUBLISHER) {
+        // ---- publisher warp: makes each finished item visible at GPU scope --
+        if (lane == 0) {
+            for (int m = 0;; m++) {
+                const int j = m % kPub;
+                if (!mbar_wait_watched<true>(smem_u32(&pub_bar[2 * j]), (m / kPub) & 1, a.err)) break;
+                const int it = pub_item[j];
+                if (it < 0) break;
+                __threadfence();  // the consumers' stores, seen through the slot's barrier, come first
+                red_release_gpu_add(a.done + it, 1u);
+                mbar_arrive(smem_u32(&pub_bar[2 * j + 1]));
+            }
+        }
+    } else if (warp == PRODUCER) {
         // ---- producer warp: tickets and dependency polls on all lanes, TMA issue on lane 0
         int issued = 0;
         bool ended = false;  // the end-of-work plane went out
@@ -152,7 +178,7 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) persis
                 break;
             }
             const int h = int(t / N), it = int(t % N);
-            const unsigned need = unsigned(NT / 32) * (a.epoch0 + unsigned(h));
+            const unsigned need = a.epoch0 + unsigned(h);
             const int nb0 = a.nbr_begin[it], nbn = a.nbr_begin[it + 1] - nb0;
             const bool ready = lane >= nbn || wait_epoch(a.done + a.nbr[nb0 + lane], need, a.err, &abort_flag);
             if (__any_sync(0xffffffffu, !ready)) {
@@ -180,9 +206,24 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) persis
         // phases have then moved past the ones a drain would test).
         if (lane == 0 && !ended) drain_ring<STAGES>(issued, full);
     } else {
-        // ---- consumer warps: each publishes its own part of an item ---------
-        int kb = 0;
+        // ---- consumer warps: finished items go to the publisher ------------
+        int kb = 0, m = 0;
         Acc<T> acc[4];
+        // slot m of the publication ring takes item `item` (-1: no more); false
+        // if the wait for a free slot ran out (the error word is then set)
+        auto hand_over = [&](int item) -> bool {
+            bool ok = true;
+            if (lane == 0) {
+                const int j = m % kPub;
+                if (m >= kPub) ok = mbar_wait_watched<true>(smem_u32(&pub_bar[2 * j + 1]), ((m / kPub) - 1) & 1, a.err);
+                if (ok) {
+                    pub_item[j] = item;  // every warp writes the same value
+                    mbar_arrive(smem_u32(&pub_bar[2 * j]));
+                }
+            }
+            m++;
+            return __shfl_sync(0xffffffffu, ok, 0);
+        };
         while (true) {
             // the ticket of the next item, from the tag of its first plane's stage
             const int st = kb % STAGES;
@@ -193,7 +234,10 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) persis
                 break;
             }
             const unsigned long long t = stage_tag[st];
-            if (t == kEnd) break;
+            if (t == kEnd) {
+                hand_over(-1);
+                break;
+            }
             const int h = int(t / N), it = int(t % N);
             void *next = (h & 1) ? a.field[0] : a.field[1];  // selects, so the argument arrays stay in registers
             uint32_t *next_lo = (h & 1) ? a.lo[0] : a.lo[1];
@@ -207,7 +251,11 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) persis
             kb += w.z1 - w.z0 + 2;
             fence_proxy_async_global();  // this thread's stores, before other CTAs' TMA reads of them
             __syncwarp();
-            if (lane == 0) red_release_gpu_add(a.done + it, 1u);
+            if (!hand_over(it)) {
+                atomicExch(a.err, kErrTimeout);
+                abort_flag = 1;
+                break;
+            }
         }
     }
 }
@@ -219,7 +267,7 @@ struct PVariant {
     int tx, ty, stages, minb;
 };
 static const PVariant kPersistVariants[] = {
-    {32, 4, 8, 5}, {32, 8, 6, 3}, {32, 4, 8, 4}, {32, 2, 8, 8}, {64, 4, 4, 3}, {32, 8, 6, 2},
+    {32, 8, 6, 2}, {32, 4, 8, 4}, {32, 2, 8, 6}, {64, 4, 4, 2}, {32, 16, 4, 1}, {16, 8, 6, 4},
 };
 constexpr int kPersistCount = int(sizeof(kPersistVariants) / sizeof(kPersistVariants[0]));
 
@@ -238,7 +286,7 @@ static cudaError_t launch_p(const PersistArgs &a, cudaStream_t s, int device, in
 {
     const int bytes = fused_smem_bytes<T, TX, TY, ST, MODE == 2>(0);
     auto kern = persistent_bcc2_kernel<T, TX, TY, MODE, POT, ST, MB>;
-    constexpr int threads = FusedShape<T, TX, TY>::NTHREADS;
+    constexpr int threads = persistent_threads<T, TX, TY>();
     static int resident = 0;  // CTAs per SM of this instantiation (the same on every GB300)
     if (resident == 0) {
         if (bytes > 48 * 1024) {
@@ -286,12 +334,12 @@ template <typename T>
 static cudaError_t launch_p_variant(const PersistLaunch &l, const PersistArgs &a, cudaStream_t s, int *grid)
 {
     switch (l.variant) {  // must list kPersistVariants in order
-    case 1: return launch_p_mode<T, 32, 8, 6, 3>(l, a, s, grid);
-    case 2: return launch_p_mode<T, 32, 4, 8, 4>(l, a, s, grid);
-    case 3: return launch_p_mode<T, 32, 2, 8, 8>(l, a, s, grid);
-    case 4: return launch_p_mode<T, 64, 4, 4, 3>(l, a, s, grid);
-    case 5: return launch_p_mode<T, 32, 8, 6, 2>(l, a, s, grid);
-    default: return launch_p_mode<T, 32, 4, 8, 5>(l, a, s, grid);
+    case 1: return launch_p_mode<T, 32, 4, 8, 4>(l, a, s, grid);
+    case 2: return launch_p_mode<T, 32, 2, 8, 6>(l, a, s, grid);
+    case 3: return launch_p_mode<T, 64, 4, 4, 2>(l, a, s, grid);
+    case 4: return launch_p_mode<T, 32, 16, 4, 1>(l, a, s, grid);
+    case 5: return launch_p_mode<T, 16, 8, 6, 4>(l, a, s, grid);
+    default: return launch_p_mode<T, 32, 8, 6, 2>(l, a, s, grid);
     }
 }
 

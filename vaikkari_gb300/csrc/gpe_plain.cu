@@ -136,20 +136,26 @@ cudaError_t set_plain_table(const gpe_lattice_info &info)
 // planes z0 .. z0+zc-1: the neighbours' offsets from the value are the same on
 // every plane, so they are formed once and each plane only advances the index
 // by one z-stride (the per-value arithmetic does not depend on this).
-// (bx, by, bz): the CTA's block of the instance's grid (32 x 8 threads,
-// bz = plane chunk * slots + slot).
+// (bx, bz): the CTA's block of the instance's grid (256 threads, bz = plane
+// chunk * slots + slot).  The values of a slot's plane are numbered x fastest
+// and CTA bx takes values 256 bx .. 256 bx + 255 of it, so that every warp but
+// a plane's last is full.  (With 32 x 8 tiles, a plane whose nx is not a
+// multiple of 32 left lanes idle in every warp of its last tile column - 87 of
+// 96 lanes busy for nx = 87 - and those lanes still took issue slots and, in
+// FP64, the FP64 pipe that bounds the path.)
 template <typename T, int LAT, int MODE, int POT>
 __device__ __forceinline__ void plain_step_body(const InstDev *__restrict__ insts, int ii,
                                                 const typename Cplx<T>::type *__restrict__ prev,
                                                 typename Cplx<T>::type *__restrict__ next,
                                                 const T *__restrict__ vpot, const ImagScalars *__restrict__ imag, int zc,
-                                                int bx, int by, int bz)
+                                                int bx, int bz)
 {
     using T2 = typename Cplx<T>::type;
     using L = Lat<LAT>;
     const InstDev &d = insts[ii];
-    const int x = bx * 32 + threadIdx.x;
-    const int y = by * 8 + threadIdx.y;
+    const int l = bx * 256 + threadIdx.y * 32 + threadIdx.x;
+    const int y = l / d.nx;
+    const int x = l - y * d.nx;
     const int s = bz % L::NS;
     const int z0 = (bz / L::NS) * zc;
     if (x >= d.nx || y >= d.ny) return;
@@ -234,11 +240,16 @@ __global__ void __launch_bounds__(256) plain_step_kernel(const InstDev *__restri
                                                          const T *__restrict__ vpot, const ImagScalars *__restrict__ imag,
                                                          int zc)
 {
-    plain_step_body<T, LAT, MODE, POT>(insts, ii, prev, next, vpot, imag, zc, blockIdx.x, blockIdx.y, blockIdx.z);
+    plain_step_body<T, LAT, MODE, POT>(insts, ii, prev, next, vpot, imag, zc, blockIdx.x, blockIdx.z);
 }
 
+// CTAs of the plain kernel per slot plane: 256 consecutive values each.
+__host__ __device__ inline int plain_plane_ctas(int nx, int ny) { return int(((long long)nx * ny + 255) / 256); }
+
+int plain_blocks_per_plane(int nx, int ny) { return plain_plane_ctas(nx, ny); }
+
 // Every instance of a batch in one launch: CTA b is block b - blk_begin[i] of
-// instance i = blk_inst[b], numbered x fastest, then y, then z chunk and slot, as
+// instance i = blk_inst[b], numbered along the plane first, then z chunk and slot, as
 // in that instance's own launch (same values per thread, same results).
 template <typename T, int LAT, int MODE, int POT>
 __global__ void __launch_bounds__(256) plain_step_batch_kernel(const InstDev *__restrict__ insts,
@@ -253,10 +264,9 @@ __global__ void __launch_bounds__(256) plain_step_batch_kernel(const InstDev *__
     const int i = blk_inst[blockIdx.x];
     const int local = blockIdx.x - blk_begin[i];
     const InstDev &d = insts[i];
-    const int gx = (d.nx + 31) / 32, gy = (d.ny + 7) / 8;
+    const int gx = plain_plane_ctas(d.nx, d.ny);
     const int rest = local / gx;
-    plain_step_body<T, LAT, MODE, POT>(insts, i, prev, next, vpot, imag, zcs[i], local - rest * gx, rest % gy,
-                                       rest / gy);
+    plain_step_body<T, LAT, MODE, POT>(insts, i, prev, next, vpot, imag, zcs[i], local - rest * gx, rest);
 }
 
 // Planes per thread.  FP32 is issue-bound, so fewer index computations per value
@@ -284,7 +294,7 @@ static cudaError_t plain_dispatch_mode(const StepLaunch &l, cudaStream_t st)
     using T2 = typename Cplx<T>::type;
     const int zc = plain_zchunk((long long)l.nx * l.ny * l.nz * Lat<LAT>::NS, sizeof(T) == 8);
     dim3 block(32, 8, 1);
-    dim3 grid((l.nx + 31) / 32, (l.ny + 7) / 8, ((l.nz + zc - 1) / zc) * Lat<LAT>::NS);
+    dim3 grid(plain_plane_ctas(l.nx, l.ny), 1, ((l.nz + zc - 1) / zc) * Lat<LAT>::NS);
     const T2 *prev = (const T2 *)l.prev;
     T2 *next = (T2 *)l.next;
     const T *v = (const T *)(l.potential == GPE_POTENTIAL_ARRAY && LAT != kStepTetra12Faces ? l.vbase : l.vpot);
