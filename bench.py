@@ -837,7 +837,7 @@ def _windowed_rate(st, verts, steps, sample_clocks, prec, kern, tile, seconds=1.
     achieved = verts * per_value_half * half_steps / (ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None, "traffic_source": "not captured for this workload",
-            "algorithmic_bytes_per_vertex_step": 2 * per_value_half, "launches_per_window": launches,
+            "algorithmic_bytes_per_vertex_step": per_value_half * half_steps // steps, "launches_per_window": launches,
             "peak_source": f"{kind} hbm_gbs (of {kind})"}
     return verts * steps / (ms * 1e-3), roof, (clk.summary() if sample_clocks else None)
 
@@ -866,8 +866,8 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1, latti
             st.upload(i, c.psi)
         t0 = time.perf_counter()
         # Both run to the criterion: FP64 tests |dmu| < tol every step; FP32
-        # tests the mean |dmu| per step over each chunk of 100 steps with mu from
-        # the FP64 observables (gpe_imaginary_time).
+        # tests the mean |dmu| per step over the last 1000 steps with mu from the
+        # FP64 observables (gpe_imaginary_time).
         lim, crit = max_steps, tol
         steps, conv, mu = st.imaginary_time(lim, crit)
         st.synchronize()

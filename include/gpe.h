@@ -232,9 +232,9 @@ gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out
  * default).  GPE_FP64: mu comes from the reductions fused into every step and
  * the test runs on the device each step; the host polls between chunks.
  * GPE_FP32: mu of the normalised field is taken from the FP64 observables after
- * each chunk, and the test is |mu_k - mu_{k-G}| < G * tol (the mean change per
- * step over the chunk), because the per-step change of an FP32 field's mu is
- * below the resolution of sums over FP32 values.  Outputs may be NULL; mu_out
+ * each chunk, and the test is |mu_k - mu_{k-W}| < W * tol over the last W = 10 G
+ * steps (the mean change per step over that window), because the per-step
+ * change of an FP32 field's mu is below the resolution of sums over FP32 values.  Outputs may be NULL; mu_out
  * receives the last mu of each instance. */
 gpe_status gpe_imaginary_time(gpe_handle h, int64_t max_steps, double tol, int64_t *steps_done,
                               int32_t *converged, double *mu_out);

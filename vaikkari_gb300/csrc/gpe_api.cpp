@@ -1477,10 +1477,12 @@ static gpe_status gpe_imaginary_time_impl(gpe_handle h, int64_t max_steps, doubl
     // FP64: the per-step test |mu_k - mu_(k-1)| < tol on the device, as the
     // reductions fused into each step compute mu.  FP32: a per-step difference
     // of mu taken from FP32 values is not resolvable at tol (a step can change
-    // no stored value, or change it by less than the sums' rounding), so the
-    // test runs once per chunk of G steps on mu from the FP64 observables of the
-    // normalised field: converged when |mu_k - mu_(k-G)| < G * tol, i.e. the
-    // mean change per step over the chunk is below tol.
+    // no stored value, or change it by less than the sums' rounding), so after
+    // every chunk of G steps mu of the normalised field is taken from the FP64
+    // observables, and the run has converged when |mu_k - mu_(k-W)| < W * tol
+    // over the last W = kWindowChunks * G steps: the mean change per step over
+    // that window is below tol.  A window of one chunk stopped a 128^3
+    // random-phase start on a slow plateau, 1e-4 above the FP64 run's mu.
     const bool windowed = h->cfg.precision != GPE_FP64;
     h->tol = windowed ? 0.0 : tol;
     st = imag_prepare(h);
@@ -1491,8 +1493,9 @@ static gpe_status gpe_imaginary_time_impl(gpe_handle h, int64_t max_steps, doubl
     const int n_inst = h->cfg.num_instances;
     std::vector<ImagScalars> sc(n_inst);
     std::vector<gpe_observables> obs(n_inst);
-    std::vector<double> mu(n_inst, 0.0), mu_prev(n_inst, 0.0);
-    bool have_prev = false;
+    constexpr int kWindowChunks = 10;
+    std::vector<double> mu(n_inst, 0.0);
+    std::vector<std::vector<double>> hist;  // mu after each of the last kWindowChunks full chunks
     while (done < max_steps) {
         const long long n = std::min<long long>(G, max_steps - done);
         st = run_steps(h, n);
@@ -1503,13 +1506,14 @@ static gpe_status gpe_imaginary_time_impl(gpe_handle h, int64_t max_steps, doubl
         if (windowed) {
             st = gpe_observables_get_impl(h, 0, obs.data());
             if (st != GPE_OK) return st;
-            all = have_prev && n == G;
-            for (int i = 0; i < n_inst; i++) {
-                mu[i] = obs[i].mu;
-                all = all && std::fabs(mu[i] - mu_prev[i]) < double(n) * tol;
+            for (int i = 0; i < n_inst; i++) mu[i] = obs[i].mu;
+            all = n == G && int(hist.size()) == kWindowChunks;
+            for (int i = 0; all && i < n_inst; i++)
+                all = std::fabs(mu[i] - hist.front()[i]) < double(kWindowChunks * G) * tol;
+            if (n == G) {
+                hist.push_back(mu);
+                if (int(hist.size()) > kWindowChunks) hist.erase(hist.begin());
             }
-            mu_prev = mu;
-            have_prev = true;
         } else {
             GPE_CUDA_TRY(cudaMemcpyAsync(sc.data(), h->imag, sizeof(ImagScalars) * sc.size(), cudaMemcpyDeviceToHost,
                                          h->stream));
