@@ -33,7 +33,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "vertex-updates/s"
 BYTES_PER_VERTEX_STEP = 48  # FP32, trap potential in-kernel: 2 half-steps x (read prev 8 B + RMW next 16 B)
-BYTES_PER_VERTEX_STEP_COMP = 64  # FP32C: plus the next field's bf16x2 residual, read and written (2 x 8 B)
+BYTES_PER_VERTEX_STEP_COMP = 56  # FP32C: plus the next field's int8 x 2 residual, read and written (2 x 4 B)
 L2_BYTES = 129e6
 HEADLINE_WORKLOAD = "batch64_bcc2_trap_realtime"
 
@@ -535,7 +535,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": args.scaling, "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": HEADLINE_WORKLOAD,
-                       "storage": "fp32 + bf16 residual (GPE_FP32C)" if comp_main else "fp32",
+                       "storage": "fp32 + int8 residual per component (GPE_FP32C)" if comp_main else "fp32",
                        "instances": len(insts), "vertices": verts, "vertices_all_ranks": verts_job,
                        "sizes": sorted({i.nx for i in insts}), "dt": 1e-4,
                        "graph_steps": gsteps, "kernel": "fused", "variant": tile, "zchunk": zchunk,
@@ -649,7 +649,7 @@ def storage_block(conds, insts, device, steps, warmup, window_seconds, prec, tun
                           "fused_bcc2_fp32c_batch64.md" if comp else "fused_bcc2_batch64.md", tile)
     return {"value": verts * steps / (ms * 1e-3), "unit": METRIC, "ms_per_step": ms / steps, "steps": steps,
             "windows": len(times), "variant": tile, "zchunk": zchunk, "gpu_launches": launches, "roofline": roof,
-            "storage": ("FP32 value + bf16 residual per component (12 B per value and field)" if comp
+            "storage": ("FP32 value + int8 residual per component (10 B per value and field)" if comp
                         else "FP32 (8 B per value and field)")}
 
 
@@ -804,7 +804,7 @@ def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1, latt
 def _windowed_rate(st, verts, steps, sample_clocks, prec, kern, tile, seconds=1.0, imaginary=False):
     """Vertex-updates/s of a prepared stepper: median of windows of `steps`
     steps after one untimed call; the roofline at the algorithmic bytes of the
-    trap form (real time: 24 B per value and half-step in FP32, 32 B in FP32C,
+    trap form (real time: 24 B per value and half-step in FP32, 28 B in FP32C,
     48 B in FP64; the two-step variants move 16 / 32 B per value and half-step;
     imaginary time: one pass per step reading psi and writing the next field,
     16 B per value in FP32, 32 B in FP64)."""
@@ -825,7 +825,7 @@ def _windowed_rate(st, verts, steps, sample_clocks, prec, kern, tile, seconds=1.
             clk.__exit__()
     ms = statistics.median(times)
     half_steps = steps if imaginary else 2 * steps
-    per_value_half = {Precision.FP32: 24, Precision.FP32C: 32, Precision.FP64: 48}[prec]
+    per_value_half = {Precision.FP32: 24, Precision.FP32C: 28, Precision.FP64: 48}[prec]
     if imaginary:
         per_value_half = {Precision.FP32: 16, Precision.FP64: 32}[prec]
     vinfo = {v["tile"]: v for v in variants()}
@@ -1179,7 +1179,7 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-comp", action="store_true", help="skip the timing of the other FP32 storage")
     ap.add_argument("--precision", default="fp32c", choices=["fp32", "fp32c"],
-                    help="batch64: storage of the timed path (fp32c = FP32 + bf16 residual, the storage that "
+                    help="batch64: storage of the timed path (fp32c = FP32 + int8 residuals, the storage that "
                          "meets relative L2 <= 1e-5 after 1000 steps; fp32 = plain FP32)")
     ap.add_argument("--window-seconds", type=float, default=2.0,
                     help="keep timing windows of --steps steps for at least this long (median reported)")

@@ -28,8 +28,8 @@
  * for block (x, y, z) and value `slot` of that block; complex values are
  * interleaved (re, im).  The element type follows the handle's precision
  * (double for GPE_FP64, float for GPE_FP32).  GPE_FP32C exchanges the fields
- * as double (each value is split into an FP32 value and a bf16 residual on
- * upload and recombined on download) and potential arrays as float.
+ * as double (each value is split into an FP32 value and an int8 residual per
+ * component on upload and recombined on download) and potential arrays as float.
  *
  * Threading: one handle per host thread; a handle owns its CUDA stream.
  */
@@ -69,12 +69,12 @@ typedef enum gpe_lattice {
     GPE_LATTICE_BCC2 = 1
 } gpe_lattice;
 
-/* GPE_FP32C: FP32 fields and arithmetic, and in real time a bf16 residual per
- * component carried from step to step, so that the accumulation of the leapfrog
- * sums loses about 8 bits less per step than FP32 storage (the stored field
- * rounds with an exact two-sum and keeps its rounding error).  BCC2, fused
- * kernel, real time, one-half-step variants only; 12 instead of 8 bytes per
- * value of a field. */
+/* GPE_FP32C: FP32 fields and arithmetic, and in real time an int8 residual per
+ * component, in units of that component's ulp / 256, carried from step to step,
+ * so that the accumulation of the leapfrog sums loses about 8 bits less per step
+ * than FP32 storage (the stored field rounds with an exact two-sum and keeps its
+ * rounding error).  BCC2, fused kernel (one-half-step and persistent variants),
+ * real time; 10 instead of 8 bytes per value of a field. */
 typedef enum gpe_precision { GPE_FP64 = 0, GPE_FP32 = 1, GPE_FP32C = 2 } gpe_precision;
 
 typedef enum gpe_time_mode {
@@ -209,7 +209,7 @@ gpe_status gpe_download_many(gpe_handle h, int32_t count, const int32_t *instanc
 
 /* Element type of the host field arrays of gpe_upload/gpe_download and their
  * batched forms.  A GPE_FP32C handle exchanges double by default (each value
- * split into its FP32 value and bf16 residual on upload, recombined on
+ * split into its FP32 value and int8 residuals on upload, recombined on
  * download); with GPE_FP32 it exchanges float: an upload sets the residual to
  * zero, a download rounds value + residual to float once.  That halves the host
  * link traffic for callers whose data are single precision; the residual still

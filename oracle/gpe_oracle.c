@@ -26,21 +26,30 @@ int oracle_get_threads(void)
 #endif
 }
 
-/* bf16 with round-to-nearest-even on the bit pattern (finite inputs), and back. */
-static inline uint16_t bf16_rn(float f)
+/* Compensated storage (GPE_FP32C): the residual of a stored FP32 value s as an
+ * int8 q in units of ulp(s)/256.  unit(s) = 2^(E - 31 - 127) for the biased
+ * exponent E of s, E raised to 32 below 2^-95; q = the residual in units,
+ * rounded to nearest even (rintf in the default rounding mode) and clipped to
+ * +-127.  Scaling by the power of two unit(s) is exact. */
+static inline float comp_unit(float s)
 {
     uint32_t u;
-    memcpy(&u, &f, 4);
-    u += 0x7fffu + ((u >> 16) & 1u);
-    return (uint16_t)(u >> 16);
-}
-static inline float bf16_value(uint16_t b)
-{
-    const uint32_t u = (uint32_t)b << 16;
+    memcpy(&u, &s, 4);
+    u &= 0x7f800000u;
+    if (u < (32u << 23)) u = 32u << 23;
+    u -= 31u << 23;
     float f;
     memcpy(&f, &u, 4);
     return f;
 }
+static inline int8_t comp_encode(float r, float s)
+{
+    float q = rintf(r / comp_unit(s));
+    if (q > 127.0f) q = 127.0f;
+    if (q < -127.0f) q = -127.0f;
+    return (int8_t)q;
+}
+static inline float comp_decode(int8_t q, float s) { return (float)q * comp_unit(s); }
 
 #define IDX(g, x, y, z, s) (((((size_t)(z) * (g)->ny) + (size_t)(y)) * (g)->nx + (size_t)(x)) * (g)->slots + (size_t)(s))
 
@@ -281,17 +290,17 @@ void oracle_leapfrog_faces_f32(int nx, int ny, int nz, const int *face, const fl
                     ay = FMA(Lc1, say, ay);                                                         \
                     const T hx = FMA(cc, px, ax), hy = FMA(cc, py, ay);                             \
                     if (mode == 0 && next_lo) { /* compensated storage: exact two-sum */            \
-                        const T tx = (T)bf16_value(next_lo[2 * o]) + hy;                            \
-                        const T ty = (T)bf16_value(next_lo[2 * o + 1]) - hx;                        \
                         const T ux = next[2 * o], uy = next[2 * o + 1];                             \
+                        const T tx = (T)comp_decode(next_lo[2 * o], (float)ux) + hy;                \
+                        const T ty = (T)comp_decode(next_lo[2 * o + 1], (float)uy) - hx;            \
                         const T wx = ux + tx, wy = uy + ty;                                         \
                         const T bx = wx - ux, by = wy - uy;                                         \
                         const T rx = (ux - (wx - bx)) + (tx - bx);                                  \
                         const T ry = (uy - (wy - by)) + (ty - by);                                  \
                         next[2 * o] = wx;                                                           \
                         next[2 * o + 1] = wy;                                                       \
-                        next_lo[2 * o] = bf16_rn((float)rx);                                        \
-                        next_lo[2 * o + 1] = bf16_rn((float)ry);                                    \
+                        next_lo[2 * o] = comp_encode((float)rx, (float)wx);                         \
+                        next_lo[2 * o + 1] = comp_encode((float)ry, (float)wy);                     \
                     } else if (mode == 0) {                                                         \
                         next[2 * o] = next[2 * o] + hy;                                             \
                         next[2 * o + 1] = next[2 * o + 1] - hx;                                     \
@@ -306,7 +315,7 @@ void oracle_leapfrog_faces_f32(int nx, int ny, int nz, const int *face, const fl
 void oracle_half_step_bcc2_f64(const oracle_grid *g, const double *prev, double *next, const double *vdt, int mode,
                                double sigma)
 {
-    uint16_t *const next_lo = NULL;
+    int8_t *const next_lo = NULL;
     BCC2_BODY(double, fma)
 }
 
@@ -391,13 +400,13 @@ static void bcc2_value_f64(const oracle_grid *g0, const double *prev, double *ne
 void oracle_half_step_bcc2_f32(const oracle_grid *g, const float *prev, float *next, const float *vdt, int mode,
                                float sigma)
 {
-    uint16_t *const next_lo = NULL;
+    int8_t *const next_lo = NULL;
     BCC2_BODY(float, fmaf)
 }
 
-/* Real time with compensated storage (GPE_FP32C): next_lo holds a bf16 residual
- * per component, (re, im) per value in block order. */
-void oracle_half_step_bcc2_f32c(const oracle_grid *g, const float *prev, float *next, uint16_t *next_lo,
+/* Real time with compensated storage (GPE_FP32C): next_lo holds the int8
+ * residual of each component (comp_encode), (re, im) per value in block order. */
+void oracle_half_step_bcc2_f32c(const oracle_grid *g, const float *prev, float *next, int8_t *next_lo,
                                 const float *vdt)
 {
     const int mode = 0;
@@ -406,7 +415,7 @@ void oracle_half_step_bcc2_f32c(const oracle_grid *g, const float *prev, float *
     BCC2_BODY(float, fmaf)
 }
 
-void oracle_leapfrog_bcc2_f32c(const oracle_grid *g, float *even, float *odd, uint16_t *even_lo, uint16_t *odd_lo,
+void oracle_leapfrog_bcc2_f32c(const oracle_grid *g, float *even, float *odd, int8_t *even_lo, int8_t *odd_lo,
                                const float *vdt, long steps)
 {
     for (long k = 0; k < steps; k++) {

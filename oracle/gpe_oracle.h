@@ -65,10 +65,10 @@ void oracle_leapfrog_bcc2_f64(const oracle_grid *g, double *even, double *odd, c
 void oracle_leapfrog_bcc2_f32(const oracle_grid *g, float *even, float *odd, const float *vdt, long steps);
 /* BCC2 real time with compensated storage: next += -i h as an exact two-sum of
  * the stored FP32 value and (residual + increment); the rounding error is kept
- * as a bf16 residual per component (re, im per value, block order). */
-void oracle_half_step_bcc2_f32c(const oracle_grid *g, const float *prev, float *next, uint16_t *next_lo,
+ * as an int8 residual per component in units of ulp/256 (re, im per value, block order). */
+void oracle_half_step_bcc2_f32c(const oracle_grid *g, const float *prev, float *next, int8_t *next_lo,
                                 const float *vdt);
-void oracle_leapfrog_bcc2_f32c(const oracle_grid *g, float *even, float *odd, uint16_t *even_lo, uint16_t *odd_lo,
+void oracle_leapfrog_bcc2_f32c(const oracle_grid *g, float *even, float *odd, int8_t *even_lo, int8_t *odd_lo,
                                const float *vdt, long steps);
 
 /* The BCC2 real-time half-step/leapfrog with direct indexing for interior values

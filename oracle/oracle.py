@@ -100,27 +100,36 @@ def factors(class_weight, entry_classes, block_scale, dt, g):
     return {"Lc": Lc, "L0": L0, "gdt": g * dt, "w": w + [0.0] * (2 - len(w))}
 
 
-def bf16_rn(x):
-    """float32 -> bf16 bits (uint16), round to nearest even (finite values)."""
-    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
-    return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+def comp_unit(hi):
+    """The residual unit of stored FP32 values: ulp(hi)/256 = 2^(E - 31 - 127) for
+    the biased exponent E of hi, E raised to 32 below 2^-95 (float32)."""
+    e = np.asarray(hi, np.float32).view(np.uint32) & np.uint32(0x7F800000)
+    e = np.maximum(e, np.uint32(32 << 23))
+    return (e - np.uint32(31 << 23)).astype(np.uint32).view(np.float32)
 
 
-def bf16_value(b):
-    """bf16 bits (uint16) -> float32."""
-    return (np.asarray(b, np.uint16).astype(np.uint32) << 16).view(np.float32)
+def comp_encode(r, hi):
+    """int8 residuals: r / unit(hi) rounded to nearest even, clipped to +-127."""
+    q = np.rint(np.asarray(r, np.float32) / comp_unit(hi))
+    return np.clip(q, -127, 127).astype(np.int8)
+
+
+def comp_decode(q, hi):
+    """float32 value of int8 residuals q of stored values hi."""
+    return np.asarray(q, np.int8).astype(np.float32) * comp_unit(hi)
 
 
 def split_comp(x):
-    """Compensated storage of float64 values: hi = float32(x), lo = bf16(float32(x - hi))."""
+    """Compensated storage of float64 values: hi = float32(x), lo = the int8
+    residual of float32(x - hi) (comp_encode)."""
     x = np.asarray(x, np.float64)
     hi = x.astype(np.float32)
-    return hi, bf16_rn((x - hi.astype(np.float64)).astype(np.float32))
+    return hi, comp_encode((x - hi.astype(np.float64)).astype(np.float32), hi)
 
 
 def join_comp(hi, lo):
-    """float64(hi) + float64(lo): the value a compensated field stands for."""
-    return hi.astype(np.float64) + bf16_value(lo).astype(np.float64)
+    """float64(hi) + float64(residual): the value a compensated field stands for."""
+    return hi.astype(np.float64) + comp_decode(lo, hi).astype(np.float64)
 
 
 class Grid:
@@ -172,9 +181,9 @@ class Grid:
 
     def leapfrog_bcc2_comp(self, even, odd, even_lo, odd_lo, vdt, steps):
         """In place, BCC2, FP32 with compensated storage: even/odd float32
-        (..., 2), even_lo/odd_lo uint16 (..., 2) bf16 residuals (split_comp)."""
+        (..., 2), even_lo/odd_lo int8 (..., 2) residuals (split_comp)."""
         lib = load()
-        assert self.slots == 2 and even.dtype == np.float32 and even_lo.dtype == np.uint16
+        assert self.slots == 2 and even.dtype == np.float32 and even_lo.dtype == np.int8
         for a in (even, odd, even_lo, odd_lo, vdt):
             assert a.flags.c_contiguous
         lib.oracle_leapfrog_bcc2_f32c(C.byref(self._g), self._p(even), self._p(odd), self._p(even_lo),

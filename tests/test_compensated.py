@@ -1,15 +1,17 @@
-"""Compensated FP32 storage (Precision.FP32C): FP32 fields and arithmetic, with a
-bf16 residual per component carried from step to step, so the leapfrog's
-accumulation of the stored values keeps about 8 bits more than FP32.
+"""Compensated FP32 storage (Precision.FP32C): FP32 fields and arithmetic, with an
+int8 residual per component, in units of ulp(value)/256, carried from step to
+step, so the leapfrog's accumulation of the stored values keeps about 8 bits
+more than FP32 at 16 bits per value.
 
-CPU: the bf16 rounding (nearest, ties to even) against a candidate-by-candidate
-reference, the float64 <-> (FP32, bf16) split and join, and the oracle's
-compensated leapfrog against FP64 of the same scheme (much closer than plain
-FP32).  GPU: the fused kernel's compensated mode equals the oracle bit for bit
-(values and residuals, through the float64 download), refuses the set-ups it
-does not cover, and keeps a strongly interacting condensate of the 64-instance
-batch within 1e-5 of FP64 after 1000 steps where plain FP32 is above 1e-4; the
-whole batch, run twice, gives identical results in FP32 and FP32C."""
+CPU: the residual code against a candidate-by-candidate reference (nearest
+multiple of the unit, ties to even, clipped to +-127), the float64 <-> (FP32,
+int8) split and join, and the oracle's compensated leapfrog against FP64 of the
+same scheme (much closer than plain FP32).  GPU: the fused kernel's compensated
+mode equals the oracle bit for bit (values and residuals, through the float64
+download), refuses the set-ups it does not cover, and keeps a strongly
+interacting condensate of the 64-instance batch within 1e-5 of FP64 after 1000
+steps where plain FP32 is above 1e-4; the whole batch, run twice, gives
+identical results in FP32 and FP32C."""
 import numpy as np
 import pytest
 
@@ -18,38 +20,50 @@ from helpers import grid_for, interleave, random_state, rel_l2, vdt_for
 from vaikkari_gb300.gpe import Instance, Kernel, Lattice, Mode, Potential, Precision, Stepper
 
 
-def _nearest_bf16_reference(x):
-    """Nearest bf16 by comparing the two bf16 neighbours of x in float64."""
-    x = np.asarray(x, np.float32)
-    u = x.view(np.uint32)
-    lo = (u >> 16).astype(np.uint32)               # truncation toward zero
-    hi = lo + 1
-    a = (lo << 16).view(np.float32).astype(np.float64)
-    b = (hi << 16).view(np.float32).astype(np.float64)
-    xv = x.astype(np.float64)
-    da, db = np.abs(xv - a), np.abs(xv - b)
-    pick_hi = (db < da) | ((db == da) & (lo % 2 == 1))
-    return np.where(pick_hi, hi, lo).astype(np.uint16)
+def _unit_reference(hi):
+    """ulp(hi)/256 from frexp, with the floor 2^-126 for tiny values."""
+    m, e = np.frexp(np.asarray(hi, np.float32).astype(np.float64))   # |hi| = m 2^e, m in [0.5, 1)
+    unit = np.ldexp(1.0, (e - 1) - 23 - 8)
+    return np.where((hi == 0) | (unit < 2.0 ** -126), 2.0 ** -126, unit)
 
 
-def test_bf16_rounding_matches_nearest_even():
+def _encode_reference(r, hi):
+    """The nearest multiple of the unit, candidate by candidate: floor and
+    floor + 1, the nearer (ties to the even one), clipped to +-127."""
+    u = _unit_reference(hi)
+    x = np.asarray(r, np.float32).astype(np.float64) / u
+    f = np.floor(x)
+    d0, d1 = x - f, f + 1 - x
+    pick = (d1 < d0) | ((d1 == d0) & (np.mod(f, 2) == 1))
+    return np.clip(np.where(pick, f + 1, f), -127, 127).astype(np.int8)
+
+
+def test_residual_code_matches_nearest_even_multiple_of_the_unit():
     rng = np.random.default_rng(0)
-    x = (rng.standard_normal(200000) * 10.0 ** rng.uniform(-44, 30, 200000)).astype(np.float32)
-    ties = (np.arange(1, 2000, dtype=np.uint32) << 16 | 0x8000).view(np.float32)   # exact halfway cases
-    special = np.array([0.0, -0.0, 1.0, -1.0, 1e-45, -1e-45, 1.17549435e-38, 3.0e38], np.float32)
-    for v in (x, ties, -ties, special):
-        np.testing.assert_array_equal(orc.bf16_rn(v), _nearest_bf16_reference(v))
-    assert orc.bf16_rn(np.float32(1.0 + 2.0 ** -8)) == 0x3F80        # tie, even below
-    assert orc.bf16_rn(np.float32(1.0 + 3 * 2.0 ** -8)) == 0x3F82    # tie, even above
+    hi = (rng.standard_normal(200000) * 10.0 ** rng.uniform(-40, 30, 200000)).astype(np.float32)
+    hi[:50] = 0.0
+    # residuals up to half an ulp of hi, as a two-sum leaves them, plus exact ties
+    r = (rng.uniform(-0.5, 0.5, hi.size) * _unit_reference(hi) * 256).astype(np.float32)
+    np.testing.assert_array_equal(orc.comp_encode(r, hi), _encode_reference(r, hi))
+    ones = np.ones(4, np.float32)
+    u = float(orc.comp_unit(ones)[0])
+    assert u == 2.0 ** -31                                                        # ulp(1) / 256
+    ties = np.array([0.5, 1.5, 2.5, -2.5], np.float32) * np.float32(u)
+    np.testing.assert_array_equal(orc.comp_encode(ties, ones), [0, 2, 2, -2])     # ties to even
+    np.testing.assert_array_equal(orc.comp_encode(np.float32(128 * u) * ones[:1], ones[:1]), [127])  # clipped
+    assert orc.comp_unit(np.float32(1e-35)) == np.float32(2.0 ** -126)           # the floor
 
 
 def test_split_join_keeps_32_bits():
     rng = np.random.default_rng(1)
     x = rng.standard_normal(100000) * 10.0 ** rng.uniform(-20, 20, 100000)
     hi, lo = orc.split_comp(x)
-    assert hi.dtype == np.float32 and lo.dtype == np.uint16
+    assert hi.dtype == np.float32 and lo.dtype == np.int8
     back = orc.join_comp(hi, lo)
-    assert np.all(np.abs(back - x) <= 2.0 ** -32 * np.abs(x))
+    # half a unit (2^-32 relative) but where a residual of half an ulp is
+    # clipped from 128 to 127 units: one unit, 2^-31
+    assert np.all(np.abs(back - x) <= 2.0 ** -31 * np.abs(x))
+    assert np.mean(np.abs(back - x) <= 2.0 ** -32 * np.abs(x)) > 0.99
     assert np.all(np.abs(hi.astype(np.float64) - x) <= 2.0 ** -24 * np.abs(x))
     np.testing.assert_array_equal(orc.join_comp(*orc.split_comp(back)), back)   # idempotent
 
@@ -243,7 +257,7 @@ def test_fp32_host_format_of_compensated_storage():
             o = interleave(random_state(shp, 95 + i, 0.3), np.float32)
             fields.append((e, o))
             eh, oh = e.copy(), o.copy()
-            el, ol = np.zeros(e.shape, np.uint16), np.zeros(o.shape, np.uint16)
+            el, ol = np.zeros(e.shape, np.int8), np.zeros(o.shape, np.int8)
             grid_for(st, i).leapfrog_bcc2_comp(eh, oh, el, ol, vdt_for(st, i), 5)
             want.append((orc.join_comp(eh, el).astype(np.float32), orc.join_comp(oh, ol).astype(np.float32)))
         if batched:

@@ -81,7 +81,7 @@ struct gpe_handle_ {
     size_t hsize = 0;  // bytes per real element of a host field array (8 for GPE_FP32C unless host_fp32)
     bool host_fp32 = false;  // GPE_FP32C: host fields are float (gpe_set_host_precision)
     bool comp = false;                   // GPE_FP32C: compensated real-time storage
-    void *lo[2] = {nullptr, nullptr};    // GPE_FP32C: bf16x2 residual per value of fields 0 and 1
+    void *lo[2] = {nullptr, nullptr};    // GPE_FP32C: int8 x 2 residual per value of fields 0 and 1
     std::vector<InstDev> idev_host;
     InstDev *idev = nullptr;
     size_t field_elems = 0, v_elems = 0;
@@ -788,7 +788,9 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
         d.nx = in.nx;
         d.ny = in.ny;
         d.nz = in.nz;
-        d.px = int(round_up(size_t(in.nx) + 3, 4));
+        // rows start on 16 bytes: 4 values (8 for GPE_FP32C, whose 16-bit
+        // residual rows have the same pitch)
+        d.px = int(round_up(size_t(in.nx) + 3, h->comp ? 8 : 4));
         d.py = in.ny + 2;
         d.slots = h->ns;
         d.plane = (long long)d.px * d.py;
@@ -854,8 +856,8 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
     GPE_CREATE_TRY(cudaMemsetAsync(h->buf[1], 0, cbytes * h->field_elems, h->stream));
     if (h->comp)
         for (int f = 0; f < 2; f++) {
-            GPE_CREATE_TRY(cudaMalloc(&h->lo[f], sizeof(uint32_t) * h->field_elems));
-            GPE_CREATE_TRY(cudaMemsetAsync(h->lo[f], 0, sizeof(uint32_t) * h->field_elems, h->stream));
+            GPE_CREATE_TRY(cudaMalloc(&h->lo[f], sizeof(uint16_t) * h->field_elems));
+            GPE_CREATE_TRY(cudaMemsetAsync(h->lo[f], 0, sizeof(uint16_t) * h->field_elems, h->stream));
         }
     GPE_CREATE_TRY(cudaMalloc(&h->vpot, h->esize * std::max<size_t>(h->v_elems, 1)));
     GPE_CREATE_TRY(cudaMemsetAsync(h->vpot, 0, h->esize * std::max<size_t>(h->v_elems, 1), h->stream));

@@ -155,6 +155,33 @@ __device__ __forceinline__ typename Cplx<T>::type integrate(typename Cplx<T>::ty
     return r;
 }
 
+// Compensated storage (GPE_FP32C): each component of a stored FP32 value s
+// carries an int8 residual q in units of ulp(s)/256, so the value stands for
+// s + q * unit(s).  unit(s) = 2^(E - 31 - 127) for the biased exponent E of s,
+// with E raised to 32 below 2^-95 so that the unit stays a normal float.  A
+// two-sum's rounding error is at most ulp(s)/2 = 128 units: q is the error in
+// units rounded to nearest even and clipped to +-127.  Scaling by a power of
+// two is exact, so encoding and decoding round only in that one place.
+__device__ __forceinline__ float comp_unit(float s)
+{
+    const uint32_t e = max(__float_as_uint(s) & 0x7f800000u, 32u << 23);
+    return __uint_as_float(e - (31u << 23));
+}
+__device__ __forceinline__ float comp_unit_inv(float s)  // 1 / comp_unit(s), exactly
+{
+    const uint32_t e = max(__float_as_uint(s) & 0x7f800000u, 32u << 23);
+    return __uint_as_float((285u << 23) - e);
+}
+__device__ __forceinline__ uint32_t comp_encode(float r, float s)  // the low 8 bits hold q
+{
+    const int q = min(max(__float2int_rn(__fmul_rn(r, comp_unit_inv(s))), -127), 127);
+    return uint32_t(q) & 0xffu;
+}
+__device__ __forceinline__ float comp_decode(uint32_t q8, float s)
+{
+    return __fmul_rn(float(int(int8_t(uint8_t(q8)))), comp_unit(s));
+}
+
 // Harmonic trap from per-axis tables (dt-scaled): V = (Vx + Vy) + Vz.
 template <typename T>
 __device__ __forceinline__ T trap_vdt(const T *tab, const InstDev &d, int s, int x, int y, int z)

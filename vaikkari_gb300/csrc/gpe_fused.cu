@@ -41,10 +41,11 @@
 // instance's rows in fixed order and updates its ImagScalars.
 //
 // Compensated real time (MODE 2, FP32 only): every value of the next field also
-// carries a bf16 residual per component (one 32-bit word, same padded index as
-// the field).  The update adds the residual to the increment, adds that to the
-// stored value with an exact two-sum, and stores the rounded sum and the bf16 of
-// its rounding error:
+// carries an int8 residual per component in units of the stored component's
+// ulp / 256 (one 16-bit word, same padded index as the field; gpe_device.cuh).
+// The update adds the residual to the increment, adds that to the stored value
+// with an exact two-sum, and stores the rounded sum and its rounding error in
+// those units:
 //   t = lo + (hy, -hx);  s = n + t;  b = s - n;  r = (n - (s - b)) + (t - b)
 // so the time accumulation keeps about 8 more bits than FP32 storage.  The
 // residual tile travels by TMA in the same stage as the next field's tile (TMA
@@ -53,7 +54,6 @@
 // registers.
 
 #include <cuda.h>
-#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -75,7 +75,7 @@ struct FusedArgs {
     int src;                  // field the previous values come from (0 or 1)
     const void *prev;
     void *next;
-    uint32_t *next_lo;        // MODE 2: bf16x2 residuals of the next field
+    uint16_t *next_lo;        // MODE 2: int8 x 2 residuals of the next field
     const void *vpot;
     ImagScalars *imag;
     double *partials;
@@ -648,7 +648,8 @@ gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *f
 }
 
 // The residual map of one field of one instance (GPE_FP32C): 4-D over the
-// padded layout in 32-bit words (x, y, slot, z); box TX + 4 columns from a
+// padded layout in 16-bit words (x, y, slot, z; rows of px words, px a multiple
+// of 8 so that every row starts on 16 bytes); box TX + 8 columns from a
 // 16-byte-aligned column, TY rows, both slots, one plane.
 gpe_status make_residual_map(void *out_map, const InstDev &d, void *lo_arena, int tile)
 {
@@ -657,11 +658,11 @@ gpe_status make_residual_map(void *out_map, const InstDev &d, void *lo_arena, in
     int tx, ty;
     fused_tile_shape(tile, &tx, &ty);
     const cuuint64_t dims[4] = {(cuuint64_t)d.px, (cuuint64_t)d.py, 2, (cuuint64_t)d.nz + 2};
-    const cuuint64_t strides[3] = {(cuuint64_t)d.px * 4, (cuuint64_t)d.plane * 4, (cuuint64_t)d.zstride * 4};
+    const cuuint64_t strides[3] = {(cuuint64_t)d.px * 2, (cuuint64_t)d.plane * 2, (cuuint64_t)d.zstride * 2};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
-    const cuuint32_t box[4] = {(cuuint32_t)(tx + 4), (cuuint32_t)ty, 2, 1};
-    void *gaddr = (char *)lo_arena + (size_t)d.base * 4;
-    CUresult r = encode((CUtensorMap *)out_map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, gaddr, dims, strides, box, estr,
+    const cuuint32_t box[4] = {(cuuint32_t)(tx + 8), (cuuint32_t)ty, 2, 1};
+    void *gaddr = (char *)lo_arena + (size_t)d.base * 2;
+    CUresult r = encode((CUtensorMap *)out_map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, gaddr, dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
@@ -825,7 +826,7 @@ cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s)
     a.src = l.src;
     a.prev = l.prev;
     a.next = l.next;
-    a.next_lo = (uint32_t *)l.next_lo;
+    a.next_lo = (uint16_t *)l.next_lo;
     a.vpot = l.vpot;
     a.imag = l.imag;
     a.partials = l.partials;

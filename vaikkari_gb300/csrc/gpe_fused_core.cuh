@@ -14,7 +14,6 @@
 #pragma once
 
 #include <cuda.h>
-#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -129,10 +128,11 @@ struct FusedShape {
     static constexpr int HALO_BYTES = 2 * SLOT * (int)sizeof(T2);
     static constexpr int NEXT_BYTES = 2 * TX * TY * (int)sizeof(T2);
     static constexpr int NEXT_OFF = ((HALO_BYTES + 127) / 128) * 128;
-    // compensated storage: the residual tile, columns x0-2 .. x0+TX+1 (its copy
-    // starts on the 16-byte boundary of column x0-2), TY rows, both slots
-    static constexpr int LO_W = TX + 4;
-    static constexpr int LO_BYTES = COMP ? 2 * TY * LO_W * 4 : 0;
+    // compensated storage: the residual tile (16 bits per value), columns
+    // x0-2 .. x0+TX+5 (its copy starts on the 16-byte boundary of column x0-2
+    // and spans a multiple of 16 bytes), TY rows, both slots
+    static constexpr int LO_W = TX + 8;
+    static constexpr int LO_BYTES = COMP ? 2 * TY * LO_W * 2 : 0;
     static constexpr int LO_OFF = ((NEXT_OFF + NEXT_BYTES + 127) / 128) * 128;
     static constexpr int STAGE_BYTES = ((LO_OFF + LO_BYTES + 127) / 128) * 128;
     static constexpr int XE = (int)sizeof(T2) / 8;  // 8-byte TMA elements per complex
@@ -242,20 +242,17 @@ template <> struct Ops<float> {
 };
 
 // Compensated update of one value (MODE 2): returns the new stored value and
-// replaces *lo (bf16 pair, x in the low half) with the new residual.
+// replaces lo (int8 residuals of x and y in its low 16 bits, units of the
+// stored value's ulp / 256, gpe_device.cuh) with the new residual.
 __device__ __forceinline__ float2 integrate_comp(float2 n, float hx, float hy, uint32_t &lo)
 {
-    __nv_bfloat162 lb;
-    memcpy(&lb, &lo, 4);
-    const float2 t = f2_add(__bfloat1622float2(lb), make_float2(hy, -hx));
+    const float2 t = f2_add(make_float2(comp_decode(lo, n.x), comp_decode(lo >> 8, n.y)), make_float2(hy, -hx));
     const float2 s = f2_add(n, t);
     const float2 b = f2_sub(s, n);
     const float2 r = f2_add(f2_sub(n, f2_sub(s, b)), f2_sub(t, b));
-    lb = __floats2bfloat162_rn(r.x, r.y);
-    memcpy(&lo, &lb, 4);
+    lo = comp_encode(r.x, s.x) | (comp_encode(r.y, s.y) << 8);
     return s;
 }
-
 
 // Barrier of threads 0..n-1 on barrier id, returning whether any of them passed v.
 __device__ __forceinline__ bool bar_any(int id, int n, bool v)
@@ -365,7 +362,7 @@ __device__ __forceinline__ void drain_ring(int issued, uint32_t full)
 // the whole warp.
 template <typename T, int TX, int TY, int MODE, int POT, int STAGES, bool WATCH>
 __device__ __forceinline__ bool consume_item(const WorkItem &w, const InstDev &d, int kb, const unsigned char *gbase,
-                                             uint32_t full, uint32_t empty, void *next, uint32_t *next_lo,
+                                             uint32_t full, uint32_t empty, void *next, uint16_t *next_lo,
                                              const void *vpot_, const T *zt, int zt_stride, int zt_base, T sig,
                                              Acc<T> (&acc)[4], int tid, int lane, int *err, volatile int *abort_flag)
 {
@@ -382,7 +379,7 @@ __device__ __forceinline__ bool consume_item(const WorkItem &w, const InstDev &d
     const T Lw[2] = {T(d.Lc[0]), T(d.Lc[1])};
     const T L0 = T(d.L0), gdt = T(d.gdt);
     T2 *__restrict__ nxt = (T2 *)next;
-    uint32_t *__restrict__ nlo = next_lo;
+    uint16_t *__restrict__ nlo = next_lo;
     uint32_t lo0 = 0u, lo1 = 0u;  // MODE 2: residuals of the output plane
     const T *__restrict__ vpot = (const T *)vpot_;
     T vxy0 = T(0), vxy1 = T(0);
@@ -426,7 +423,7 @@ __device__ __forceinline__ bool consume_item(const WorkItem &w, const InstDev &d
             n0 = Np[ty * TX + tx];
             n1 = Np[TX * TY + ty * TX + tx];
             if (MODE == 2) {
-                const uint32_t *Lp = (const uint32_t *)(sb + S::LO_OFF);
+                const uint16_t *Lp = (const uint16_t *)(sb + S::LO_OFF);
                 lo0 = Lp[ty * S::LO_W + tx + 2];
                 lo1 = Lp[(TY + ty) * S::LO_W + tx + 2];
             }
@@ -484,8 +481,8 @@ __device__ __forceinline__ bool consume_item(const WorkItem &w, const InstDev &d
             nxt[i0] = o0;
             nxt[i0 + plane] = o1;
             if (MODE == 2) {
-                nlo[i0] = lo0;
-                nlo[i0 + plane] = lo1;
+                nlo[i0] = uint16_t(lo0);
+                nlo[i0 + plane] = uint16_t(lo1);
             }
         }
         cm = cc;

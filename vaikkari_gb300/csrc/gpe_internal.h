@@ -89,7 +89,7 @@ cudaError_t launch_potential_base(int precision, const InstDev *inst, int ii, in
 struct FusedLaunch {
     int precision, mode, potential, tile;
     int comp;             // real time, FP32: compensated storage (next_lo holds the residuals)
-    void *next_lo;        // bf16x2 residual per value of the next field, same padded index
+    void *next_lo;        // int8 x 2 residual per value of the next field, same padded index
     const void *lo_maps;  // CUtensorMap[num_instances][2 fields] of the residual arrays
     const void *maps;     // CUtensorMap[num_instances][2 fields][2 boxes] in device memory
     int zcmax;            // longest z-range of a work item
@@ -195,7 +195,7 @@ cudaError_t launch_pack(int precision, const InstDev *inst, int inst_index, int 
 cudaError_t launch_unpack(int precision, const InstDev *inst, int inst_index, int nx, int ny, int nz,
                           int slots, const void *field, void *host_order, const ImagScalars *imag,
                           cudaStream_t s);
-// GPE_FP32C: double host order <-> FP32 field plus bf16x2 residuals.
+// GPE_FP32C: double (or float) host order <-> FP32 field plus int8 x 2 residuals.
 cudaError_t launch_pack_split(const InstDev *inst, int ii, int nx, int ny, int nz, int slots, const void *host_order,
                               void *field, void *lo, bool host_fp32, cudaStream_t s);
 cudaError_t launch_unpack_join(const InstDev *inst, int ii, int nx, int ny, int nz, int slots, const void *field,

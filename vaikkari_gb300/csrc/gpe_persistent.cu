@@ -57,7 +57,7 @@ struct PersistArgs {
     const CUtensorMap *maps;     // [instance][field][halo box, interior box]
     const CUtensorMap *lo_maps;  // MODE 2: [instance][field] residual box
     void *field[2];              // even, odd
-    uint32_t *lo[2];             // MODE 2: their bf16x2 residuals
+    uint16_t *lo[2];             // MODE 2: their int8 x 2 residuals
     const void *vpot;
     unsigned long long *ticket;  // ticket counter, zero at launch
     const int *nbr_begin;        // [num_items + 1]: CSR rows of nbr
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(persistent_threads<T, TX, TY>(), MinBlocks<T, 
             }
             const int h = int(t / N), it = int(t % N);
             void *next = (h & 1) ? a.field[0] : a.field[1];  // selects, so the argument arrays stay in registers
-            uint32_t *next_lo = (h & 1) ? a.lo[0] : a.lo[1];
+            uint16_t *next_lo = (h & 1) ? a.lo[0] : a.lo[1];
             const WorkItem w = a.items[it];
             const InstDev &d = a.inst[w.inst];
             const T *tz = (const T *)a.vpot + d.vbase + 2ll * d.nx + 2ll * d.ny;  // trap: z-terms [slot][z]
@@ -353,8 +353,8 @@ cudaError_t launch_persistent(const PersistLaunch &l, cudaStream_t s, int *grid)
     a.lo_maps = (const CUtensorMap *)l.lo_maps;
     a.field[0] = l.field[0];
     a.field[1] = l.field[1];
-    a.lo[0] = (uint32_t *)l.lo[0];
-    a.lo[1] = (uint32_t *)l.lo[1];
+    a.lo[0] = (uint16_t *)l.lo[0];
+    a.lo[1] = (uint16_t *)l.lo[1];
     a.vpot = l.vpot;
     a.ticket = l.ticket;
     a.nbr_begin = l.nbr_begin;

@@ -8,7 +8,6 @@
 // reference's lanes are 192 bytes apart), and the neighbour table is read from
 // constant memory with a warp-uniform index.
 
-#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -857,12 +856,13 @@ __global__ void scale_field_kernel(const InstDev *__restrict__ insts, int ii, T 
     }
 }
 
-// GPE_FP32C transfers.  Upload: a double x becomes hi = float(x) and the
-// residual lo = bf16(float(x - hi)) (x - hi is exact in double); download:
-// double(hi) + double(lo).  lo holds both components in one word, re in the low half.
+// GPE_FP32C transfers.  Upload: a double x becomes hi = float(x) and the int8
+// residual of float(x - hi) (x - hi is exact in double) in units of ulp(hi)/256;
+// download: double(hi) + double(residual).  lo holds both components in one
+// 16-bit word, re in the low byte.
 template <typename H>  // host element: double, or float (the residual starts at zero)
 __global__ void pack_split_kernel(const InstDev *__restrict__ insts, int ii, const H *__restrict__ src,
-                                  float *__restrict__ hi, uint32_t *__restrict__ lo)
+                                  float *__restrict__ hi, uint16_t *__restrict__ lo)
 {
     const InstDev &d = insts[ii];
     const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
@@ -880,16 +880,16 @@ __global__ void pack_split_kernel(const InstDev *__restrict__ insts, int ii, con
         const float ha = __double2float_rn(a), hb = __double2float_rn(b);
         hi[2 * o] = ha;
         hi[2 * o + 1] = hb;
-        const __nv_bfloat162 l = __floats2bfloat162_rn(__double2float_rn(a - double(ha)), __double2float_rn(b - double(hb)));
-        uint32_t w;
-        memcpy(&w, &l, 4);
-        lo[o] = w;
+        // residual = the part of the value below FP32, in units of ulp(hi) / 256
+        const uint32_t qa = comp_encode(__double2float_rn(a - double(ha)), ha);
+        const uint32_t qb = comp_encode(__double2float_rn(b - double(hb)), hb);
+        lo[o] = uint16_t(qa | (qb << 8));
     }
 }
 
 template <typename H>  // host element: double, or float (value + residual rounded once)
 __global__ void unpack_join_kernel(const InstDev *__restrict__ insts, int ii, const float *__restrict__ hi,
-                                   const uint32_t *__restrict__ lo, H *__restrict__ dst)
+                                   const uint16_t *__restrict__ lo, H *__restrict__ dst)
 {
     const InstDev &d = insts[ii];
     const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
@@ -903,12 +903,11 @@ __global__ void unpack_join_kernel(const InstDev *__restrict__ insts, int ii, co
         const int y = int(r % d.ny);
         const int z = int(r / d.ny);
         const long long o = field_index(d, s, x, y, z);
-        __nv_bfloat162 l;
         const uint32_t w = lo[o];
-        memcpy(&l, &w, 4);
-        const float2 lf = __bfloat1622float2(l);
-        dst[2 * v] = H(double(hi[2 * o]) + double(lf.x));
-        dst[2 * v + 1] = H(double(hi[2 * o + 1]) + double(lf.y));
+        const float ha = hi[2 * o], hb = hi[2 * o + 1];
+        const float2 lf = make_float2(comp_decode(w, ha), comp_decode(w >> 8, hb));
+        dst[2 * v] = H(double(ha) + double(lf.x));
+        dst[2 * v + 1] = H(double(hb) + double(lf.y));
     }
 }
 
@@ -949,10 +948,10 @@ cudaError_t launch_pack_split(const InstDev *inst, int ii, int nx, int ny, int n
 {
     const int g = grid_for((long long)nx * ny * nz * slots);
     if (host_fp32)
-        pack_split_kernel<float><<<g, 256, 0, s>>>(inst, ii, (const float *)host_order, (float *)field, (uint32_t *)lo);
+        pack_split_kernel<float><<<g, 256, 0, s>>>(inst, ii, (const float *)host_order, (float *)field, (uint16_t *)lo);
     else
         pack_split_kernel<double><<<g, 256, 0, s>>>(inst, ii, (const double *)host_order, (float *)field,
-                                                    (uint32_t *)lo);
+                                                    (uint16_t *)lo);
     return cudaGetLastError();
 }
 
@@ -961,10 +960,10 @@ cudaError_t launch_unpack_join(const InstDev *inst, int ii, int nx, int ny, int 
 {
     const int g = grid_for((long long)nx * ny * nz * slots);
     if (host_fp32)
-        unpack_join_kernel<float><<<g, 256, 0, s>>>(inst, ii, (const float *)field, (const uint32_t *)lo,
+        unpack_join_kernel<float><<<g, 256, 0, s>>>(inst, ii, (const float *)field, (const uint16_t *)lo,
                                                     (float *)host_order);
     else
-        unpack_join_kernel<double><<<g, 256, 0, s>>>(inst, ii, (const float *)field, (const uint32_t *)lo,
+        unpack_join_kernel<double><<<g, 256, 0, s>>>(inst, ii, (const float *)field, (const uint16_t *)lo,
                                                      (double *)host_order);
     return cudaGetLastError();
 }

@@ -30,8 +30,8 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libvaikkari_gpe.so")
 class Precision(enum.IntEnum):
     FP64 = 0
     FP32 = 1
-    # FP32 fields with a bf16 residual per component carried across real-time
-    # steps (BCC2, fused kernel); fields are exchanged as float64.
+    # FP32 fields with an int8 residual per component (units of ulp/256) carried
+    # across real-time steps (BCC2, fused kernel); fields are exchanged as float64.
     FP32C = 2
 
 
