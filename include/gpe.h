@@ -283,6 +283,16 @@ int32_t gpe_variant_kind(int32_t variant);
 /* Kernel launches the handle has issued (for accounting). */
 int64_t gpe_launch_count(gpe_handle h);
 
+/* Host buffers the handle's transfers (gpe_upload, gpe_download and their
+ * batched forms) have converted in place since creation: buffers in page-locked
+ * memory mapped into the handle's device's address space (cudaHostAlloc,
+ * cudaHostRegister on that device), aligned to their element pair and wholly
+ * inside one such allocation.  Their conversion kernels read or write the host
+ * buffer over the host link directly, with no device staging or copy-engine
+ * pass; every other buffer is staged.  The reference copies whole blocks with
+ * cudaMemcpy3D (GPUGrossPitaevskii_BCC.cu:370-391,415,484). */
+int64_t gpe_mapped_transfers(gpe_handle h);
+
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their own
  * work or record CUDA events against the library's launches. */
 void *gpe_stream(gpe_handle h);

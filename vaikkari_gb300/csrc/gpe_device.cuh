@@ -62,10 +62,49 @@ struct ImagScalars {
     long long steps;      // steps taken
 };
 
+// Columns of zero padding before x = 0 in every row of the padded layout.  The
+// tile boxes start at column x0 - 2 + kPadX (previous field, two-column halo) and
+// x0 + kPadX (interior), both 16-byte aligned for any even kPadX.
+constexpr int kPadX = 2;
+
 __host__ __device__ inline long long field_index(const InstDev &d, int s, int x, int y, int z)
 {
-    return d.base + (long long)(z + 1) * d.zstride + (long long)s * d.plane + (long long)(y + 1) * d.px + (x + 2);
+    return d.base + (long long)(z + 1) * d.zstride + (long long)s * d.plane + (long long)(y + 1) * d.px + (x + kPadX);
 }
+
+// GPE_FP32C: the residual of the value at field index i is word i - kLoShift of
+// the residual array, which puts column x of a row at word x of the row, so a
+// tile's residual box starts on the tile's first column (16-byte aligned: rows
+// of px = 8k words from an instance base that is a multiple of 64) and is
+// exactly the tile wide.  Only interior values (index >= 2 within their row)
+// have residuals.
+constexpr int kLoShift = kPadX;
+
+#ifdef __CUDACC__
+// The digits of a value number v = ((d3 * r2 + d2) * r1 + d1) * r0 + d0, d0
+// fastest: in 32-bit division whenever v fits in 31 bits (64-bit division is a
+// long instruction sequence on the GPU, 32-bit division a short one).
+__device__ __forceinline__ void digits(long long v, int r0, int r1, int r2, int &d0, int &d1, int &d2, int &d3)
+{
+    if (v <= 0x7fffffffll) {
+        unsigned u = unsigned(v);
+        d0 = int(u % unsigned(r0));
+        u /= unsigned(r0);
+        d1 = int(u % unsigned(r1));
+        u /= unsigned(r1);
+        d2 = int(u % unsigned(r2));
+        d3 = int(u / unsigned(r2));
+        return;
+    }
+    long long r = v;
+    d0 = int(r % r0);
+    r /= r0;
+    d1 = int(r % r1);
+    r /= r1;
+    d2 = int(r % r2);
+    d3 = int(r / r2);
+}
+#endif
 
 #ifdef __CUDACC__
 // Rounded arithmetic without contraction, so that the CPU oracle (C fma(),
@@ -78,6 +117,49 @@ __device__ __forceinline__ double d_add(double a, double b) { return __dadd_rn(a
 __device__ __forceinline__ double d_sub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double d_mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double d_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// Packed FP32 pairs (add / mul / fma .rn.f32x2, sm_100 and later): each lane is
+// the IEEE operation of that lane, so a complex sum, or a complex times a real
+// factor, rounds exactly as the two scalar operations do, in one instruction.
+__device__ __forceinline__ float2 f2_add(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "add.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
+__device__ __forceinline__ float2 f2_mul(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "mul.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "sub.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
+__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, c, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "mov.b64 c, {%6, %7};\n\tfma.rn.f32x2 d, a, b, c;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
+}
 
 template <typename T> struct Cplx;
 template <> struct Cplx<float> { using type = float2; };

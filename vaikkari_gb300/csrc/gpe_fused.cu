@@ -380,13 +380,13 @@ __global__ void __launch_bounds__(TwoStepShape<T, TX, TY>::NTHREADS, MinBlocks<T
                 }
                 const bool with_o = k >= 2;
                 mbar_arrive_expect_tx(full + 8 * st, S::E_BYTES + (with_o ? S::O_BYTES : 0));
-                // padded coordinates: x0-2 -> x0; E rows from y0-2 -> y0-1, O rows from
-                // y0-1 -> y0; plane q = z0-2+k -> z0-1+k
-                tma_load_4d(base + st * S::STAGE_BYTES, emap, w.x0 * S::XE, w.y0 - 1, 0, w.z0 - 1 + k,
+                // padded coordinates: x0-2 -> x0-2+kPadX; E rows from y0-2 -> y0-1, O
+                // rows from y0-1 -> y0; plane q = z0-2+k -> z0-1+k
+                tma_load_4d(base + st * S::STAGE_BYTES, emap, (w.x0 - 2 + kPadX) * S::XE, w.y0 - 1, 0, w.z0 - 1 + k,
                             full + 8 * st);
                 if (with_o)
-                    tma_load_4d(base + st * S::STAGE_BYTES + S::O_OFF, omap, w.x0 * S::XE, w.y0, 0, w.z0 - 2 + k,
-                                full + 8 * st);
+                    tma_load_4d(base + st * S::STAGE_BYTES + S::O_OFF, omap, (w.x0 - 2 + kPadX) * S::XE, w.y0, 0,
+                                w.z0 - 2 + k, full + 8 * st);
                 issued = k + 1;
             }
             if (abort_flag) {
@@ -649,8 +649,10 @@ gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *f
 
 // The residual map of one field of one instance (GPE_FP32C): 4-D over the
 // padded layout in 16-bit words (x, y, slot, z; rows of px words, px a multiple
-// of 8 so that every row starts on 16 bytes); box TX + 8 columns from a
-// 16-byte-aligned column, TY rows, both slots, one plane.
+// of 8 so that every row starts on 16 bytes).  The residual of padded column c
+// sits at column c - kLoShift, so the map's column X is the instance's column
+// x = X and a tile's box is TX columns from x0 (16-byte aligned), TY rows, both
+// slots, one plane.
 gpe_status make_residual_map(void *out_map, const InstDev &d, void *lo_arena, int tile)
 {
     TensorMapEncode encode = tensor_map_encoder();
@@ -660,7 +662,7 @@ gpe_status make_residual_map(void *out_map, const InstDev &d, void *lo_arena, in
     const cuuint64_t dims[4] = {(cuuint64_t)d.px, (cuuint64_t)d.py, 2, (cuuint64_t)d.nz + 2};
     const cuuint64_t strides[3] = {(cuuint64_t)d.px * 2, (cuuint64_t)d.plane * 2, (cuuint64_t)d.zstride * 2};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
-    const cuuint32_t box[4] = {(cuuint32_t)(tx + 8), (cuuint32_t)ty, 2, 1};
+    const cuuint32_t box[4] = {(cuuint32_t)tx, (cuuint32_t)ty, 2, 1};
     void *gaddr = (char *)lo_arena + (size_t)d.base * 2;
     CUresult r = encode((CUtensorMap *)out_map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, gaddr, dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,

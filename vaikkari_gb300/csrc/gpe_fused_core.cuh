@@ -129,9 +129,9 @@ struct FusedShape {
     static constexpr int NEXT_BYTES = 2 * TX * TY * (int)sizeof(T2);
     static constexpr int NEXT_OFF = ((HALO_BYTES + 127) / 128) * 128;
     // compensated storage: the residual tile (16 bits per value), columns
-    // x0-2 .. x0+TX+5 (its copy starts on the 16-byte boundary of column x0-2
-    // and spans a multiple of 16 bytes), TY rows, both slots
-    static constexpr int LO_W = TX + 8;
+    // x0 .. x0+TX-1, TY rows, both slots (residuals sit kLoShift places before
+    // their values, so the tile's box starts on its first column)
+    static constexpr int LO_W = TX;
     static constexpr int LO_BYTES = COMP ? 2 * TY * LO_W * 2 : 0;
     static constexpr int LO_OFF = ((NEXT_OFF + NEXT_BYTES + 127) / 128) * 128;
     static constexpr int STAGE_BYTES = ((LO_OFF + LO_BYTES + 127) / 128) * 128;
@@ -170,49 +170,6 @@ static cudaError_t launch_pdl(Kern kern, int grid, int threads, int bytes, cudaS
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, kern, a);
-}
-
-// Packed FP32 pairs (add / mul / fma .rn.f32x2, sm_100 and later): each lane is
-// the IEEE operation of that lane, so a complex sum, or a complex times a real
-// factor, rounds exactly as the two scalar operations do, in one instruction.
-__device__ __forceinline__ float2 f2_add(float2 a, float2 b)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
-        "add.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-
-__device__ __forceinline__ float2 f2_mul(float2 a, float2 b)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
-        "mul.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-
-__device__ __forceinline__ float2 f2_sub(float2 a, float2 b)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
-        "sub.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-
-__device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 a, b, c, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
-        "mov.b64 c, {%6, %7};\n\tfma.rn.f32x2 d, a, b, c;\n\tmov.b64 {%0, %1}, d;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-    return r;
 }
 
 // Complex sums and dt*H psi (gpe_device.cuh's hpsi, two classes) with the same
@@ -326,12 +283,12 @@ __device__ __forceinline__ int produce_item(const WorkItem &w, int kb, int src, 
         if (k == 0 && tag) tag[st] = tag_value;
         const bool with_next = REAL && (k >= 2);
         mbar_arrive_expect_tx(full + 8 * st, S::HALO_BYTES + (with_next ? S::NEXT_BYTES + S::LO_BYTES : 0));
-        // padded coordinates: x0-2 -> x0, y0-1 -> y0, plane q -> q+1
-        tma_load_4d(base + st * S::STAGE_BYTES, halo, w.x0 * S::XE, w.y0, 0, w.z0 + k, full + 8 * st);
+        // padded coordinates: x0-2 -> x0-2+kPadX, y0-1 -> y0, plane q -> q+1
+        tma_load_4d(base + st * S::STAGE_BYTES, halo, (w.x0 - 2 + kPadX) * S::XE, w.y0, 0, w.z0 + k, full + 8 * st);
         if (with_next)  // next field, interior tile of plane q-1 = z0+k-2
-            tma_load_4d(base + st * S::STAGE_BYTES + S::NEXT_OFF, inner, (w.x0 + 2) * S::XE, w.y0 + 1, 0,
+            tma_load_4d(base + st * S::STAGE_BYTES + S::NEXT_OFF, inner, (w.x0 + kPadX) * S::XE, w.y0 + 1, 0,
                         w.z0 + k - 1, full + 8 * st);
-        if (MODE == 2 && with_next)  // its residuals, from padded column x0 (16-byte aligned)
+        if (MODE == 2 && with_next)  // its residuals (columns x0.. in the residual rows)
             tma_load_4d(base + st * S::STAGE_BYTES + S::LO_OFF, lo_maps + 2 * w.inst + (1 - src), w.x0, w.y0 + 1, 0,
                         w.z0 + k - 1, full + 8 * st);
         issued = n + 1;
@@ -424,8 +381,8 @@ __device__ __forceinline__ bool consume_item(const WorkItem &w, const InstDev &d
             n1 = Np[TX * TY + ty * TX + tx];
             if (MODE == 2) {
                 const uint16_t *Lp = (const uint16_t *)(sb + S::LO_OFF);
-                lo0 = Lp[ty * S::LO_W + tx + 2];
-                lo1 = Lp[(TY + ty) * S::LO_W + tx + 2];
+                lo0 = Lp[ty * S::LO_W + tx];
+                lo1 = Lp[(TY + ty) * S::LO_W + tx];
             }
         }
         __syncwarp();
@@ -481,8 +438,8 @@ __device__ __forceinline__ bool consume_item(const WorkItem &w, const InstDev &d
             nxt[i0] = o0;
             nxt[i0 + plane] = o1;
             if (MODE == 2) {
-                nlo[i0] = uint16_t(lo0);
-                nlo[i0 + plane] = uint16_t(lo1);
+                nlo[i0 - kLoShift] = uint16_t(lo0);
+                nlo[i0 + plane - kLoShift] = uint16_t(lo1);
             }
         }
         cm = cc;

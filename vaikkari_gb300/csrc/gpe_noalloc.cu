@@ -165,13 +165,8 @@ __global__ void __launch_bounds__(kThreads) noalloc_observables_kernel(const Noa
     for (int j = 0; j < kPerThread; j++) {
         const long long v = first + j * kThreads + threadIdx.x;
         if (v >= total) break;
-        long long r = v;
-        const int s = int(r % ns);
-        r /= ns;
-        const int x = int(r % gr.nx);
-        r /= gr.nx;
-        const int y = int(r % gr.ny);
-        const int z = int(r / gr.ny);
+        int s, x, y, z;
+        digits(v, ns, gr.nx, gr.ny, s, x, y, z);
         double lx = 0.0, ly = 0.0;
         for (int k = 0; k < nb; k++) {
             const int e = st.entry[s * nb + k];

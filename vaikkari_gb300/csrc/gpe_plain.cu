@@ -320,13 +320,8 @@ __global__ void potential_base_kernel(const InstDev *__restrict__ insts, int ii,
     const T L0 = T(d.L0);
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
          v += (long long)gridDim.x * blockDim.x) {
-        long long r = v;
-        const int x = int(r % d.nx);
-        r /= d.nx;
-        const int y = int(r % d.ny);
-        r /= d.ny;
-        const int s = int(r % d.slots);
-        const int z = int(r / d.slots);
+        int x, y, s, z;
+        digits(v, d.nx, d.ny, d.slots, x, y, s, z);
         const long long o = field_index(d, s, x, y, z) - d.base + d.vbase;
         vbase[o] = d_add(L0, vpot[o]);  // the add hpsi would do every half-step
     }
@@ -476,11 +471,48 @@ __device__ __forceinline__ FPair fp_of(double v)
 }
 __device__ __forceinline__ double fp_value(FPair x) { return __dadd_rn(double(x.hi), double(x.lo)); }
 
+// The same pairs for the two components of a complex value at once: each
+// packed f32x2 operation is the two scalar operations of its lanes, so a pair of
+// float2 carries (re, im) through exactly the arithmetic of two FPairs.
+struct FPair2 {
+    float2 hi, lo;
+};
+__device__ __forceinline__ float2 f2_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ FPair2 fp2_two_sum(float2 a, float2 b)
+{
+    const float2 s = f2_add(a, b);
+    const float2 bb = f2_sub(s, a);
+    return {s, f2_add(f2_sub(a, f2_sub(s, bb)), f2_sub(b, bb))};
+}
+__device__ __forceinline__ FPair2 fp2_fast_two_sum(float2 a, float2 b)
+{
+    const float2 s = f2_add(a, b);
+    return {s, f2_sub(b, f2_sub(s, a))};
+}
+__device__ __forceinline__ FPair2 fp2_two_prod(float2 a, float2 b)
+{
+    const float2 p = f2_mul(a, b);
+    return {p, f2_fma(a, b, f2_neg(p))};
+}
+__device__ __forceinline__ FPair2 fp2_add(FPair2 x, FPair2 y)
+{
+    FPair2 s = fp2_two_sum(x.hi, y.hi);
+    const FPair2 t = fp2_two_sum(x.lo, y.lo);
+    s = fp2_fast_two_sum(s.hi, f2_add(s.lo, t.hi));
+    return fp2_fast_two_sum(s.hi, f2_add(s.lo, t.lo));
+}
+__device__ __forceinline__ FPair2 fp2_mul(FPair2 x, FPair2 y)
+{
+    const FPair2 p = fp2_two_prod(x.hi, y.hi);
+    return fp2_fast_two_sum(p.hi, f2_fma(x.hi, y.lo, f2_fma(x.lo, y.hi, p.lo)));
+}
+
 // The observables of FP32 values, all in float-pair arithmetic: per class c
 // the neighbour sum S_c as an error-free pair, the bracket S_c - n_c psi (the
 // Laplacian's cancellation, exact up to the pair's rounding), Lap psi =
 // sum_c w_c (S_c - n_c psi), and the four terms, each added into a float-pair
-// accumulator.  Agrees with FP64 evaluation to about 1e-13 relative.
+// accumulator.  Agrees with FP64 evaluation to about 1e-13 relative.  The
+// per-neighbour and per-class work runs on both components at once (FPair2).
 template <int LAT, int POT>
 __device__ __forceinline__ void observables_terms_f32(const InstDev &d, const float2 *__restrict__ f,
                                                       const float *__restrict__ vpot, int s, int x, int y, int z,
@@ -489,29 +521,27 @@ __device__ __forceinline__ void observables_terms_f32(const InstDev &d, const fl
 {
     using L = Lat<LAT>;
     const float2 pt = f[self];
-    float hx[2] = {0.f, 0.f}, lx_[2] = {0.f, 0.f}, hy[2] = {0.f, 0.f}, ly_[2] = {0.f, 0.f};
+    const float2 zero = make_float2(0.f, 0.f);
+    float2 h[2] = {zero, zero}, l[2] = {zero, zero};
 #pragma unroll
     for (int k = 0; k < L::NB; k++) {
         const int e = L::entry(s * L::NB + k);
         const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
-        const float2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
+        const float2 q = f[self + (long long)dz * d.zstride + (long long)(sl - s) * d.plane + dy * d.px + dx];
         const int c = (k < L::N0) ? 0 : 1;
-        const FPair tx = fp_two_sum(hx[c], q.x), ty = fp_two_sum(hy[c], q.y);
-        hx[c] = tx.hi;
-        lx_[c] = __fadd_rn(lx_[c], tx.lo);
-        hy[c] = ty.hi;
-        ly_[c] = __fadd_rn(ly_[c], ty.lo);
+        const FPair2 t = fp2_two_sum(h[c], q);
+        h[c] = t.hi;
+        l[c] = f2_add(l[c], t.lo);
     }
-    FPair lapx = {0.f, 0.f}, lapy = {0.f, 0.f};
+    FPair2 lap = {zero, zero};
 #pragma unroll
     for (int c = 0; c < L::NC; c++) {
         const float n = float(c == 0 ? L::N0 : L::NB - L::N0);
-        const FPair npx = fp_two_prod(n, pt.x), npy = fp_two_prod(n, pt.y);
-        const FPair bx = fp_add(fp_two_sum(hx[c], lx_[c]), {-npx.hi, -npx.lo});
-        const FPair by = fp_add(fp_two_sum(hy[c], ly_[c]), {-npy.hi, -npy.lo});
-        lapx = fp_add(lapx, fp_mul(w[c], bx));
-        lapy = fp_add(lapy, fp_mul(w[c], by));
+        const FPair2 np = fp2_two_prod(make_float2(n, n), pt);
+        const FPair2 b = fp2_add(fp2_two_sum(h[c], l[c]), {f2_neg(np.hi), f2_neg(np.lo)});
+        lap = fp2_add(lap, fp2_mul({make_float2(w[c].hi, w[c].hi), make_float2(w[c].lo, w[c].lo)}, b));
     }
+    const FPair lapx = {lap.hi.x, lap.lo.x}, lapy = {lap.hi.y, lap.lo.y};
     float vdt;
     if (POT == GPE_POTENTIAL_ARRAY) vdt = vpot[self - d.base + d.vbase];
     else vdt = trap_vdt<float>(vpot, d, s, x, y, z);
@@ -542,13 +572,8 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
             const FPair rdt2 = fp_of(rdt), half_g = fp_of(0.5 * d.g);
             FPair acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
             for (long long v = first; v < total; v += stride) {
-                long long r = v;
-                const int x = int(r % d.nx);
-                r /= d.nx;
-                const int y = int(r % d.ny);
-                r /= d.ny;
-                const int s = int(r % L::NS);
-                const int z = int(r / L::NS);
+                int x, y, s, z;
+                digits(v, d.nx, d.ny, L::NS, x, y, s, z);
                 observables_terms_f32<LAT, POT>(d, (const float2 *)f, (const float *)vpot, s, x, y, z,
                                                 field_index(d, s, x, y, z), w, rdt2, half_g, acc);
             }
@@ -558,13 +583,8 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
         }
     }
     for (long long v = first; v < total; v += stride) {
-        long long r = v;
-        const int x = int(r % d.nx);
-        r /= d.nx;
-        const int y = int(r % d.ny);
-        r /= d.ny;
-        const int s = int(r % L::NS);
-        const int z = int(r / L::NS);
+        int x, y, s, z;
+        digits(v, d.nx, d.ny, L::NS, x, y, s, z);
         const long long self = field_index(d, s, x, y, z);
         const T2 pt = f[self];
         const double px = double(pt.x), py = double(pt.y);
@@ -789,17 +809,11 @@ __global__ void pack_kernel(const InstDev *__restrict__ insts, int ii, const T *
     const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
          v += (long long)gridDim.x * blockDim.x) {
-        long long r = v;
-        const int s = int(r % d.slots);
-        r /= d.slots;
-        const int x = int(r % d.nx);
-        r /= d.nx;
-        const int y = int(r % d.ny);
-        const int z = int(r / d.ny);
+        int s, x, y, z;
+        digits(v, d.slots, d.nx, d.ny, s, x, y, z);
         if (CPLX) {
             const long long o = field_index(d, s, x, y, z);
-            dst[2 * o] = src[2 * v];
-            dst[2 * o + 1] = src[2 * v + 1];
+            ((typename Cplx<T>::type *)dst)[o] = ((const typename Cplx<T>::type *)src)[v];
         } else {
             const long long o = field_index(d, s, x, y, z) - d.base + d.vbase;
             dst[o] = T(double(src[v]) * scale);
@@ -816,21 +830,15 @@ __global__ void unpack_kernel(const InstDev *__restrict__ insts, int ii, const T
     const T sig = imag ? T(imag[ii].sigma) : T(1);
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
          v += (long long)gridDim.x * blockDim.x) {
-        long long r = v;
-        const int s = int(r % d.slots);
-        r /= d.slots;
-        const int x = int(r % d.nx);
-        r /= d.nx;
-        const int y = int(r % d.ny);
-        const int z = int(r / d.ny);
+        int s, x, y, z;
+        digits(v, d.slots, d.nx, d.ny, s, x, y, z);
         const long long o = field_index(d, s, x, y, z);
+        typename Cplx<T>::type q = ((const typename Cplx<T>::type *)src)[o];
         if (imag) {
-            dst[2 * v] = d_mul(sig, src[2 * o]);
-            dst[2 * v + 1] = d_mul(sig, src[2 * o + 1]);
-        } else {
-            dst[2 * v] = src[2 * o];
-            dst[2 * v + 1] = src[2 * o + 1];
+            q.x = d_mul(sig, q.x);
+            q.y = d_mul(sig, q.y);
         }
+        ((typename Cplx<T>::type *)dst)[v] = q;
     }
 }
 
@@ -843,13 +851,8 @@ __global__ void scale_field_kernel(const InstDev *__restrict__ insts, int ii, T 
     const T sig = T(imag[ii].sigma);
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
          v += (long long)gridDim.x * blockDim.x) {
-        long long r = v;
-        const int x = int(r % d.nx);
-        r /= d.nx;
-        const int y = int(r % d.ny);
-        r /= d.ny;
-        const int s = int(r % d.slots);
-        const int z = int(r / d.slots);
+        int x, y, s, z;
+        digits(v, d.nx, d.ny, d.slots, x, y, s, z);
         const long long o = field_index(d, s, x, y, z);
         f[2 * o] = d_mul(sig, f[2 * o]);
         f[2 * o + 1] = d_mul(sig, f[2 * o + 1]);
@@ -868,22 +871,17 @@ __global__ void pack_split_kernel(const InstDev *__restrict__ insts, int ii, con
     const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
          v += (long long)gridDim.x * blockDim.x) {
-        long long r = v;
-        const int s = int(r % d.slots);
-        r /= d.slots;
-        const int x = int(r % d.nx);
-        r /= d.nx;
-        const int y = int(r % d.ny);
-        const int z = int(r / d.ny);
+        int s, x, y, z;
+        digits(v, d.slots, d.nx, d.ny, s, x, y, z);
         const long long o = field_index(d, s, x, y, z);
-        const double a = double(src[2 * v]), b = double(src[2 * v + 1]);
+        const typename Cplx<H>::type hv = ((const typename Cplx<H>::type *)src)[v];
+        const double a = double(hv.x), b = double(hv.y);
         const float ha = __double2float_rn(a), hb = __double2float_rn(b);
-        hi[2 * o] = ha;
-        hi[2 * o + 1] = hb;
+        ((float2 *)hi)[o] = make_float2(ha, hb);
         // residual = the part of the value below FP32, in units of ulp(hi) / 256
         const uint32_t qa = comp_encode(__double2float_rn(a - double(ha)), ha);
         const uint32_t qb = comp_encode(__double2float_rn(b - double(hb)), hb);
-        lo[o] = uint16_t(qa | (qb << 8));
+        lo[o - kLoShift] = uint16_t(qa | (qb << 8));
     }
 }
 
@@ -895,19 +893,17 @@ __global__ void unpack_join_kernel(const InstDev *__restrict__ insts, int ii, co
     const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
     for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < total;
          v += (long long)gridDim.x * blockDim.x) {
-        long long r = v;
-        const int s = int(r % d.slots);
-        r /= d.slots;
-        const int x = int(r % d.nx);
-        r /= d.nx;
-        const int y = int(r % d.ny);
-        const int z = int(r / d.ny);
+        int s, x, y, z;
+        digits(v, d.slots, d.nx, d.ny, s, x, y, z);
         const long long o = field_index(d, s, x, y, z);
-        const uint32_t w = lo[o];
-        const float ha = hi[2 * o], hb = hi[2 * o + 1];
+        const uint32_t w = lo[o - kLoShift];
+        const float2 hv = ((const float2 *)hi)[o];
+        const float ha = hv.x, hb = hv.y;
         const float2 lf = make_float2(comp_decode(w, ha), comp_decode(w >> 8, hb));
-        dst[2 * v] = H(double(ha) + double(lf.x));
-        dst[2 * v + 1] = H(double(hb) + double(lf.y));
+        typename Cplx<H>::type out;
+        out.x = H(double(ha) + double(lf.x));
+        out.y = H(double(hb) + double(lf.y));
+        ((typename Cplx<H>::type *)dst)[v] = out;
     }
 }
 

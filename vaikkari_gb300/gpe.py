@@ -202,6 +202,8 @@ def load_library(path: str = LIB_PATH):
                                        C.POINTER(C.c_int32), C.POINTER(C.c_double)]
     lib.gpe_launch_count.restype = C.c_int64
     lib.gpe_launch_count.argtypes = [C.c_void_p]
+    lib.gpe_mapped_transfers.restype = C.c_int64
+    lib.gpe_mapped_transfers.argtypes = [C.c_void_p]
     lib.gpe_stream.restype = C.c_void_p
     lib.gpe_stream.argtypes = [C.c_void_p]
     lib.gpe_time_steps.restype = st
@@ -514,6 +516,10 @@ class Stepper:
 
     def launch_count(self) -> int:
         return int(self.lib.gpe_launch_count(self.h))
+
+    def mapped_transfers(self) -> int:
+        """Host buffers converted in place (mapped page-locked memory, no staging copy)."""
+        return int(self.lib.gpe_mapped_transfers(self.h))
 
     def stream_handle(self) -> int:
         """The cudaStream_t the library launches on (as an integer)."""
