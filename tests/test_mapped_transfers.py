@@ -120,3 +120,47 @@ def test_misaligned_mapped_buffer_falls_back_to_staging():
     del be, bo
     a.close()
     b.close()
+
+
+def test_mixed_mapped_and_pageable_batch():
+    """Batched calls with some buffers mapped and some pageable: the mapped ones
+    are converted in place, the rest staged, and the fields are the same."""
+    insts = _insts()
+    kw = dict(lattice=Lattice.BCC2, precision=Precision.FP32C, kernel=Kernel.FUSED, potential=Potential.TRAP)
+    a, b = Stepper(insts, **kw), Stepper(insts, **kw)
+    keep, staged, mixed = [], [], []
+    for i in range(len(insts)):
+        shp = a.shape(i)
+        ze, zo = random_state(shp, 60 + i, 0.3), random_state(shp, 70 + i, 0.3)
+        e = np.stack([ze.real, ze.imag], -1)
+        o = np.stack([zo.real, zo.imag], -1)
+        staged.append((i, e, o, None))
+        if i % 2 == 0:  # even field pinned on even instances
+            pe, be = _pinned(e.shape, np.float64)
+            pe[...] = e
+            keep.append(be)
+            mixed.append((i, pe, o, None))
+        else:
+            mixed.append((i, e, o, None))
+    a.upload_many(staged)
+    b.upload_many(mixed)
+    assert b.mapped_transfers() == (len(insts) + 1) // 2
+    a.step(4)
+    b.step(4)
+    want = a.download_many(range(len(insts)))
+    outs = []
+    for i in range(len(insts)):
+        shp = a.shape(i) + (2,)
+        if i % 2:
+            po, bo = _pinned(shp, np.float64)
+            keep.append(bo)
+            outs.append((np.empty(shp), po))
+        else:
+            outs.append((np.empty(shp), np.empty(shp)))
+    b.download_many(range(len(insts)), outs=outs)
+    assert b.mapped_transfers() == (len(insts) + 1) // 2 + len(insts) // 2
+    for (we, wo), (ge, go) in zip(want, outs):
+        np.testing.assert_array_equal(ge, we)
+        np.testing.assert_array_equal(go, wo)
+    a.close()
+    b.close()

@@ -119,6 +119,9 @@ struct gpe_handle_ {
     size_t batch_bytes = 0;
     cudaStream_t copy_stream = nullptr;     // their host<->device copies, beside the conversions
     std::vector<cudaEvent_t> xfer_events;   // one per transfer slot
+    XferSeg *xfer_segs = nullptr;           // batched in-place transfers: the launch's segments
+    size_t xfer_segs_cap = 0;
+    std::vector<XferSeg> xfer_segs_host;
     cudaStream_t stream = nullptr;
     std::map<GraphKey, cudaGraphExec_t> graphs;
     int parity = 0;      // imaginary time: which buffer holds psi; two-step: which set holds the fields
@@ -677,6 +680,7 @@ void free_handle(gpe_handle h)
     cudaFree(h->staging);
     cudaFree(h->batch_staging);
     for (cudaEvent_t e : h->xfer_events) cudaEventDestroy(e);
+    cudaFree(h->xfer_segs);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -946,7 +950,7 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
     std::vector<int> cta_begin(cfg->num_instances + 1, 0), cta_inst;
     for (int i = 0; i < cfg->num_instances; i++) {
         const gpe_instance &in = h->inst[i];
-        const int c = observables_ctas((long long)in.nx * in.ny * in.nz * h->ns, h->obs_max_ctas);
+        const int c = observables_batch_ctas((long long)in.nx * in.ny * in.nz * h->ns, h->obs_max_ctas);
         cta_begin[i + 1] = cta_begin[i] + c;
         cta_inst.insert(cta_inst.end(), size_t(c), i);
     }
@@ -1312,6 +1316,37 @@ gpe_status ensure_xfer(gpe_handle h, size_t n)
     return GPE_OK;
 }
 
+// One launch converting every listed (instance, field) between its mapped host
+// buffer and the device layout, on the handle's stream (segments in order).
+gpe_status run_xfer_batch(gpe_handle h, bool up, const std::vector<std::tuple<const void *, int, int>> &items)
+{
+    std::vector<XferSeg> &segs = h->xfer_segs_host;
+    segs.clear();
+    int cta = 0;
+    for (const auto &it : items) {
+        const gpe_instance &in = h->inst[std::get<1>(it)];
+        const long long vals = (long long)in.nx * in.ny * in.nz * h->ns;
+        segs.push_back({std::get<0>(it), std::get<1>(it), std::get<2>(it), cta, 0});
+        cta += int((vals + kXferValuesPerCta - 1) / kXferValuesPerCta);
+    }
+    segs.push_back({nullptr, 0, 0, cta, 0});
+    if (segs.size() > h->xfer_segs_cap) {
+        cudaFree(h->xfer_segs);
+        h->xfer_segs = nullptr;
+        h->xfer_segs_cap = 0;
+        GPE_CUDA_TRY(cudaMalloc(&h->xfer_segs, sizeof(XferSeg) * segs.size()));
+        h->xfer_segs_cap = segs.size();
+    }
+    GPE_CUDA_TRY(cudaMemcpyAsync(h->xfer_segs, segs.data(), sizeof(XferSeg) * segs.size(), cudaMemcpyHostToDevice,
+                                 h->stream));
+    GPE_CUDA_TRY(launch_xfer_batch(h->cfg.precision, h->comp, h->host_fp32, up, h->idev, h->xfer_segs,
+                                   int(segs.size()) - 1, cta, field_buf(h, 0), field_buf(h, 1), h->lo[0], h->lo[1],
+                                   h->stream));
+    h->launches++;
+    h->mapped_transfers += (long long)items.size();
+    return GPE_OK;
+}
+
 }  // namespace
 
 static gpe_status gpe_upload_many_impl(gpe_handle h, int32_t count, const int32_t *instances, const void *const *even,
@@ -1342,9 +1377,18 @@ static gpe_status gpe_upload_many_impl(gpe_handle h, int32_t count, const int32_
         for (int f = 0; f < 3; f++) {
             if (!bufs[f]) continue;
             mapped[3 * k + f] = mapped_host_range(bufs[f], bytes[f], align[f], h->cfg.device);
-            if (mapped[3 * k + f]) h->mapped_transfers++;
-            else total += slot_bytes(bytes[f]);
+            if (!mapped[3 * k + f]) total += slot_bytes(bytes[f]);
         }
+    }
+    if (total == 0 && !arr) {  // every field in mapped memory: one in-place launch
+        std::vector<std::tuple<const void *, int, int>> items;
+        for (int k = 0; k < count; k++)
+            for (int f = 0; f < 2; f++)
+                if (mapped[3 * k + f]) items.emplace_back(mapped[3 * k + f], instances[k], f);
+        if (!items.empty() && (st = run_xfer_batch(h, true, items)) != GPE_OK) return st;
+        GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+        h->imag_ready = false;
+        return GPE_OK;
     }
     st = ensure_batch_staging(h, std::max<size_t>(total, 256));
     if (st == GPE_OK) st = ensure_xfer(h, size_t(3) * count + 1);
@@ -1374,7 +1418,8 @@ static gpe_status gpe_upload_many_impl(gpe_handle h, int32_t count, const int32_
             if (!srcs[f]) continue;
             const size_t b = vals * 2 * h->hsize;
             const void *src = mapped[3 * k + f];
-            if (!src) {
+            if (src) h->mapped_transfers++;
+            else {
                 if ((st = copy_in(stage, srcs[f], b)) != GPE_OK) return st;
                 src = stage;
                 stage += slot_bytes(b);
@@ -1390,7 +1435,8 @@ static gpe_status gpe_upload_many_impl(gpe_handle h, int32_t count, const int32_
         if (arr) {
             const size_t b = vals * h->esize;
             const void *src = mapped[3 * k + 2];
-            if (!src) {
+            if (src) h->mapped_transfers++;
+            else {
                 if ((st = copy_in(stage, potential[k], b)) != GPE_OK) return st;
                 src = stage;
                 stage += slot_bytes(b);
@@ -1433,12 +1479,20 @@ static gpe_status gpe_download_many_impl(gpe_handle h, int32_t count, const int3
         for (int f = 0; f < 2; f++) {
             if (!dsts[f]) continue;
             mapped[2 * k + f] = mapped_host_range(dsts[f], vals * 2 * h->hsize, 2 * h->hsize, h->cfg.device);
-            if (mapped[2 * k + f]) h->mapped_transfers++;
-            else total += slot_bytes(vals * 2 * h->hsize);
+            if (!mapped[2 * k + f]) total += slot_bytes(vals * 2 * h->hsize);
         }
     }
     st = sync_and_check(h);
     if (st != GPE_OK) return st;
+    if (total == 0) {  // every buffer in mapped memory: one in-place launch
+        std::vector<std::tuple<const void *, int, int>> items;
+        for (int k = 0; k < count; k++)
+            for (int f = 0; f < 2; f++)
+                if (mapped[2 * k + f]) items.emplace_back(mapped[2 * k + f], instances[k], f);
+        if (!items.empty() && (st = run_xfer_batch(h, false, items)) != GPE_OK) return st;
+        GPE_CUDA_TRY(cudaStreamSynchronize(h->stream));
+        return GPE_OK;
+    }
     st = ensure_batch_staging(h, std::max<size_t>(total, 256));
     if (st == GPE_OK) st = ensure_xfer(h, size_t(2) * count);
     if (st != GPE_OK) return st;
@@ -1455,6 +1509,7 @@ static gpe_status gpe_download_many_impl(gpe_handle h, int32_t count, const int3
             if (!dsts[f]) continue;
             const size_t b = vals * 2 * h->hsize;
             void *out = mapped[2 * k + f] ? mapped[2 * k + f] : stage;
+            if (mapped[2 * k + f]) h->mapped_transfers++;
             if (h->comp)
                 GPE_CUDA_TRY(launch_unpack_join(h->idev, i, in.nx, in.ny, in.nz, h->ns, field_buf(h, f), h->lo[f], out,
                                                 h->host_fp32, h->stream));

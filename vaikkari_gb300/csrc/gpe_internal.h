@@ -171,6 +171,8 @@ struct ObsLaunch {
 cudaError_t launch_observables(const ObsLaunch &l, cudaStream_t s, int *ctas_used);
 // CTAs the observables kernel uses for an instance of `values` values.
 int observables_ctas(long long values, int max_ctas);
+constexpr int kObsValuesPerBatchCta = 4096;
+int observables_batch_ctas(long long values, int max_ctas);
 // Observables partial rows of every instance in one launch (cta_inst: instance of
 // each CTA; cta_begin: first CTA of each instance, plus the total), then one
 // CTA per instance folding its rows into out[6 * i ...].
@@ -200,6 +202,23 @@ cudaError_t launch_pack_split(const InstDev *inst, int ii, int nx, int ny, int n
                               void *field, void *lo, bool host_fp32, cudaStream_t s);
 cudaError_t launch_unpack_join(const InstDev *inst, int ii, int nx, int ny, int nz, int slots, const void *field,
                                const void *lo, void *host_order, bool host_fp32, cudaStream_t s);
+// One field of one instance in a batched transfer: its host buffer (mapped
+// page-locked memory, used in place) and the first CTA of its share of the
+// launch.  The array ends with a sentinel whose cta0 is the launch's CTA count.
+struct XferSeg {
+    const void *host;
+    int inst;
+    int field;
+    int cta0;
+    int pad;
+};
+constexpr int kXferValuesPerCta = 1024;  // 256 threads, 4 values each
+// Every segment of a batched upload (up = true: host order -> device layout)
+// or download in one launch: plain storage of `precision` (GPE_FP32, GPE_FP64),
+// or comp (GPE_FP32C) with the host element float (host_fp32) or double.
+cudaError_t launch_xfer_batch(int precision, bool comp, bool host_fp32, bool up, const InstDev *inst,
+                              const XferSeg *segs, int nseg, int ctas, void *field0, void *field1, void *lo0, void *lo1,
+                              cudaStream_t s);
 // Field outputs (gpe_output.cu).
 cudaError_t launch_volume(int precision, const InstDev *inst, int ii, const void *field, double unit, int quirk,
                           uint16_t *out, long long total, cudaStream_t s);

@@ -516,8 +516,8 @@ __device__ __forceinline__ FPair2 fp2_mul(FPair2 x, FPair2 y)
 template <int LAT, int POT>
 __device__ __forceinline__ void observables_terms_f32(const InstDev &d, const float2 *__restrict__ f,
                                                       const float *__restrict__ vpot, int s, int x, int y, int z,
-                                                      long long self, const FPair (&w)[2], FPair rdt, FPair half_g,
-                                                      FPair (&acc)[4])
+                                                      long long self, const long long *__restrict__ off,
+                                                      const FPair (&w)[2], FPair rdt, FPair half_g, FPair (&acc)[4])
 {
     using L = Lat<LAT>;
     const float2 pt = f[self];
@@ -525,9 +525,7 @@ __device__ __forceinline__ void observables_terms_f32(const InstDev &d, const fl
     float2 h[2] = {zero, zero}, l[2] = {zero, zero};
 #pragma unroll
     for (int k = 0; k < L::NB; k++) {
-        const int e = L::entry(s * L::NB + k);
-        const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
-        const float2 q = f[self + (long long)dz * d.zstride + (long long)(sl - s) * d.plane + dy * d.px + dx];
+        const float2 q = f[self + off[k]];
         const int c = (k < L::N0) ? 0 : 1;
         const FPair2 t = fp2_two_sum(h[c], q);
         h[c] = t.hi;
@@ -566,6 +564,15 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
     Kahan k0, k1, k2, k3;
     const double wsum = L::N0 * d.w[0] + (L::NB - L::N0) * d.w[1];
     const double rdt = 1.0 / d.dt;
+    // neighbour k of a value in slot s sits nb_off[s * NB + k] places from it
+    // (the CTA's instance; the lattice form's table)
+    __shared__ long long nb_off[L::NS * L::NB];
+    for (int i = threadIdx.x; i < L::NS * L::NB; i += blockDim.x) {
+        const int e = L::entry(i), sl0 = i / L::NB;
+        const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
+        nb_off[i] = (long long)dz * d.zstride + (long long)(sl - sl0) * d.plane + (long long)dy * d.px + dx;
+    }
+    __syncthreads();
     if constexpr (sizeof(T) == 4 && LAT != kStepTetra12Faces) {
         if (!(LAT == GPE_LATTICE_TETRA12 && d.face)) {
             const FPair w[2] = {fp_of(d.w[0]), fp_of(d.w[1])};
@@ -575,7 +582,8 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
                 int x, y, s, z;
                 digits(v, d.nx, d.ny, L::NS, x, y, s, z);
                 observables_terms_f32<LAT, POT>(d, (const float2 *)f, (const float *)vpot, s, x, y, z,
-                                                field_index(d, s, x, y, z), w, rdt2, half_g, acc);
+                                                field_index(d, s, x, y, z), nb_off + s * L::NB, w, rdt2, half_g,
+                                                acc);
             }
             double out[6] = {fp_value(acc[0]), fp_value(acc[1]), fp_value(acc[2]), fp_value(acc[3]), 0.0, 0.0};
             cta_tree_store<6>(out, row);
@@ -612,9 +620,7 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
                 float hx[2] = {0.f, 0.f}, lx_[2] = {0.f, 0.f}, hy[2] = {0.f, 0.f}, ly_[2] = {0.f, 0.f};
 #pragma unroll
                 for (int k = 0; k < L::NB; k++) {
-                    const int e = L::entry(s * L::NB + k);
-                    const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
-                    const T2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
+                    const T2 q = f[self + nb_off[s * L::NB + k]];
                     const int c = (k < L::N0) ? 0 : 1;
                     float t = __fadd_rn(hx[c], q.x), bb = __fsub_rn(t, hx[c]);
                     lx_[c] = __fadd_rn(lx_[c], __fadd_rn(__fsub_rn(hx[c], __fsub_rn(t, bb)), __fsub_rn(q.x, bb)));
@@ -632,9 +638,7 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
             } else {
 #pragma unroll
                 for (int k = 0; k < L::NB; k++) {
-                    const int e = L::entry(s * L::NB + k);
-                    const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
-                    const T2 q = f[field_index(d, sl, x + dx, y + dy, z + dz)];
+                    const T2 q = f[self + nb_off[s * L::NB + k]];
                     const int c = (k < L::N0) ? 0 : 1;
                     sx[c] += double(q.x);
                     sy[c] += double(q.y);
@@ -666,8 +670,9 @@ __global__ void __launch_bounds__(256) observables_kernel(const InstDev *__restr
 }
 
 // Every instance in one launch: CTA b belongs to instance cta_inst[b] and is its
-// (b - cta_begin[i])-th CTA of cta_begin[i+1] - cta_begin[i], so each CTA covers
-// the values it would cover in that instance's own launch (same sums, same rows).
+// (b - cta_begin[i])-th CTA of cta_begin[i+1] - cta_begin[i]
+// (observables_batch_ctas), covering values first, first + stride, ... of the
+// instance as in its own launch, with fewer, longer-lived CTAs.
 template <typename T, int LAT, int POT>
 __global__ void __launch_bounds__(256) observables_batch_kernel(const InstDev *__restrict__ insts,
                                                                 const int *__restrict__ cta_inst,
@@ -718,6 +723,17 @@ __global__ void __launch_bounds__(256) reduce_partials_kernel(const double *__re
 int observables_ctas(long long values, int max_ctas)
 {
     long long want = (values + 255) / 256;
+    int ctas = int(want < max_ctas ? want : max_ctas);
+    return ctas < 1 ? 1 : ctas;
+}
+
+// In the batched launch the instances' CTAs run together, so each instance gets
+// one CTA per 4096 values (16 per thread): a CTA then spends most of its life on
+// values rather than on its closing tree of partial sums (one value per thread
+// left the warps waiting at that tree's barriers for most of the launch).
+int observables_batch_ctas(long long values, int max_ctas)
+{
+    long long want = (values + kObsValuesPerBatchCta - 1) / kObsValuesPerBatchCta;
     int ctas = int(want < max_ctas ? want : max_ctas);
     return ctas < 1 ? 1 : ctas;
 }
@@ -961,6 +977,82 @@ cudaError_t launch_unpack_join(const InstDev *inst, int ii, int nx, int ny, int 
     else
         unpack_join_kernel<double><<<g, 256, 0, s>>>(inst, ii, (const float *)field, (const uint16_t *)lo,
                                                      (double *)host_order);
+    return cudaGetLastError();
+}
+
+// ---- Batched transfers: every instance's fields in one launch ---------------
+// Segment k (one field of one instance) owns CTAs segs[k].cta0 .. segs[k+1].cta0
+// - 1 and converts between its host buffer, which the kernel reads or writes in
+// place over the host link, and the padded device layout, with the arithmetic
+// of pack_kernel / unpack_kernel (plain storage) or pack_split_kernel /
+// unpack_join_kernel (GPE_FP32C).  One launch instead of one per field keeps the
+// host link busy from the first segment to the last.
+struct XferFields {
+    void *field[2];
+    uint16_t *lo[2];
+};
+
+template <typename T, typename H, bool COMP, bool UP>
+__global__ void __launch_bounds__(256) xfer_batch_kernel(const InstDev *__restrict__ insts,
+                                                         const XferSeg *__restrict__ segs, int nseg, XferFields fl)
+{
+    int a = 0, b = nseg - 1;  // the last segment whose first CTA is <= this one
+    while (a < b) {
+        const int m = (a + b + 1) >> 1;
+        if (segs[m].cta0 <= int(blockIdx.x)) a = m;
+        else b = m - 1;
+    }
+    const XferSeg g = segs[a];
+    const int ctas = segs[a + 1].cta0 - g.cta0;
+    const InstDev &d = insts[g.inst];
+    const long long total = (long long)d.nx * d.ny * d.nz * d.slots;
+    using T2 = typename Cplx<T>::type;
+    using H2 = typename Cplx<H>::type;
+    T2 *__restrict__ field = (T2 *)fl.field[g.field];
+    uint16_t *__restrict__ lo = fl.lo[g.field];
+    for (long long v = (long long)(blockIdx.x - g.cta0) * blockDim.x + threadIdx.x; v < total;
+         v += (long long)ctas * blockDim.x) {
+        int s, x, y, z;
+        digits(v, d.slots, d.nx, d.ny, s, x, y, z);
+        const long long o = field_index(d, s, x, y, z);
+        if constexpr (UP && COMP) {
+            const H2 hv = ((const H2 *)g.host)[v];
+            const double va = double(hv.x), vb = double(hv.y);
+            const float ha = __double2float_rn(va), hb = __double2float_rn(vb);
+            field[o] = make_float2(ha, hb);
+            const uint32_t qa = comp_encode(__double2float_rn(va - double(ha)), ha);
+            const uint32_t qb = comp_encode(__double2float_rn(vb - double(hb)), hb);
+            lo[o - kLoShift] = uint16_t(qa | (qb << 8));
+        } else if constexpr (UP) {
+            field[o] = ((const T2 *)g.host)[v];
+        } else if constexpr (COMP) {
+            const uint32_t w = lo[o - kLoShift];
+            const float2 hv = field[o];
+            H2 out;
+            out.x = H(double(hv.x) + double(comp_decode(w, hv.x)));
+            out.y = H(double(hv.y) + double(comp_decode(w >> 8, hv.y)));
+            ((H2 *)g.host)[v] = out;
+        } else {
+            ((T2 *)g.host)[v] = field[o];
+        }
+    }
+}
+
+cudaError_t launch_xfer_batch(int precision, bool comp, bool host_fp32, bool up, const InstDev *inst,
+                              const XferSeg *segs, int nseg, int ctas, void *field0, void *field1, void *lo0, void *lo1,
+                              cudaStream_t s)
+{
+    const XferFields fl = {{field0, field1}, {(uint16_t *)lo0, (uint16_t *)lo1}};
+#define GPE_XB(T, H, C, U) xfer_batch_kernel<T, H, C, U><<<ctas, 256, 0, s>>>(inst, segs, nseg, fl)
+    if (comp) {
+        if (host_fp32) { if (up) GPE_XB(float, float, true, true); else GPE_XB(float, float, true, false); }
+        else { if (up) GPE_XB(float, double, true, true); else GPE_XB(float, double, true, false); }
+    } else if (precision == GPE_FP64) {
+        if (up) GPE_XB(double, double, false, true); else GPE_XB(double, double, false, false);
+    } else {
+        if (up) GPE_XB(float, float, false, true); else GPE_XB(float, float, false, false);
+    }
+#undef GPE_XB
     return cudaGetLastError();
 }
 
