@@ -3,11 +3,11 @@
 //
 // Device layout of one field of one instance ("block-ordered structure of
 // arrays"): index
-//     base + (z+1)*zstride + s*plane + (y+1)*px + (x+2)
+//     base + (z+1)*zstride + s*plane + (y+1)*px + (x+kPadX)
 // for block (x,y,z), slot s; plane = px*(ny+2), zstride = slots*plane.  Each
 // instance carries a ring of zero values around its blocks (one plane below and
-// above, one row at each y end, one column before and after x, plus one more
-// column in front so that interior rows start on a 16-byte boundary for FP32
+// above, one row at each y end, at least one column after x and kPadX = 2
+// columns before it, so that interior rows start on a 16-byte boundary for FP32
 // pairs).  The zeros are the Dirichlet psi = 0 boundary that the reference gets
 // from its padding blocks (GPUGrossPitaevskii_BCC.cu:269-287); they are never
 // written, so stencil reads need no bounds checks.
