@@ -1010,13 +1010,27 @@ __global__ void __launch_bounds__(256) xfer_batch_kernel(const InstDev *__restri
     using H2 = typename Cplx<H>::type;
     T2 *__restrict__ field = (T2 *)fl.field[g.field];
     uint16_t *__restrict__ lo = fl.lo[g.field];
-    for (long long v = (long long)(blockIdx.x - g.cta0) * blockDim.x + threadIdx.x; v < total;
-         v += (long long)ctas * blockDim.x) {
+    // Each thread's values v0, v0 + step, ...: the host reads of an upload are
+    // issued together (kXferValuesPerCta / 256 of them in flight per thread),
+    // then converted and stored.
+    constexpr int K = kXferValuesPerCta / 256;
+    const long long step = (long long)ctas * blockDim.x;
+    const long long v0 = (long long)(blockIdx.x - g.cta0) * blockDim.x + threadIdx.x;
+    H2 hin[K];
+    if constexpr (UP) {
+#pragma unroll
+        for (int k = 0; k < K; k++)
+            if (v0 + k * step < total) hin[k] = ((const H2 *)g.host)[v0 + k * step];
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const long long v = v0 + k * step;
+        if (v >= total) break;
         int s, x, y, z;
         digits(v, d.slots, d.nx, d.ny, s, x, y, z);
         const long long o = field_index(d, s, x, y, z);
         if constexpr (UP && COMP) {
-            const H2 hv = ((const H2 *)g.host)[v];
+            const H2 hv = hin[k];
             const double va = double(hv.x), vb = double(hv.y);
             const float ha = __double2float_rn(va), hb = __double2float_rn(vb);
             field[o] = make_float2(ha, hb);
@@ -1024,7 +1038,7 @@ __global__ void __launch_bounds__(256) xfer_batch_kernel(const InstDev *__restri
             const uint32_t qb = comp_encode(__double2float_rn(vb - double(hb)), hb);
             lo[o - kLoShift] = uint16_t(qa | (qb << 8));
         } else if constexpr (UP) {
-            field[o] = ((const T2 *)g.host)[v];
+            field[o] = hin[k];
         } else if constexpr (COMP) {
             const uint32_t w = lo[o - kLoShift];
             const float2 hv = field[o];
