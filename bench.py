@@ -727,7 +727,8 @@ def _cpu_config_rate(conds, budget_s=5.0, lattice=None):
 def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1, lattice=None):
     """FP32 against FP64 of the same scheme at each checkpoint, plus throughput.
     BCC2 (config-mode): the fused kernel, and the FP64 plain path beside it.
-    TETRA12 (ref-mode, the reference's discretisation): the plain kernel."""
+    TETRA12 (ref-mode, the reference's discretisation): the fused TETRA12 kernel
+    in FP32 (the line's value), the plain kernel in FP32 and FP64 beside it."""
     from vaikkari_gb300.gpe import Kernel, Lattice, Mode, Precision
     lattice = Lattice.BCC2 if lattice is None else Lattice(lattice)
     ref_mode = lattice == Lattice.TETRA12
@@ -745,7 +746,8 @@ def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1, latt
     fp64_last = fp64_steps or checkpoints[-1]
     runs = {}
     for prec, dt_, last in ((Precision.FP64, np.float64, fp64_last), (Precision.FP32, np.float32, checkpoints[-1])):
-        st = _stepper(conds, prec, kern, Mode.REAL, tile=tile, lattice=lattice, zchunk=zchunk)
+        k_ = Kernel.PLAIN if (ref_mode and prec == Precision.FP64) else (Kernel.FUSED if ref_mode else kern)
+        st = _stepper(conds, prec, k_, Mode.REAL, tile=tile, lattice=lattice, zchunk=zchunk)
         prepare_fields(st, conds, dt_)
         o0 = st.observables(0)
         done, cps = 0, {}
@@ -775,10 +777,11 @@ def run_config_realtime(name, conds, checkpoints, fp64_steps=None, tile=-1, latt
     # throughput, device time: windows of 200 steps (one graph replay each) after
     # warm-up, median, with the clocks sampled over the FP32 windows
     rates, rooflines, clocks = {}, {}, None
-    cases = ((("fp32_plain", Precision.FP32, Kernel.PLAIN), ("fp64_plain", Precision.FP64, Kernel.PLAIN)) if ref_mode
+    cases = ((("fp32_fused", Precision.FP32, Kernel.FUSED), ("fp32_plain", Precision.FP32, Kernel.PLAIN),
+              ("fp64_plain", Precision.FP64, Kernel.PLAIN)) if ref_mode
              else (("fp32_fused", Precision.FP32, Kernel.FUSED), ("fp32c_fused", Precision.FP32C, Kernel.FUSED),
                    ("fp64_fused", Precision.FP64, Kernel.FUSED), ("fp64_plain", Precision.FP64, Kernel.PLAIN)))
-    head = "fp32_plain" if ref_mode else "fp32_fused"
+    head = "fp32_fused"
     for key, prec, kern_ in cases:
         tk, zk = (tile, zchunk) if kern_ == kern and prec != Precision.FP32C else (0, 0)
         if prec == Precision.FP32C:
@@ -1058,10 +1061,13 @@ def run_tetra12(args):
     vals = inst.nx * inst.ny * inst.nz * 12
     rates = {}
     faces = default_face_table()
-    for name, prec, fc in (("fp64", Precision.FP64, None), ("fp32", Precision.FP32, None),
-                           ("fp64_faces", Precision.FP64, faces), ("fp32_faces", Precision.FP32, faces)):
-        st = Stepper([inst], lattice=Lattice.TETRA12, precision=prec, kernel=Kernel.PLAIN,
-                     potential=Potential.ARRAY, graph_steps=100, faces=fc)
+    for name, prec, fc, kern in (("fp64", Precision.FP64, None, Kernel.PLAIN),
+                                 ("fp32", Precision.FP32, None, Kernel.PLAIN),
+                                 ("fp32_fused", Precision.FP32, None, Kernel.FUSED),
+                                 ("fp64_faces", Precision.FP64, faces, Kernel.PLAIN),
+                                 ("fp32_faces", Precision.FP32, faces, Kernel.PLAIN)):
+        st = Stepper([inst], lattice=Lattice.TETRA12, precision=prec, kernel=kern,
+                     potential=Potential.ARRAY, graph_steps=100, faces=fc, tile=3 if kern == Kernel.FUSED else 0)
         st.upload(0, e, o, V)
         st.time_steps(100)
         ms = min(st.time_steps(args.steps) for _ in range(3))
@@ -1072,6 +1078,7 @@ def run_tetra12(args):
             "config": {"workload": "tetra12_plain_production_grid", "values": vals, "blocks": [87, 87, 302],
                        "lattice": "TETRA12", "kernel": "plain", "potential": "array"},
             "fp32": rates["fp32"],
+            "fp32_fused": rates["fp32_fused"],
             "faces": {"fp64": rates["fp64_faces"], "fp32": rates["fp32_faces"],
                       "form": "Hodge (face) form of GPUGrossPitaevskii_BCC_multi.cu:329-397, weights 1.5"},
             "note": "FP64 performs the reference kernel's rounded operations and equals its results bit for "

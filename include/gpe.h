@@ -83,9 +83,12 @@ typedef enum gpe_time_mode {
 } gpe_time_mode;
 
 typedef enum gpe_kernel_kind {
-    GPE_KERNEL_AUTO = 0,   /* fused where built (BCC2), plain otherwise          */
+    GPE_KERNEL_AUTO = 0,   /* fused where built, plain otherwise                 */
     GPE_KERNEL_PLAIN = 1,  /* table-driven, one value per thread, any lattice    */
-    GPE_KERNEL_FUSED = 2   /* BCC2 only: shared-memory tiled, z-marching, batched */
+    GPE_KERNEL_FUSED = 2   /* shared-memory tiled, z-marching, batched: BCC2 in
+                            * every storage and mode; TETRA12 in GPE_FP32, real
+                            * time, lattice form (the reference's neighbour order,
+                            * results equal the plain kernel's bit for bit)      */
 } gpe_kernel_kind;
 
 typedef enum gpe_potential_kind {
@@ -143,7 +146,10 @@ typedef struct gpe_config {
     int32_t num_instances;  /* >= 1               */
     const gpe_instance *instances;
     int32_t graph_steps;    /* steps per captured CUDA graph; 0 = 100, < 0 = no graphs */
-    int32_t tile;           /* fused-kernel tile variant; 0 = autotuned/default   */
+    int32_t tile;           /* fused-kernel tile variant; 0 = autotuned/default.
+                             * TETRA12: 0..3 = 32x4 (6 stages), 32x2 (8), 32x6 (5),
+                             * 32x3 (7) block columns (gpe_variant_* describe the
+                             * BCC2 variants)                                     */
     int32_t zchunk;         /* planes per work item of the fused kernel; 0 = auto  */
     int32_t device;         /* CUDA device ordinal                                 */
     /* TETRA12 and the plain kernel only.  NULL: the update of

@@ -59,7 +59,8 @@ def test_invalid_arguments_return_status():
         Stepper([Instance(4, 4, 4, -1.0, 1e-3, 1.0)])
     assert e.value.status == Status.INVALID_ARGUMENT
     with pytest.raises(GpeError) as e:
-        Stepper([Instance(4, 4, 4, 0.5, 1e-3, 1.0)], lattice=Lattice.TETRA12, kernel=gpe.Kernel.FUSED)
+        Stepper([Instance(4, 4, 4, 0.5, 1e-3, 1.0)], lattice=Lattice.TETRA12, kernel=gpe.Kernel.FUSED,
+                precision=gpe.Precision.FP64)  # the fused TETRA12 kernel is FP32 only
     assert e.value.status == Status.UNSUPPORTED
     with pytest.raises(GpeError) as e:
         Stepper([Instance(4, 4, 6000, 0.5, 1e-3, 1.0)], lattice=Lattice.TETRA12)

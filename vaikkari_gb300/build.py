@@ -24,7 +24,7 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "libgpe_oracle.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["gpe_lattice.cpp", "gpe_api.cpp", "gpe_vortex.cpp", "gpe_plain.cu", "gpe_fused.cu", "gpe_persistent.cu", "gpe_output.cu", "gpe_noalloc.cu", "gpe_relax.cu",
+SOURCES = ["gpe_lattice.cpp", "gpe_api.cpp", "gpe_vortex.cpp", "gpe_plain.cu", "gpe_fused.cu", "gpe_fused_t12.cu", "gpe_persistent.cu", "gpe_output.cu", "gpe_noalloc.cu", "gpe_relax.cu",
            "gpe_setup.cu"]
 
 

@@ -95,6 +95,9 @@ struct gpe_handle_ {
     int *pb_inst = nullptr, *pb_begin = nullptr, *pb_zcs = nullptr;
     int pb_blocks = 0;
     bool fused = false;
+    bool t12 = false;                 // the fused TETRA12 kernel (FP32, real time)
+    int t12_tab[48] = {};             // its packed neighbour entries
+    void *t12_vmaps = nullptr;        // its ARRAY-potential maps, one per instance
     int tile = 0, tx = 32, ty = 8, zchunk = 0, zcmax = 1;
     std::vector<WorkItem> items;
     WorkItem *items_dev = nullptr;
@@ -370,7 +373,24 @@ gpe_status enqueue_step_real(gpe_handle h)
     for (int half = 0; half < 2; half++) {
         void *prev = field_buf(h, half == 0 ? 0 : 1);
         void *next = field_buf(h, half == 0 ? 1 : 0);
-        if (h->fused) {
+        if (h->t12) {
+            T12Launch l{};
+            l.potential = h->cfg.potential;
+            l.variant = h->tile;
+            l.grid = h->grid;
+            l.src = half == 0 ? 0 : 1;
+            l.inject_skip_plane = h->inject;
+            l.inst = h->idev;
+            l.items = h->items_dev;
+            l.maps = h->maps;
+            l.vmaps = h->t12_vmaps;
+            l.next = next;
+            l.vpot = h->cfg.potential == GPE_POTENTIAL_ARRAY ? h->vbase : h->vpot;
+            l.err = h->err;
+            std::memcpy(l.tab, h->t12_tab, sizeof(l.tab));
+            GPE_CUDA_TRY(launch_t12_step(l, h->stream));
+            h->launches++;
+        } else if (h->fused) {
             FusedLaunch l{};
             l.precision = h->cfg.precision;
             l.mode = GPE_REAL_TIME;
@@ -681,6 +701,7 @@ void free_handle(gpe_handle h)
     cudaFree(h->batch_staging);
     for (cudaEvent_t e : h->xfer_events) cudaEventDestroy(e);
     cudaFree(h->xfer_segs);
+    cudaFree(h->t12_vmaps);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -759,8 +780,10 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: unknown kernel kind");
     if (cfg->num_instances < 1 || !cfg->instances)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: need at least one instance");
-    if (cfg->kernel == GPE_KERNEL_FUSED && cfg->lattice != GPE_LATTICE_BCC2)
-        return fail(GPE_ERR_UNSUPPORTED, "gpe_create: the fused kernel is built for the BCC2 lattice only");
+    if (cfg->kernel == GPE_KERNEL_FUSED && cfg->lattice == GPE_LATTICE_TETRA12 &&
+        (cfg->precision != GPE_FP32 || cfg->mode != GPE_REAL_TIME || cfg->faces))
+        return fail(GPE_ERR_UNSUPPORTED, "gpe_create: the fused kernel takes the TETRA12 lattice in GPE_FP32, real "
+                                         "time and the lattice form only (the plain kernel runs the rest)");
     if (cfg->faces) {
         if (cfg->lattice != GPE_LATTICE_TETRA12 || cfg->kernel == GPE_KERNEL_FUSED || cfg->precision == GPE_FP32C)
             return fail(GPE_ERR_UNSUPPORTED, "gpe_create: a face table needs the TETRA12 lattice, the plain kernel "
@@ -803,8 +826,20 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
     h->esize = cfg->precision == GPE_FP64 ? 8 : 4;
     h->comp = cfg->precision == GPE_FP32C;
     h->hsize = h->comp ? 8 : h->esize;
-    h->fused = (cfg->lattice == GPE_LATTICE_BCC2) && (cfg->kernel != GPE_KERNEL_PLAIN);
-    if (h->fused && !bcc2_order_matches(h->lat)) {
+    // TETRA12: the fused kernel when asked for, and by default in FP32 real time
+    // in the lattice form (the plain kernel runs FP64, imaginary time and faces).
+    h->t12 = cfg->lattice == GPE_LATTICE_TETRA12 &&
+             (cfg->kernel == GPE_KERNEL_FUSED ||
+              (cfg->kernel == GPE_KERNEL_AUTO && cfg->precision == GPE_FP32 && cfg->mode == GPE_REAL_TIME &&
+               !cfg->faces));
+    h->fused = (cfg->lattice == GPE_LATTICE_BCC2 && cfg->kernel != GPE_KERNEL_PLAIN) || h->t12;
+    if (h->t12)
+        for (int s = 0; s < 12; s++)
+            for (int k = 0; k < 4; k++) {
+                const int *e = h->lat.entry[s][k];
+                h->t12_tab[s * 4 + k] = (e[0] + 1) | ((e[1] + 1) << 2) | ((e[2] + 1) << 4) | (e[3] << 6);
+            }
+    if (h->fused && !h->t12 && !bcc2_order_matches(h->lat)) {
         free_handle(h);
         return fail(GPE_ERR_INTERNAL, "BCC2 table order differs from the fused kernel's");
     }
@@ -993,10 +1028,16 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
     }
     GPE_CREATE_TRY(cudaStreamSynchronize(h->stream));  // the host tables above go out of scope
 
-    if (h->fused) {
+    if (h->t12) {
+        int st_;
+        h->tile = cfg->tile > 0 && cfg->tile < t12_variant_count() ? cfg->tile : 0;
+        t12_variant(h->tile, &h->tx, &h->ty, &st_);
+    } else if (h->fused) {
         h->tile = cfg->tile > 0 && cfg->tile < fused_tile_count() ? cfg->tile : 0;
         fused_tile_shape(h->tile, &h->tx, &h->ty);
-        if (fused_variant_kind(h->tile) == kVariantPersistent) {
+    }
+    if (h->fused) {
+        if (!h->t12 && fused_variant_kind(h->tile) == kVariantPersistent) {
             if (cfg->mode != GPE_REAL_TIME) {
                 free_handle(h);
                 return fail(GPE_ERR_UNSUPPORTED, "gpe_create: the persistent kernel variants advance real time; "
@@ -1004,7 +1045,7 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
             }
             h->persistent = true;
         }
-        if (fused_half_steps(h->tile) == 2) {
+        if (!h->t12 && fused_half_steps(h->tile) == 2) {
             if (cfg->mode != GPE_REAL_TIME) {
                 free_handle(h);
                 return fail(GPE_ERR_UNSUPPORTED, "gpe_create: this kernel variant advances whole real-time steps; "
@@ -1033,7 +1074,8 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
             // fold over all items every step, so it aims for about two items per SM
             // and keeps chunks of at least 8 planes.
             const bool imag = cfg->mode == GPE_IMAGINARY_TIME;
-            const long long target = imag ? 152ll * 2 : 152ll * 8 * 4;
+            // (the TETRA12 kernel runs one CTA per SM: four waves of 152)
+            const long long target = imag ? 152ll * 2 : (h->t12 ? 152ll * 4 : 152ll * 8 * 4);
             const int zmin = imag ? 8 : 2;
             long long maxnz = 1;
             for (auto &in : h->inst) maxnz = std::max<long long>(maxnz, in.nz);
@@ -1119,10 +1161,11 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
         std::vector<CUtensorMap> maps(4 * cfg->num_instances);
         for (int i = 0; i < cfg->num_instances; i++)
             for (int f = 0; f < 2; f++) {
-                gpe_status ms = h->two_step ? make_twostep_maps(&maps[4 * i + 2 * f], cfg->precision, h->idev_host[i],
-                                                                h->buf[2 * f], h->buf[2 * f + 1], h->tile)
-                                            : make_halo_map(&maps[4 * i + 2 * f], cfg->precision, h->idev_host[i],
-                                                            h->buf[f], h->tile);
+                gpe_status ms = h->t12 ? make_t12_maps(&maps[4 * i + 2 * f], h->idev_host[i], h->buf[f], h->tx, h->ty)
+                                : h->two_step ? make_twostep_maps(&maps[4 * i + 2 * f], cfg->precision, h->idev_host[i],
+                                                                  h->buf[2 * f], h->buf[2 * f + 1], h->tile)
+                                              : make_halo_map(&maps[4 * i + 2 * f], cfg->precision, h->idev_host[i],
+                                                              h->buf[f], h->tile);
                 if (ms != GPE_OK) {
                     free_handle(h);
                     return ms;
@@ -1131,6 +1174,19 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
         GPE_CREATE_TRY(cudaMalloc(&h->maps, sizeof(CUtensorMap) * maps.size()));
         GPE_CREATE_TRY(cudaMemcpyAsync(h->maps, maps.data(), sizeof(CUtensorMap) * maps.size(),
                                        cudaMemcpyHostToDevice, h->stream));
+        if (h->t12 && cfg->potential == GPE_POTENTIAL_ARRAY) {
+            std::vector<CUtensorMap> vmaps(cfg->num_instances);
+            for (int i = 0; i < cfg->num_instances; i++) {
+                gpe_status ms = make_t12_vmap(&vmaps[i], h->idev_host[i], h->vbase, h->tx, h->ty);
+                if (ms != GPE_OK) {
+                    free_handle(h);
+                    return ms;
+                }
+            }
+            GPE_CREATE_TRY(cudaMalloc(&h->t12_vmaps, sizeof(CUtensorMap) * vmaps.size()));
+            GPE_CREATE_TRY(cudaMemcpyAsync(h->t12_vmaps, vmaps.data(), sizeof(CUtensorMap) * vmaps.size(),
+                                           cudaMemcpyHostToDevice, h->stream));
+        }
         std::vector<CUtensorMap> lo_maps(h->comp ? 2 * cfg->num_instances : 0);
         for (int i = 0; i < int(lo_maps.size()) / 2; i++)
             for (int f = 0; f < 2; f++) {

@@ -647,6 +647,43 @@ gpe_status make_halo_map(void *out_map, int precision, const InstDev &d, void *f
     return GPE_OK;
 }
 
+gpe_status make_t12_maps(void *out_map, const InstDev &d, void *field_arena, int tx, int ty)
+{
+    TensorMapEncode encode = tensor_map_encoder();
+    if (!encode) return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t dims[4] = {(cuuint64_t)d.px, (cuuint64_t)d.py, (cuuint64_t)d.slots, (cuuint64_t)d.nz + 2};
+    const cuuint64_t strides[3] = {(cuuint64_t)d.px * 8, (cuuint64_t)d.plane * 8, (cuuint64_t)d.zstride * 8};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const cuuint32_t boxes[2][4] = {{(cuuint32_t)(tx + 4), (cuuint32_t)(ty + 2), (cuuint32_t)d.slots, 1},
+                                    {(cuuint32_t)tx, (cuuint32_t)ty, (cuuint32_t)d.slots, 1}};
+    void *gaddr = (char *)field_arena + (size_t)d.base * 8;
+    for (int b = 0; b < 2; b++) {
+        CUresult r = encode((CUtensorMap *)out_map + b, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, gaddr, dims, strides,
+                            boxes[b], estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    }
+    return GPE_OK;
+}
+
+gpe_status make_t12_vmap(void *out_map, const InstDev &d, void *vbase_arena, int tx, int ty)
+{
+    TensorMapEncode encode = tensor_map_encoder();
+    if (!encode) return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t dims[4] = {(cuuint64_t)d.px, (cuuint64_t)d.py, (cuuint64_t)d.slots, (cuuint64_t)d.nz + 2};
+    const cuuint64_t strides[3] = {(cuuint64_t)d.px * 4, (cuuint64_t)d.plane * 4, (cuuint64_t)d.zstride * 4};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const cuuint32_t box[4] = {(cuuint32_t)(tx + 4), (cuuint32_t)ty, (cuuint32_t)d.slots, 1};
+    void *gaddr = (char *)vbase_arena + (size_t)d.vbase * 4;
+    CUresult r = encode((CUtensorMap *)out_map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, gaddr, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return fail(GPE_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return GPE_OK;
+}
+
 // The residual map of one field of one instance (GPE_FP32C): 4-D over the
 // padded layout in 16-bit words (x, y, slot, z; rows of px words, px a multiple
 // of 8 so that every row starts on 16 bytes).  The residual of padded column c

@@ -113,6 +113,29 @@ struct FusedLaunch {
     void *out_e, *out_o;  // two-step variants: the other buffer set (src = the set read)
 };
 cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s);
+// The fused TETRA12 half-step (gpe_fused_t12.cu): FP32, real time, one work
+// item per CTA, a TMA ring of the previous field's planes (all 12 slots).
+struct T12Launch {
+    int potential, variant, grid, src, inject_skip_plane;
+    const InstDev *inst;
+    const WorkItem *items;
+    const void *maps;   // CUtensorMap[num_instances][2 fields][prev box, next box]
+    const void *vmaps;  // ARRAY potential: CUtensorMap[num_instances] over L0 + V dt
+    void *next;
+    const void *vpot;   // TRAP: per-axis tables; ARRAY: L0 + V dt per value
+    int *err;
+    int tab[48];        // packed neighbour entries, slot-major
+};
+cudaError_t launch_t12_step(const T12Launch &l, cudaStream_t s);
+int t12_variant_count();
+void t12_variant(int v, int *tx, int *ty, int *stages);
+// Its two 4-D maps of one field of one instance: (x, y, slot, z) over the padded
+// layout; boxes = tile plus a 2-column / 1-row halo, and the interior tile, all
+// 12 slots, one plane.
+gpe_status make_t12_maps(void *out_map, const InstDev &d, void *field_arena, int tx, int ty);
+// The map of one instance's L0 + V dt array (ARRAY potential, 4-byte values):
+// box = the interior tile plus 2 columns either side (16-byte aligned), all slots.
+gpe_status make_t12_vmap(void *out_map, const InstDev &d, void *vbase_arena, int tx, int ty);
 // A whole leapfrog step (both half-steps) per launch: reads set l.src through
 // l.maps ([instance][set][E box, O box]), writes l.out_e / l.out_o.
 cudaError_t launch_twostep(const FusedLaunch &l, cudaStream_t s);
