@@ -147,9 +147,9 @@ typedef struct gpe_config {
     const gpe_instance *instances;
     int32_t graph_steps;    /* steps per captured CUDA graph; 0 = 100, < 0 = no graphs */
     int32_t tile;           /* fused-kernel tile variant; 0 = autotuned/default.
-                             * TETRA12: 0..3 = 32x4 (6 stages), 32x2 (8), 32x6 (5),
-                             * 32x3 (7) block columns (gpe_variant_* describe the
-                             * BCC2 variants)                                     */
+                             * TETRA12: 0..5 = 32x4 (6 stages), 32x2 (8), 32x6 (5),
+                             * 32x3 (7), 32x2 (5), 32x3 (4) block columns
+                             * (gpe_variant_* describe the BCC2 variants)         */
     int32_t zchunk;         /* planes per work item of the fused kernel; 0 = auto  */
     int32_t device;         /* CUDA device ordinal                                 */
     /* TETRA12 and the plain kernel only.  NULL: the update of

@@ -37,7 +37,7 @@ def _fields(st, insts, seed, potential):
 
 
 @pytest.mark.parametrize("potential", [Potential.TRAP, Potential.ARRAY])
-@pytest.mark.parametrize("tile", [0, 1, 2, 3])
+@pytest.mark.parametrize("tile", [0, 1, 2, 3, 4, 5])
 def test_t12_fused_equals_oracle_and_plain(tile, potential):
     insts = _insts(SIZES)
     kw = dict(lattice=Lattice.TETRA12, precision=Precision.FP32, potential=potential, graph_steps=-1)

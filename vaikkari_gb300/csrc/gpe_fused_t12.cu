@@ -133,13 +133,16 @@ __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_
         const bool xin = x < d.nx;
         const float Lw[1] = {float(d.Lc[0])};
         const float L0 = float(d.L0), gdt = float(d.gdt);
-        float vx = 0.f;
-        const float *tz = nullptr, *tyt = nullptr;
+        // trap: Vx + Vy of the thread's column and rows, Vz per plane
+        float vxy[TY];
+        const float *tz = nullptr;
         if (POT == GPE_POTENTIAL_TRAP) {
             const float *txt = a.vpot + d.vbase;
-            tyt = txt + (long long)d.slots * d.nx;
+            const float *tyt = txt + (long long)d.slots * d.nx;
             tz = tyt + (long long)d.slots * d.ny;
-            if (xin) vx = txt[s * d.nx + x];
+            const float vx = xin ? txt[s * d.nx + x] : 0.f;
+#pragma unroll
+            for (int ty = 0; ty < TY; ty++) vxy[ty] = w.y0 + ty < d.ny ? d_add(vx, tyt[s * d.ny + w.y0 + ty]) : 0.f;
         }
         int off[4], dzk[4];  // per neighbour: offset in its plane's box, plane (-1, 0, +1)
 #pragma unroll
@@ -187,7 +190,7 @@ __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_
                     if (POT == GPE_POTENTIAL_ARRAY) {
                         hpsi<float, 1, true>(p, Sg, Lw, L0, Vb[ty * S::BW], gdt, hx, hy, nrm);
                     } else {
-                        const float vdt = d_add(d_add(vx, tyt[s * d.ny + y]), vz);
+                        const float vdt = d_add(vxy[ty], vz);
                         hpsi<float, 1, false>(p, Sg, Lw, L0, vdt, gdt, hx, hy, nrm);
                     }
                     a.next[self] = integrate<float, 0>(n, p, hx, hy);
@@ -200,12 +203,13 @@ __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_
     launch_dependents();
 }
 
-// Variants: tile (TX, TY) and pipeline depth; one CTA per SM (the largest ring,
-// 32 x 6 with 5 stages, takes 230,608 of the 232,448 bytes a CTA may have).
+// Variants: tile (TX, TY) and pipeline depth.  The first four run one CTA per SM
+// (the largest ring, 32 x 6 with 5 stages, takes 230,608 of the 232,448 bytes a
+// CTA may have); the last two fit two CTAs per SM with the trap potential.
 struct T12Variant {
     int tx, ty, stages;
 };
-static const T12Variant kT12Variants[] = {{32, 4, 6}, {32, 2, 8}, {32, 6, 5}, {32, 3, 7}};
+static const T12Variant kT12Variants[] = {{32, 4, 6}, {32, 2, 8}, {32, 6, 5}, {32, 3, 7}, {32, 2, 5}, {32, 3, 4}};
 constexpr int kT12Count = int(sizeof(kT12Variants) / sizeof(kT12Variants[0]));
 
 int t12_variant_count() { return kT12Count; }
@@ -241,6 +245,8 @@ static cudaError_t launch_t12_pot(int variant, const T12Args &a, int grid, cudaS
     case 1: return launch_t12_t<32, 2, POT, 8>(a, grid, s);
     case 2: return launch_t12_t<32, 6, POT, A ? 4 : 5>(a, grid, s);
     case 3: return launch_t12_t<32, 3, POT, 7>(a, grid, s);
+    case 4: return launch_t12_t<32, 2, POT, A ? 4 : 5>(a, grid, s);
+    case 5: return launch_t12_t<32, 3, POT, 4>(a, grid, s);
     default: return launch_t12_t<32, 4, POT, A ? 5 : 6>(a, grid, s);
     }
 }
