@@ -517,7 +517,7 @@ template <int LAT, int POT>
 __device__ __forceinline__ void observables_terms_f32(const InstDev &d, const float2 *__restrict__ f,
                                                       const float *__restrict__ vpot, int s, int x, int y, int z,
                                                       long long self, const long long *__restrict__ off,
-                                                      const FPair (&w)[2], FPair rdt, FPair half_g, FPair (&acc)[4])
+                                                      const FPair (&w)[2], FPair rdt, FPair half_g, FPair2 (&acc)[2])
 {
     using L = Lat<LAT>;
     const float2 pt = f[self];
@@ -539,16 +539,22 @@ __device__ __forceinline__ void observables_terms_f32(const InstDev &d, const fl
         const FPair2 b = fp2_add(fp2_two_sum(h[c], l[c]), {f2_neg(np.hi), f2_neg(np.lo)});
         lap = fp2_add(lap, fp2_mul({make_float2(w[c].hi, w[c].hi), make_float2(w[c].lo, w[c].lo)}, b));
     }
-    const FPair lapx = {lap.hi.x, lap.lo.x}, lapy = {lap.hi.y, lap.lo.y};
     float vdt;
     if (POT == GPE_POTENTIAL_ARRAY) vdt = vpot[self - d.base + d.vbase];
     else vdt = trap_vdt<float>(vpot, d, s, x, y, z);
-    const FPair n2 = fp_add(fp_two_prod(pt.x, pt.x), fp_two_prod(pt.y, pt.y));
-    const FPair kin = fp_scale(fp_add(fp_mul({pt.x, 0.f}, lapx), fp_mul({pt.y, 0.f}, lapy)), -0.5f);
-    acc[0] = fp_add(acc[0], n2);
-    acc[1] = fp_add(acc[1], kin);
-    acc[2] = fp_add(acc[2], fp_mul(fp_mul({vdt, 0.f}, rdt), n2));
-    acc[3] = fp_add(acc[3], fp_mul(half_g, fp_mul(n2, n2)));
+    // The four terms, two at a time: lane pairs (re, im), then (norm, kinetic)
+    // and (potential, interaction) - each lane the scalar pair arithmetic.
+    const FPair2 sq = fp2_two_prod(pt, pt);                          // x^2, y^2
+    const FPair n2 = fp_add({sq.hi.x, sq.lo.x}, {sq.hi.y, sq.lo.y});
+    const FPair2 pl = fp2_mul({pt, zero}, lap);                      // x Lap_x, y Lap_y
+    const FPair kin = fp_scale(fp_add({pl.hi.x, pl.lo.x}, {pl.hi.y, pl.lo.y}), -0.5f);
+    acc[0] = fp2_add(acc[0], {make_float2(n2.hi, kin.hi), make_float2(n2.lo, kin.lo)});
+    // (vdt * rdt, n2 * n2), then (that * n2, half_g * n2^2)
+    const FPair2 m1 = fp2_mul({make_float2(vdt, n2.hi), make_float2(0.f, n2.lo)},
+                              {make_float2(rdt.hi, n2.hi), make_float2(rdt.lo, n2.lo)});
+    const FPair2 m2 = fp2_mul({make_float2(m1.hi.x, half_g.hi), make_float2(m1.lo.x, half_g.lo)},
+                              {make_float2(n2.hi, m1.hi.y), make_float2(n2.lo, m1.lo.y)});
+    acc[1] = fp2_add(acc[1], m2);
 }
 
 // One CTA's share of one instance's sums: values first, first + stride, ...;
@@ -577,7 +583,9 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
         if (!(LAT == GPE_LATTICE_TETRA12 && d.face)) {
             const FPair w[2] = {fp_of(d.w[0]), fp_of(d.w[1])};
             const FPair rdt2 = fp_of(rdt), half_g = fp_of(0.5 * d.g);
-            FPair acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+            // (norm, kinetic) and (potential, interaction) float pairs
+            FPair2 acc[2] = {{make_float2(0.f, 0.f), make_float2(0.f, 0.f)},
+                             {make_float2(0.f, 0.f), make_float2(0.f, 0.f)}};
             for (long long v = first; v < total; v += stride) {
                 int x, y, s, z;
                 digits(v, d.nx, d.ny, L::NS, x, y, s, z);
@@ -585,7 +593,8 @@ __device__ __forceinline__ void observables_body(const InstDev &d, const typenam
                                                 field_index(d, s, x, y, z), nb_off + s * L::NB, w, rdt2, half_g,
                                                 acc);
             }
-            double out[6] = {fp_value(acc[0]), fp_value(acc[1]), fp_value(acc[2]), fp_value(acc[3]), 0.0, 0.0};
+            double out[6] = {fp_value({acc[0].hi.x, acc[0].lo.x}), fp_value({acc[0].hi.y, acc[0].lo.y}),
+                             fp_value({acc[1].hi.x, acc[1].lo.x}), fp_value({acc[1].hi.y, acc[1].lo.y}), 0.0, 0.0};
             cta_tree_store<6>(out, row);
             return;
         }
