@@ -847,7 +847,8 @@ def _windowed_rate(st, verts, steps, sample_clocks, prec, kern, tile, seconds=1.
 
 def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1, lattice=None):
     """BCC2: FP64 fused to the criterion, FP32 fused over the same steps.  TETRA12
-    (ref-mode): the plain kernel, both precisions over a fixed `max_steps`."""
+    (ref-mode): both precisions over a fixed `max_steps`, FP32 on the fused TETRA12
+    kernel (the line's value), FP64 on the plain kernel."""
     from vaikkari_gb300.gpe import Kernel, Lattice, Mode, Precision
     lattice = Lattice.BCC2 if lattice is None else Lattice(lattice)
     ref_mode = lattice == Lattice.TETRA12
@@ -864,7 +865,8 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1, latti
     res = {}
     steps64 = None
     for prec in (Precision.FP64, Precision.FP32):
-        st = _stepper(conds, prec, kern, Mode.IMAGINARY, tile=tile, zchunk=zchunk, lattice=lattice)
+        k_ = Kernel.PLAIN if (ref_mode and prec == Precision.FP64) else (Kernel.FUSED if ref_mode else kern)
+        st = _stepper(conds, prec, k_, Mode.IMAGINARY, tile=tile, zchunk=zchunk, lattice=lattice)
         for i, c in enumerate(conds):
             st.upload(i, c.psi)
         t0 = time.perf_counter()
@@ -890,6 +892,7 @@ def run_config_imaginary(name, conds, tol=1e-9, max_steps=200000, tile=-1, latti
            "rel_l2_fp32_vs_fp64": _rel_l2_phase(r32["fields"], r64["fields"])}
     # throughput of the imaginary-time step (FP32), device time: median of
     # windows of 1000 steps (ten graph replays), clocks sampled over them
+    kern = Kernel.FUSED  # FP32: the fused kernel of either lattice
     st = _stepper(conds, Precision.FP32, kern, Mode.IMAGINARY, tile=tile, zchunk=zchunk, lattice=lattice)
     for i, c in enumerate(conds):
         st.upload(i, c.psi)

@@ -86,9 +86,10 @@ typedef enum gpe_kernel_kind {
     GPE_KERNEL_AUTO = 0,   /* fused where built, plain otherwise                 */
     GPE_KERNEL_PLAIN = 1,  /* table-driven, one value per thread, any lattice    */
     GPE_KERNEL_FUSED = 2   /* shared-memory tiled, z-marching, batched: BCC2 in
-                            * every storage and mode; TETRA12 in GPE_FP32, real
-                            * time, lattice form (the reference's neighbour order,
-                            * results equal the plain kernel's bit for bit)      */
+                            * every storage and mode; TETRA12 in GPE_FP32, lattice
+                            * form (the reference's neighbour order; real-time
+                            * results equal the plain kernel's bit for bit;
+                            * imaginary time fuses the sums into the step)       */
 } gpe_kernel_kind;
 
 typedef enum gpe_potential_kind {

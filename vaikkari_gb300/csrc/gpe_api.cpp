@@ -375,6 +375,7 @@ gpe_status enqueue_step_real(gpe_handle h)
         void *next = field_buf(h, half == 0 ? 1 : 0);
         if (h->t12) {
             T12Launch l{};
+            l.mode = GPE_REAL_TIME;
             l.potential = h->cfg.potential;
             l.variant = h->tile;
             l.grid = h->grid;
@@ -471,6 +472,32 @@ gpe_status enqueue_observables(gpe_handle h, const void *field, int i, double *s
 gpe_status enqueue_step_imag(gpe_handle h, int parity)
 {
     void *prev = h->buf[parity], *next = h->buf[1 - parity];
+    if (h->t12) {
+        T12Launch l{};
+        l.mode = GPE_IMAGINARY_TIME;
+        l.potential = h->cfg.potential;
+        l.variant = h->tile;
+        l.grid = h->grid;
+        l.src = parity;
+        l.inject_skip_plane = h->inject;
+        l.imag = h->imag;
+        l.partials = h->partials;
+        l.counter = h->counter;
+        l.inst_item_begin = h->item_begin_dev;
+        l.num_instances = h->cfg.num_instances;
+        l.tol = h->tol;
+        l.inst = h->idev;
+        l.items = h->items_dev;
+        l.maps = h->maps;
+        l.vmaps = h->t12_vmaps;
+        l.next = next;
+        l.vpot = h->cfg.potential == GPE_POTENTIAL_ARRAY ? h->vbase : h->vpot;
+        l.err = h->err;
+        std::memcpy(l.tab, h->t12_tab, sizeof(l.tab));
+        GPE_CUDA_TRY(launch_t12_step(l, h->stream));
+        h->launches++;
+        return GPE_OK;
+    }
     if (h->fused) {
         FusedLaunch l{};
         l.precision = h->cfg.precision;
@@ -781,9 +808,9 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
     if (cfg->num_instances < 1 || !cfg->instances)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: need at least one instance");
     if (cfg->kernel == GPE_KERNEL_FUSED && cfg->lattice == GPE_LATTICE_TETRA12 &&
-        (cfg->precision != GPE_FP32 || cfg->mode != GPE_REAL_TIME || cfg->faces))
-        return fail(GPE_ERR_UNSUPPORTED, "gpe_create: the fused kernel takes the TETRA12 lattice in GPE_FP32, real "
-                                         "time and the lattice form only (the plain kernel runs the rest)");
+        (cfg->precision != GPE_FP32 || cfg->faces))
+        return fail(GPE_ERR_UNSUPPORTED, "gpe_create: the fused kernel takes the TETRA12 lattice in GPE_FP32 and "
+                                         "the lattice form only (the plain kernel runs the rest)");
     if (cfg->faces) {
         if (cfg->lattice != GPE_LATTICE_TETRA12 || cfg->kernel == GPE_KERNEL_FUSED || cfg->precision == GPE_FP32C)
             return fail(GPE_ERR_UNSUPPORTED, "gpe_create: a face table needs the TETRA12 lattice, the plain kernel "
@@ -826,12 +853,11 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
     h->esize = cfg->precision == GPE_FP64 ? 8 : 4;
     h->comp = cfg->precision == GPE_FP32C;
     h->hsize = h->comp ? 8 : h->esize;
-    // TETRA12: the fused kernel when asked for, and by default in FP32 real time
-    // in the lattice form (the plain kernel runs FP64, imaginary time and faces).
+    // TETRA12: the fused kernel when asked for, and by default in FP32 in the
+    // lattice form (the plain kernel runs FP64 and the face form).
     h->t12 = cfg->lattice == GPE_LATTICE_TETRA12 &&
              (cfg->kernel == GPE_KERNEL_FUSED ||
-              (cfg->kernel == GPE_KERNEL_AUTO && cfg->precision == GPE_FP32 && cfg->mode == GPE_REAL_TIME &&
-               !cfg->faces));
+              (cfg->kernel == GPE_KERNEL_AUTO && cfg->precision == GPE_FP32 && !cfg->faces));
     h->fused = (cfg->lattice == GPE_LATTICE_BCC2 && cfg->kernel != GPE_KERNEL_PLAIN) || h->t12;
     if (h->t12)
         for (int s = 0; s < 12; s++)

@@ -170,87 +170,9 @@ __global__ void __launch_bounds__(TX *TY + 32, MinBlocks<T, MINB>::value) fused_
     }
 
     launch_dependents();  // the next grid may be scheduled; it waits for this one to finish
-    if (MODE == 1) {
-        // Last CTA to finish reduces every instance's rows (fixed order).  The
-        // producer warp's first lane publishes this CTA's row: it has no field
-        // stores in flight, so its fence only waits for the row itself (a fence
-        // in a consumer thread waits for all of that thread's output stores).
-        __shared__ bool last;
-        __syncthreads();
-        if (abort_flag) return;
-        if (warp == NWARPS - 1 && lane == 0) {
-            for (int k = 0; k < 4; k++) a.partials[4ll * it + k] = row_sums[k];
-            __threadfence();
-            last = (atomicAdd(a.counter, 1u) == gridDim.x - 1);
-            if (last) __threadfence();
-        }
-        __syncthreads();
-        if (!last) return;
-        // Each instance's rows are folded by one warp, the instances taken
-        // round-robin by the warps, so a batch folds its instances in parallel.
-        // Lane l takes rows b+l, b+l+32, ... in groups of eight: the group is
-        // added as a fixed pairwise tree (short FP64 dependency chains), the
-        // group sums are accumulated in order with compensation, then a fixed
-        // xor tree combines the lanes.  The order depends only on the
-        // instance's own rows, so an instance gives the same result alone or in
-        // any batch.
-        for (int i = warp; i < a.num_instances; i += NWARPS) {
-            const int b = a.inst_item_begin[2 * i], e = a.inst_item_begin[2 * i + 1];
-            double sk[4] = {0.0, 0.0, 0.0, 0.0}, ck[4] = {0.0, 0.0, 0.0, 0.0};
-            for (int r0 = b; r0 < e; r0 += 8 * 32) {
-                double v[8][4];
-#pragma unroll
-                for (int u = 0; u < 8; u++) {  // the loads first; rows past the end add zero
-                    const int r = r0 + u * 32 + lane;
-                    double2 v01 = make_double2(0.0, 0.0), v23 = make_double2(0.0, 0.0);
-                    if (r < e) {
-                        v01 = __ldcg((const double2 *)(a.partials + 4ll * r));
-                        v23 = __ldcg((const double2 *)(a.partials + 4ll * r + 2));
-                    }
-                    v[u][0] = v01.x;
-                    v[u][1] = v01.y;
-                    v[u][2] = v23.x;
-                    v[u][3] = v23.y;
-                }
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    const double g8 = ((v[0][k] + v[1][k]) + (v[2][k] + v[3][k])) +
-                                      ((v[4][k] + v[5][k]) + (v[6][k] + v[7][k]));
-                    const double yv = g8 - ck[k];
-                    const double t = sk[k] + yv;
-                    ck[k] = (t - sk[k]) - yv;
-                    sk[k] = t;
-                }
-            }
-            for (int off = 16; off > 0; off >>= 1) {
-#pragma unroll
-                for (int k = 0; k < 4; k++) sk[k] += __shfl_xor_sync(0xffffffffu, sk[k], off);
-            }
-            // sk (every lane): |p'|^2, Re(conj(p') dt H p'), |p'|^4, |next|^2 over values.
-            // Lanes 0, 1, 2 form mu, the energy's t1/dt and sigma with one
-            // division in lockstep (FP64 division is long-latency here).
-            const InstDev &di = a.inst[i];
-            ImagScalars &sc = a.imag[i];
-            const double sq = sqrt(di.vol * sk[3]);
-            const double num = (lane == 2) ? 1.0 : sk[1];
-            const double den = (lane == 0) ? di.dt * sk[0] : (lane == 1) ? di.dt : sq;
-            const double q = num / den;
-            if (lane == 0) {
-                const double mu = q;
-                sc.mu_prev = sc.mu;
-                sc.mu = mu;
-                sc.dmu = (sc.steps > 0) ? fabs(mu - sc.mu_prev) : INFINITY;
-                if (sc.steps > 0 && sc.conv_step < 0 && sc.dmu < a.tol) sc.conv_step = sc.steps;
-                sc.steps += 1;
-            } else if (lane == 1) {
-                sc.norm_in = di.vol * sk[0];
-                sc.energy = di.vol * (q - 0.5 * di.g * sk[2]);
-            } else if (lane == 2) {
-                sc.sigma = q;
-            }
-        }
-        if (tid == 0) *a.counter = 0u;
-    }
+    if (MODE == 1)
+        imag_publish_and_fold<NWARPS>(it, row_sums, abort_flag, NWARPS - 1, a.partials, a.counter,
+                                      a.inst_item_begin, a.num_instances, a.inst, a.imag, a.tol);
 }
 
 // ---- Both half-steps of a leapfrog step in one pass --------------------------

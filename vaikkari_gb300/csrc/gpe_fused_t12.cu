@@ -49,6 +49,12 @@ int t12_smem_bytes()
 
 struct T12Args {
     const InstDev *__restrict__ inst;
+    ImagScalars *imag;        // imaginary time: per-instance scalars (sigma in, sums folded out)
+    double *partials;         // imaginary time: 4 sums per work item
+    unsigned int *counter;    // imaginary time: CTAs done
+    const int *inst_item_begin;
+    int num_instances;
+    double tol;
     const WorkItem *__restrict__ items;
     const CUtensorMap *maps;  // [instance][field][prev box, next box]
     const CUtensorMap *vmaps; // ARRAY potential: [instance] (L0 + V dt, next-tile box)
@@ -60,19 +66,22 @@ struct T12Args {
     int tab[48];              // packed neighbour entries, slot-major, the reference's order
 };
 
-template <int TX, int TY, int POT, int STAGES>
+template <int TX, int TY, int MODE, int POT, int STAGES>
 __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_kernel(const T12Args a)
 {
     static_assert(TX == 32, "one lane per column of the tile");
     static_assert(STAGES >= 4, "three resident planes and one in flight");
     using S = T12Shape<TX, TY, POT>;
+    constexpr bool REAL = MODE == 0;  // MODE 1: imaginary time (psi' = sigma psi - dt H sigma psi)
+    constexpr int NWARPS = S::NTHREADS / 32;
     extern __shared__ unsigned char dyn_smem[];
     const uint32_t raw = smem_u32(dyn_smem);
     const uint32_t base = (raw + 127u) & ~127u;
     unsigned char *const gbase = dyn_smem + (base - raw);
     const uint32_t full = base + STAGES * S::STAGE_BYTES;
     const uint32_t empty = full + 8 * STAGES;
-    __shared__ int abort_flag;
+    __shared__ volatile int abort_flag;
+    __shared__ double row_sums[4];  // imaginary time: this work item's four sums
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
@@ -113,10 +122,11 @@ __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_
                 }
                 if (a.inject_skip_plane == k && blockIdx.x == 0) break;  // test hook: withhold this plane
                 const bool with_next = k >= 2;
-                mbar_arrive_expect_tx(full + 8 * st, S::PREV_BYTES + (with_next ? S::NEXT_BYTES + S::V_BYTES : 0));
+                mbar_arrive_expect_tx(full + 8 * st,
+                                      S::PREV_BYTES + (with_next ? (REAL ? S::NEXT_BYTES : 0) + S::V_BYTES : 0));
                 // padded coordinates: x0-2 -> x0-2+kPadX, y0-1 -> y0, plane q -> q+1
                 tma_load_4d(base + st * S::STAGE_BYTES, prevmap, w.x0 - 2 + kPadX, w.y0, 0, w.z0 + k, full + 8 * st);
-                if (with_next)  // next field, interior tile of plane q-1
+                if (REAL && with_next)  // next field, interior tile of plane q-1
                     tma_load_4d(base + st * S::STAGE_BYTES + S::NEXT_OFF, nextmap, w.x0 + kPadX, w.y0 + 1, 0,
                                 w.z0 + k - 1, full + 8 * st);
                 if (POT == GPE_POTENTIAL_ARRAY && with_next)  // and its L0 + V dt
@@ -127,6 +137,7 @@ __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_
             if (abort_flag) drain_ring<STAGES>(issued, full);
         }
     } else {
+        Acc<float> acc[4];  // imaginary time: |p|^2, Re(conj(p) h), |p|^4, |next|^2
         // ---- consumer warp: slot s, columns x0 .. x0+31 --------------------------
         const int s = warp;
         const int x = w.x0 + lane;
@@ -153,6 +164,7 @@ __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_
             dzk[k] = dz;
         }
         const int selfoff = s * S::PREV_SLOT + S::BW + lane + 2;
+        const float sig = (MODE == 1) ? float(a.imag[w.inst].sigma) : 1.f;
         for (int k = 0; k < nplanes; k++) {
             const int st = k % STAGES;
             const bool got = mbar_wait_bounded(full + 8 * st, (k / STAGES) & 1);
@@ -178,12 +190,13 @@ __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_
             for (int ty = 0; ty < TY; ty++) {
                 const int y = w.y0 + ty;
                 const int r = ty * S::BW;
+                auto rd = [&](float2 v) { return MODE == 1 ? c_scale<float>(sig, v) : v; };
                 float2 Sg[1];
-                Sg[0] = Q[0][r];
+                Sg[0] = rd(Q[0][r]);
 #pragma unroll
-                for (int kk = 1; kk < 4; kk++) Sg[0] = c_add<float>(Sg[0], Q[kk][r]);
-                const float2 p = P0[selfoff + r];
-                const float2 n = N[ty * TX];
+                for (int kk = 1; kk < 4; kk++) Sg[0] = c_add<float>(Sg[0], rd(Q[kk][r]));
+                const float2 p = rd(P0[selfoff + r]);
+                const float2 n = REAL ? N[ty * TX] : make_float2(0.f, 0.f);
                 if (xin && y < d.ny) {
                     const long long self = field_index(d, s, x, y, z);
                     float hx, hy, nrm;
@@ -193,14 +206,39 @@ __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_
                         const float vdt = d_add(vxy[ty], vz);
                         hpsi<float, 1, false>(p, Sg, Lw, L0, vdt, gdt, hx, hy, nrm);
                     }
-                    a.next[self] = integrate<float, 0>(n, p, hx, hy);
+                    const float2 o = integrate<float, MODE>(n, p, hx, hy);
+                    a.next[self] = o;
+                    if (MODE == 1) {
+                        acc[0].add(nrm);
+                        acc[1].add(d_fma(p.x, hx, d_mul(p.y, hy)));
+                        acc[2].add(d_mul(nrm, nrm));
+                        acc[3].add(d_fma(o.x, o.x, d_mul(o.y, o.y)));
+                    }
                 }
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(empty + 8 * ((k - 2) % STAGES));  // plane z-1 is no longer read
         }
+        if (MODE == 1) {
+            double v[4] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value()};
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], off);
+            __shared__ double red[S::NS][4];
+            if (lane == 0)
+                for (int k = 0; k < 4; k++) red[warp][k] = v[k];
+            asm volatile("bar.sync 1, %0;" ::"r"(S::NCONS) : "memory");  // consumer warps only
+            if (tid < 4) {
+                double t = 0.0;
+                for (int wi = 0; wi < S::NS; wi++) t += red[wi][tid];
+                row_sums[tid] = t;
+            }
+        }
     }
     launch_dependents();
+    if (MODE == 1)
+        imag_publish_and_fold<NWARPS>(blockIdx.x, row_sums, abort_flag, S::NS, a.partials, a.counter,
+                                      a.inst_item_begin, a.num_instances, a.inst, a.imag, a.tol);
 }
 
 // Variants: tile (TX, TY) and pipeline depth.  The first four run one CTA per SM
@@ -221,33 +259,38 @@ void t12_variant(int v, int *tx, int *ty, int *stages)
     *stages = kT12Variants[v].stages;
 }
 
-template <int TX, int TY, int POT, int STAGES>
+template <int TX, int TY, int MODE, int POT, int STAGES>
 static cudaError_t launch_t12_t(const T12Args &a, int grid, cudaStream_t s)
 {
     const int bytes = t12_smem_bytes<TX, TY, POT, STAGES>();
-    auto kern = fused_t12_kernel<TX, TY, POT, STAGES>;
+    auto kern = fused_t12_kernel<TX, TY, MODE, POT, STAGES>;
     static int allowed = 48 * 1024;
     if (bytes > allowed) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) return e;
         allowed = bytes;
     }
-    return launch_pdl(kern, grid, T12Shape<TX, TY, POT>::NTHREADS, bytes, s, a);
+    // Real time: programmatic dependent launch.  Imaginary time ends every grid
+    // with the fold in its last CTA; an early-scheduled next grid there would
+    // only hold SM slots, so it launches plainly.
+    if (MODE == 0) return launch_pdl(kern, grid, T12Shape<TX, TY, POT>::NTHREADS, bytes, s, a);
+    kern<<<grid, T12Shape<TX, TY, POT>::NTHREADS, bytes, s>>>(a);
+    return cudaGetLastError();
 }
 
 // With an ARRAY potential each stage also holds the L0 + V dt box, so the
 // deeper variants give up a stage to stay within the CTA's shared memory.
-template <int POT>
+template <int MODE, int POT>
 static cudaError_t launch_t12_pot(int variant, const T12Args &a, int grid, cudaStream_t s)
 {
     constexpr bool A = POT == GPE_POTENTIAL_ARRAY;
     switch (variant) {  // must list kT12Variants in order
-    case 1: return launch_t12_t<32, 2, POT, 8>(a, grid, s);
-    case 2: return launch_t12_t<32, 6, POT, A ? 4 : 5>(a, grid, s);
-    case 3: return launch_t12_t<32, 3, POT, 7>(a, grid, s);
-    case 4: return launch_t12_t<32, 2, POT, A ? 4 : 5>(a, grid, s);
-    case 5: return launch_t12_t<32, 3, POT, 4>(a, grid, s);
-    default: return launch_t12_t<32, 4, POT, A ? 5 : 6>(a, grid, s);
+    case 1: return launch_t12_t<32, 2, MODE, POT, 8>(a, grid, s);
+    case 2: return launch_t12_t<32, 6, MODE, POT, A ? 4 : 5>(a, grid, s);
+    case 3: return launch_t12_t<32, 3, MODE, POT, 7>(a, grid, s);
+    case 4: return launch_t12_t<32, 2, MODE, POT, A ? 4 : 5>(a, grid, s);
+    case 5: return launch_t12_t<32, 3, MODE, POT, 4>(a, grid, s);
+    default: return launch_t12_t<32, 4, MODE, POT, A ? 5 : 6>(a, grid, s);
     }
 }
 
@@ -255,6 +298,12 @@ cudaError_t launch_t12_step(const T12Launch &l, cudaStream_t s)
 {
     T12Args a;
     a.inst = l.inst;
+    a.imag = l.imag;
+    a.partials = l.partials;
+    a.counter = l.counter;
+    a.inst_item_begin = l.inst_item_begin;
+    a.num_instances = l.num_instances;
+    a.tol = l.tol;
     a.items = l.items;
     a.maps = (const CUtensorMap *)l.maps;
     a.vmaps = (const CUtensorMap *)l.vmaps;
@@ -264,8 +313,13 @@ cudaError_t launch_t12_step(const T12Launch &l, cudaStream_t s)
     a.err = l.err;
     a.inject_skip_plane = l.inject_skip_plane;
     for (int i = 0; i < 48; i++) a.tab[i] = l.tab[i];
-    if (l.potential == GPE_POTENTIAL_ARRAY) return launch_t12_pot<GPE_POTENTIAL_ARRAY>(l.variant, a, l.grid, s);
-    return launch_t12_pot<GPE_POTENTIAL_TRAP>(l.variant, a, l.grid, s);
+    const bool arr = l.potential == GPE_POTENTIAL_ARRAY;
+    if (l.mode == GPE_IMAGINARY_TIME) {
+        if (arr) return launch_t12_pot<1, GPE_POTENTIAL_ARRAY>(l.variant, a, l.grid, s);
+        return launch_t12_pot<1, GPE_POTENTIAL_TRAP>(l.variant, a, l.grid, s);
+    }
+    if (arr) return launch_t12_pot<0, GPE_POTENTIAL_ARRAY>(l.variant, a, l.grid, s);
+    return launch_t12_pot<0, GPE_POTENTIAL_TRAP>(l.variant, a, l.grid, s);
 }
 
 }  // namespace gpe

@@ -113,10 +113,16 @@ struct FusedLaunch {
     void *out_e, *out_o;  // two-step variants: the other buffer set (src = the set read)
 };
 cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s);
-// The fused TETRA12 half-step (gpe_fused_t12.cu): FP32, real time, one work
+// The fused TETRA12 half-step (gpe_fused_t12.cu): FP32, real or imaginary time, one work
 // item per CTA, a TMA ring of the previous field's planes (all 12 slots).
 struct T12Launch {
-    int potential, variant, grid, src, inject_skip_plane;
+    int mode, potential, variant, grid, src, inject_skip_plane;
+    ImagScalars *imag;            // imaginary time: per-instance scalars
+    double *partials;             // imaginary time: 4 sums per work item
+    unsigned int *counter;        // imaginary time: CTAs done
+    const int *inst_item_begin;   // per instance: [begin, end) item rows
+    int num_instances;
+    double tol;
     const InstDev *inst;
     const WorkItem *items;
     const void *maps;   // CUtensorMap[num_instances][2 fields][prev box, next box]
