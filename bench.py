@@ -1068,7 +1068,8 @@ def run_tetra12(args):
                                  ("fp32", Precision.FP32, None, Kernel.PLAIN),
                                  ("fp32_fused", Precision.FP32, None, Kernel.FUSED),
                                  ("fp64_faces", Precision.FP64, faces, Kernel.PLAIN),
-                                 ("fp32_faces", Precision.FP32, faces, Kernel.PLAIN)):
+                                 ("fp32_faces", Precision.FP32, faces, Kernel.PLAIN),
+                                 ("fp32_faces_fused", Precision.FP32, faces, Kernel.FUSED)):
         st = Stepper([inst], lattice=Lattice.TETRA12, precision=prec, kernel=kern,
                      potential=Potential.ARRAY, graph_steps=100, faces=fc, tile=3 if kern == Kernel.FUSED else 0)
         st.upload(0, e, o, V)
@@ -1082,7 +1083,7 @@ def run_tetra12(args):
                        "lattice": "TETRA12", "kernel": "plain", "potential": "array"},
             "fp32": rates["fp32"],
             "fp32_fused": rates["fp32_fused"],
-            "faces": {"fp64": rates["fp64_faces"], "fp32": rates["fp32_faces"],
+            "faces": {"fp64": rates["fp64_faces"], "fp32": rates["fp32_faces"], "fp32_fused": rates["fp32_faces_fused"],
                       "form": "Hodge (face) form of GPUGrossPitaevskii_BCC_multi.cu:329-397, weights 1.5"},
             "note": "FP64 performs the reference kernel's rounded operations and equals its results bit for "
                     "bit; the per-value constant L0 + V*dt is added once per potential upload, leaving 15 FP64 "

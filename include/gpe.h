@@ -87,9 +87,9 @@ typedef enum gpe_kernel_kind {
     GPE_KERNEL_PLAIN = 1,  /* table-driven, one value per thread, any lattice    */
     GPE_KERNEL_FUSED = 2   /* shared-memory tiled, z-marching, batched: BCC2 in
                             * every storage and mode; TETRA12 in GPE_FP32, lattice
-                            * form (the reference's neighbour order; real-time
-                            * results equal the plain kernel's bit for bit;
-                            * imaginary time fuses the sums into the step)       */
+                            * or face form (real-time results equal the plain
+                            * kernel's bit for bit; imaginary time fuses the sums
+                            * into the step)                                     */
 } gpe_kernel_kind;
 
 typedef enum gpe_potential_kind {
@@ -153,7 +153,7 @@ typedef struct gpe_config {
                              * (gpe_variant_* describe the BCC2 variants)         */
     int32_t zchunk;         /* planes per work item of the fused kernel; 0 = auto  */
     int32_t device;         /* CUDA device ordinal                                 */
-    /* TETRA12 and the plain kernel only.  NULL: the update of
+    /* TETRA12 only (the plain kernel, or the fused one in GPE_FP32).  NULL: the update of
      * GPUGrossPitaevskii_BCC.cu:213, lapfac * sum(psi_f) + (lapfac0 + V + g|psi|^2) psi.
      * Non-NULL: the Hodge (face) form of GPUGrossPitaevskii_BCC_multi.cu:329-397,
      * sum_f h_f (psi_f - psi) + (V + g|psi|^2) psi with h_f = -0.5 hodge_f / bs^2 * dt,

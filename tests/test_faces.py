@@ -83,11 +83,11 @@ def test_face_oracle_equals_lattice_form_to_rounding():
     assert not np.array_equal(e1, e2)   # a different order of operations
 
 
-def _run_faces(prec, potential, dims, steps, table=TABLE):
+def _run_faces(prec, potential, dims, steps, table=TABLE, kernel=Kernel.PLAIN, tile=0):
     T = np.float64 if prec == Precision.FP64 else np.float32
     insts = _insts(dims)
-    st = Stepper(insts, lattice=Lattice.TETRA12, precision=prec, kernel=Kernel.PLAIN, potential=potential,
-                 faces=table)
+    st = Stepper(insts, lattice=Lattice.TETRA12, precision=prec, kernel=kernel, potential=potential,
+                 faces=table, tile=tile)
     want = []
     for i in range(len(insts)):
         shp = st.shape(i)
@@ -114,6 +114,38 @@ def test_faces_bit_exact_oracle(prec, potential):
     for i, ((ge, go), (we, wo)) in enumerate(zip(got, want)):
         np.testing.assert_array_equal(ge, we, err_msg=f"even, instance {i}")
         np.testing.assert_array_equal(go, wo, err_msg=f"odd, instance {i}")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("potential", [Potential.ARRAY, Potential.TRAP])
+@pytest.mark.parametrize("tile", [0, 3])
+def test_fused_face_form_bit_exact_oracle(tile, potential):
+    """FP32: the fused TETRA12 kernel in the face form (faces and weights from the
+    handle, one fma per face) equals the oracle's face form bit for bit."""
+    got, want = _run_faces(Precision.FP32, potential, [(1, 1, 1), (7, 5, 3), (33, 9, 6), (40, 4, 9)], 5,
+                           kernel=Kernel.FUSED, tile=tile)
+    for i, ((ge, go), (we, wo)) in enumerate(zip(got, want)):
+        np.testing.assert_array_equal(ge, we, err_msg=f"even, instance {i}")
+        np.testing.assert_array_equal(go, wo, err_msg=f"odd, instance {i}")
+
+
+@pytest.mark.gpu
+def test_fused_face_form_imaginary_time_follows_plain():
+    """FP32 imaginary time in the face form: the fused kernel (sums fused into the
+    step) and the plain kernel end within FP32 rounding of each other."""
+    insts = [Instance(10, 10, 10, 0.5, 2e-3, 30.0, origin=(-7.1, -7.1, -7.1), trap=(1.0, 1.0, 1.0))]
+    rng = np.random.default_rng(19)
+    psi0 = np.exp(1j * rng.uniform(0, 2 * np.pi, size=(10, 10, 10, 12)))
+    out = []
+    for kern in (Kernel.FUSED, Kernel.PLAIN):
+        st = Stepper(insts, lattice=Lattice.TETRA12, precision=Precision.FP32, kernel=kern, mode=Mode.IMAGINARY,
+                     potential=Potential.TRAP, faces=TABLE, graph_steps=20)
+        st.upload(0, psi0)
+        steps, conv, mu = st.imaginary_time(120, 0.0)
+        out.append((mu[0], st.download(0, odd=False)[0]))
+        st.close()
+    assert out[0][0] == pytest.approx(out[1][0], rel=1e-6)
+    assert rel_l2(out[0][1], out[1][1]) < 2e-6
 
 
 @pytest.mark.gpu

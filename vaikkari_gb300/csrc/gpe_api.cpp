@@ -389,6 +389,7 @@ gpe_status enqueue_step_real(gpe_handle h)
             l.vpot = h->cfg.potential == GPE_POTENTIAL_ARRAY ? h->vbase : h->vpot;
             l.err = h->err;
             std::memcpy(l.tab, h->t12_tab, sizeof(l.tab));
+            l.face = h->faces ? 1 : 0;
             GPE_CUDA_TRY(launch_t12_step(l, h->stream));
             h->launches++;
         } else if (h->fused) {
@@ -494,6 +495,7 @@ gpe_status enqueue_step_imag(gpe_handle h, int parity)
         l.vpot = h->cfg.potential == GPE_POTENTIAL_ARRAY ? h->vbase : h->vpot;
         l.err = h->err;
         std::memcpy(l.tab, h->t12_tab, sizeof(l.tab));
+        l.face = h->faces ? 1 : 0;
         GPE_CUDA_TRY(launch_t12_step(l, h->stream));
         h->launches++;
         return GPE_OK;
@@ -807,14 +809,13 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: unknown kernel kind");
     if (cfg->num_instances < 1 || !cfg->instances)
         return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_create: need at least one instance");
-    if (cfg->kernel == GPE_KERNEL_FUSED && cfg->lattice == GPE_LATTICE_TETRA12 &&
-        (cfg->precision != GPE_FP32 || cfg->faces))
-        return fail(GPE_ERR_UNSUPPORTED, "gpe_create: the fused kernel takes the TETRA12 lattice in GPE_FP32 and "
-                                         "the lattice form only (the plain kernel runs the rest)");
+    if (cfg->kernel == GPE_KERNEL_FUSED && cfg->lattice == GPE_LATTICE_TETRA12 && cfg->precision != GPE_FP32)
+        return fail(GPE_ERR_UNSUPPORTED, "gpe_create: the fused kernel takes the TETRA12 lattice in GPE_FP32 only "
+                                         "(the plain kernel runs FP64)");
     if (cfg->faces) {
-        if (cfg->lattice != GPE_LATTICE_TETRA12 || cfg->kernel == GPE_KERNEL_FUSED || cfg->precision == GPE_FP32C)
-            return fail(GPE_ERR_UNSUPPORTED, "gpe_create: a face table needs the TETRA12 lattice, the plain kernel "
-                                             "and GPE_FP64 or GPE_FP32");
+        if (cfg->lattice != GPE_LATTICE_TETRA12 || cfg->precision == GPE_FP32C)
+            return fail(GPE_ERR_UNSUPPORTED, "gpe_create: a face table needs the TETRA12 lattice and GPE_FP64 or "
+                                             "GPE_FP32");
         gpe_status fst = check_face_table(*cfg->faces);
         if (fst != GPE_OK) return fst;
     }
@@ -853,11 +854,10 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
     h->esize = cfg->precision == GPE_FP64 ? 8 : 4;
     h->comp = cfg->precision == GPE_FP32C;
     h->hsize = h->comp ? 8 : h->esize;
-    // TETRA12: the fused kernel when asked for, and by default in FP32 in the
-    // lattice form (the plain kernel runs FP64 and the face form).
+    // TETRA12: the fused kernel when asked for, and by default in FP32, in either
+    // form (the plain kernel runs FP64).
     h->t12 = cfg->lattice == GPE_LATTICE_TETRA12 &&
-             (cfg->kernel == GPE_KERNEL_FUSED ||
-              (cfg->kernel == GPE_KERNEL_AUTO && cfg->precision == GPE_FP32 && !cfg->faces));
+             (cfg->kernel == GPE_KERNEL_FUSED || (cfg->kernel == GPE_KERNEL_AUTO && cfg->precision == GPE_FP32));
     h->fused = (cfg->lattice == GPE_LATTICE_BCC2 && cfg->kernel != GPE_KERNEL_PLAIN) || h->t12;
     if (h->t12)
         for (int s = 0; s < 12; s++)
@@ -1203,7 +1203,9 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
         if (h->t12 && cfg->potential == GPE_POTENTIAL_ARRAY) {
             std::vector<CUtensorMap> vmaps(cfg->num_instances);
             for (int i = 0; i < cfg->num_instances; i++) {
-                gpe_status ms = make_t12_vmap(&vmaps[i], h->idev_host[i], h->vbase, h->tx, h->ty);
+                // the face form adds V dt itself; the lattice form reads L0 + V dt
+                gpe_status ms = make_t12_vmap(&vmaps[i], h->idev_host[i], h->faces ? h->vpot : h->vbase, h->tx,
+                                              h->ty);
                 if (ms != GPE_OK) {
                     free_handle(h);
                     return ms;

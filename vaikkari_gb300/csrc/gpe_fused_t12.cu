@@ -66,7 +66,7 @@ struct T12Args {
     int tab[48];              // packed neighbour entries, slot-major, the reference's order
 };
 
-template <int TX, int TY, int MODE, int POT, int STAGES>
+template <int TX, int TY, int MODE, int POT, int STAGES, bool FACE>
 __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_kernel(const T12Args a)
 {
     static_assert(TX == 32, "one lane per column of the tile");
@@ -156,9 +156,11 @@ __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_
             for (int ty = 0; ty < TY; ty++) vxy[ty] = w.y0 + ty < d.ny ? d_add(vx, tyt[s * d.ny + w.y0 + ty]) : 0.f;
         }
         int off[4], dzk[4];  // per neighbour: offset in its plane's box, plane (-1, 0, +1)
+        float hk[4];         // FACE: the faces' weights -0.5 hodge / bs^2 * dt, summation order
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            const int e = a.tab[s * 4 + k];
+            const int e = FACE ? d.fe[4 * s + k] : a.tab[s * 4 + k];
+            hk[k] = FACE ? d.hf32[4 * s + k] : 0.f;
             const int dx = (e & 3) - 1, dy = ((e >> 2) & 3) - 1, dz = ((e >> 4) & 3) - 1, sl = (e >> 6) & 15;
             off[k] = sl * S::PREV_SLOT + (1 + dy) * S::BW + (lane + 2 + dx);
             dzk[k] = dz;
@@ -191,16 +193,34 @@ __global__ void __launch_bounds__(T12Shape<TX, TY, POT>::NTHREADS, 1) fused_t12_
                 const int y = w.y0 + ty;
                 const int r = ty * S::BW;
                 auto rd = [&](float2 v) { return MODE == 1 ? c_scale<float>(sig, v) : v; };
-                float2 Sg[1];
-                Sg[0] = rd(Q[0][r]);
-#pragma unroll
-                for (int kk = 1; kk < 4; kk++) Sg[0] = c_add<float>(Sg[0], rd(Q[kk][r]));
                 const float2 p = rd(P0[selfoff + r]);
+                float2 Sg[1];
+                float fx = 0.f, fy = 0.f;  // FACE: sum of h_k (psi_k - psi), one fma per face
+                if (FACE) {
+#pragma unroll
+                    for (int kk = 0; kk < 4; kk++) {
+                        const float2 v = rd(Q[kk][r]);
+                        fx = d_fma(hk[kk], d_sub(v.x, p.x), fx);
+                        fy = d_fma(hk[kk], d_sub(v.y, p.y), fy);
+                    }
+                } else {
+                    Sg[0] = rd(Q[0][r]);
+#pragma unroll
+                    for (int kk = 1; kk < 4; kk++) Sg[0] = c_add<float>(Sg[0], rd(Q[kk][r]));
+                }
                 const float2 n = REAL ? N[ty * TX] : make_float2(0.f, 0.f);
                 if (xin && y < d.ny) {
                     const long long self = field_index(d, s, x, y, z);
                     float hx, hy, nrm;
-                    if (POT == GPE_POTENTIAL_ARRAY) {
+                    if (FACE) {
+                        // the face form's update (the multi-GPU program's roundings):
+                        // c = fma(g dt, fma(x, x, y y), V dt), h = fma(c, psi, sum)
+                        const float vdt = POT == GPE_POTENTIAL_ARRAY ? Vb[ty * S::BW] : d_add(vxy[ty], vz);
+                        nrm = d_fma(p.x, p.x, d_mul(p.y, p.y));
+                        const float c = d_fma(gdt, nrm, vdt);
+                        hx = d_fma(c, p.x, fx);
+                        hy = d_fma(c, p.y, fy);
+                    } else if (POT == GPE_POTENTIAL_ARRAY) {
                         hpsi<float, 1, true>(p, Sg, Lw, L0, Vb[ty * S::BW], gdt, hx, hy, nrm);
                     } else {
                         const float vdt = d_add(vxy[ty], vz);
@@ -259,11 +279,11 @@ void t12_variant(int v, int *tx, int *ty, int *stages)
     *stages = kT12Variants[v].stages;
 }
 
-template <int TX, int TY, int MODE, int POT, int STAGES>
+template <int TX, int TY, int MODE, int POT, int STAGES, bool FACE>
 static cudaError_t launch_t12_t(const T12Args &a, int grid, cudaStream_t s)
 {
     const int bytes = t12_smem_bytes<TX, TY, POT, STAGES>();
-    auto kern = fused_t12_kernel<TX, TY, MODE, POT, STAGES>;
+    auto kern = fused_t12_kernel<TX, TY, MODE, POT, STAGES, FACE>;
     static int allowed = 48 * 1024;
     if (bytes > allowed) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -280,18 +300,25 @@ static cudaError_t launch_t12_t(const T12Args &a, int grid, cudaStream_t s)
 
 // With an ARRAY potential each stage also holds the L0 + V dt box, so the
 // deeper variants give up a stage to stay within the CTA's shared memory.
-template <int MODE, int POT>
+template <int MODE, int POT, bool FACE>
 static cudaError_t launch_t12_pot(int variant, const T12Args &a, int grid, cudaStream_t s)
 {
     constexpr bool A = POT == GPE_POTENTIAL_ARRAY;
     switch (variant) {  // must list kT12Variants in order
-    case 1: return launch_t12_t<32, 2, MODE, POT, 8>(a, grid, s);
-    case 2: return launch_t12_t<32, 6, MODE, POT, A ? 4 : 5>(a, grid, s);
-    case 3: return launch_t12_t<32, 3, MODE, POT, 7>(a, grid, s);
-    case 4: return launch_t12_t<32, 2, MODE, POT, A ? 4 : 5>(a, grid, s);
-    case 5: return launch_t12_t<32, 3, MODE, POT, 4>(a, grid, s);
-    default: return launch_t12_t<32, 4, MODE, POT, A ? 5 : 6>(a, grid, s);
+    case 1: return launch_t12_t<32, 2, MODE, POT, 8, FACE>(a, grid, s);
+    case 2: return launch_t12_t<32, 6, MODE, POT, A ? 4 : 5, FACE>(a, grid, s);
+    case 3: return launch_t12_t<32, 3, MODE, POT, 7, FACE>(a, grid, s);
+    case 4: return launch_t12_t<32, 2, MODE, POT, A ? 4 : 5, FACE>(a, grid, s);
+    case 5: return launch_t12_t<32, 3, MODE, POT, 4, FACE>(a, grid, s);
+    default: return launch_t12_t<32, 4, MODE, POT, A ? 5 : 6, FACE>(a, grid, s);
     }
+}
+
+template <int MODE, int POT>
+static cudaError_t launch_t12_form(bool face, int variant, const T12Args &a, int grid, cudaStream_t s)
+{
+    if (face) return launch_t12_pot<MODE, POT, true>(variant, a, grid, s);
+    return launch_t12_pot<MODE, POT, false>(variant, a, grid, s);
 }
 
 cudaError_t launch_t12_step(const T12Launch &l, cudaStream_t s)
@@ -315,11 +342,11 @@ cudaError_t launch_t12_step(const T12Launch &l, cudaStream_t s)
     for (int i = 0; i < 48; i++) a.tab[i] = l.tab[i];
     const bool arr = l.potential == GPE_POTENTIAL_ARRAY;
     if (l.mode == GPE_IMAGINARY_TIME) {
-        if (arr) return launch_t12_pot<1, GPE_POTENTIAL_ARRAY>(l.variant, a, l.grid, s);
-        return launch_t12_pot<1, GPE_POTENTIAL_TRAP>(l.variant, a, l.grid, s);
+        if (arr) return launch_t12_form<1, GPE_POTENTIAL_ARRAY>(l.face, l.variant, a, l.grid, s);
+        return launch_t12_form<1, GPE_POTENTIAL_TRAP>(l.face, l.variant, a, l.grid, s);
     }
-    if (arr) return launch_t12_pot<0, GPE_POTENTIAL_ARRAY>(l.variant, a, l.grid, s);
-    return launch_t12_pot<0, GPE_POTENTIAL_TRAP>(l.variant, a, l.grid, s);
+    if (arr) return launch_t12_form<0, GPE_POTENTIAL_ARRAY>(l.face, l.variant, a, l.grid, s);
+    return launch_t12_form<0, GPE_POTENTIAL_TRAP>(l.face, l.variant, a, l.grid, s);
 }
 
 }  // namespace gpe

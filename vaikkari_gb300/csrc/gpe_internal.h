@@ -117,6 +117,7 @@ cudaError_t launch_fused_step(const FusedLaunch &l, cudaStream_t s);
 // item per CTA, a TMA ring of the previous field's planes (all 12 slots).
 struct T12Launch {
     int mode, potential, variant, grid, src, inject_skip_plane;
+    int face;                     // the face (Hodge) form: faces and weights from InstDev
     ImagScalars *imag;            // imaginary time: per-instance scalars
     double *partials;             // imaginary time: 4 sums per work item
     unsigned int *counter;        // imaginary time: CTAs done
@@ -128,7 +129,7 @@ struct T12Launch {
     const void *maps;   // CUtensorMap[num_instances][2 fields][prev box, next box]
     const void *vmaps;  // ARRAY potential: CUtensorMap[num_instances] over L0 + V dt
     void *next;
-    const void *vpot;   // TRAP: per-axis tables; ARRAY: L0 + V dt per value
+    const void *vpot;   // TRAP: per-axis tables; ARRAY: L0 + V dt per value (face form: V dt)
     int *err;
     int tab[48];        // packed neighbour entries, slot-major
 };
