@@ -1,7 +1,11 @@
 // gpe_fused_t12.cu - the fused half-step for the TETRA12 lattice (the
-// reference's own discretisation: 12 values per block, 4 neighbours each), FP32,
-// real time: the same update as the plain kernel (GPUGrossPitaevskii_BCC.cu:
-// 176-216 with the reference's neighbour order), fed by a TMA ring of planes.
+// reference's own discretisation: 12 values per block, 4 neighbours each) in
+// FP32: the same update as the plain kernel, fed by a TMA ring of planes.  The
+// lattice form is the reference's update (GPUGrossPitaevskii_BCC.cu:176-216, its
+// neighbour order); the face form is its multi-GPU program's Hodge form
+// (GPUGrossPitaevskii_BCC_multi.cu:329-397, faces and weights from the handle).
+// Real time (MODE 0) or imaginary time (MODE 1: the previous field scaled by
+// sigma as it is read, the item's sums folded at the end of the grid).
 //
 // One CTA runs one work item (instance, TX x TY tile of block columns, z-range).
 // The producer lane loads, per plane q = z0-1 .. z1, the previous field's box of
@@ -12,8 +16,8 @@
 // STAGES - 3.  Consumer warp w handles slot w for the tile's 32 columns, row
 // after row, so every table lookup is uniform across the warp; the sums follow
 // the table order exactly as the plain kernel's do, so the two kernels' results
-// are the same bit for bit.  Every mbarrier wait is bounded (about a second);
-// a timeout sets the launch's error word and the CTA returns.
+// are the same bit for bit in real time.  Every mbarrier wait is bounded (about
+// a second); a timeout sets the launch's error word and the CTA returns.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
