@@ -234,6 +234,25 @@ gpe_status gpe_synchronize(gpe_handle h);
  * out has num_instances entries.  Returns GPE_ERR_NOT_FINITE if any is NaN/Inf. */
 gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out);
 
+/* One round trip of every instance: upload both fields, advance `steps` steps
+ * (as gpe_step), take the observables of field 0 (as gpe_observables_get) and
+ * download both fields, returning when the outputs are written.  The fields and
+ * observables equal those of gpe_upload_many + gpe_step + gpe_observables_get +
+ * gpe_download_many.  Arrays hold num_instances pointers indexed by instance, in
+ * the host element type (gpe_set_host_precision); odd_in may be NULL in
+ * imaginary time; even_out, odd_out, obs and any output entry may be NULL (not
+ * downloaded).  An output buffer may be any instance's input buffer.
+ * In real time with the fused half-step kernels (no slabs) the instances go in up
+ * to four groups of about equal size, contiguous in the work-item order: the
+ * copy engines move group g+1 up and group g-1 down while the SMs step group g,
+ * and the last group's download runs beside the observables.  Overlap needs
+ * page-locked host buffers; a pageable one makes its copy wait for the host.
+ * Replaces the reference's upload (cudaMemcpy3D, GPUGrossPitaevskii_BCC.cu:
+ * 370-391), its step loop (475-481) and its download (484), which run one after
+ * another. */
+gpe_status gpe_round_trip(gpe_handle h, const void *const *even_in, const void *const *odd_in, int64_t steps,
+                          void *const *even_out, void *const *odd_out, gpe_observables *obs);
+
 /* Imaginary time until |mu_k - mu_{k-1}| < tol for every instance or max_steps.
  * Steps run in graph-sized chunks of G steps (gpe_config.graph_steps, 100 by
  * default).  GPE_FP64: mu comes from the reductions fused into every step and

@@ -69,7 +69,12 @@ struct GraphKey {
     long long steps;
     int parity;
     double tol;
-    bool operator<(const GraphKey &o) const { return std::tie(steps, parity, tol) < std::tie(o.steps, o.parity, o.tol); }
+    int run_first, run_count;  // the work items the graph's launches cover
+    bool operator<(const GraphKey &o) const
+    {
+        return std::tie(steps, parity, tol, run_first, run_count) <
+               std::tie(o.steps, o.parity, o.tol, o.run_first, o.run_count);
+    }
 };
 
 struct gpe_handle_ {
@@ -103,6 +108,9 @@ struct gpe_handle_ {
     WorkItem *items_dev = nullptr;
     int *item_begin_dev = nullptr;
     int grid = 0;
+    std::vector<int> item_order;               // instances in work-item order (decreasing size)
+    std::vector<int> item_first, item_count;   // per instance: its first work item and how many
+    int run_first = 0, run_count = 0;          // items a real-time half-step launch covers (count 0: all)
     ImagScalars *imag = nullptr;
     double *partials = nullptr;       // fused imaginary-time rows
     unsigned int *counter = nullptr;
@@ -121,6 +129,7 @@ struct gpe_handle_ {
     void *batch_staging = nullptr;  // gpe_upload_many / gpe_download_many: one slot per transfer
     size_t batch_bytes = 0;
     cudaStream_t copy_stream = nullptr;     // their host<->device copies, beside the conversions
+    cudaStream_t down_stream = nullptr;     // gpe_round_trip: device->host copies beside the uploads
     std::vector<cudaEvent_t> xfer_events;   // one per transfer slot
     XferSeg *xfer_segs = nullptr;           // batched in-place transfers: the launch's segments
     size_t xfer_segs_cap = 0;
@@ -369,6 +378,9 @@ gpe_status enqueue_step_real(gpe_handle h)
         h->parity = 1 - h->parity;
         return GPE_OK;
     }
+    // the fused kernels' work items: all, or the run a round trip steps
+    const int run_first = h->run_count > 0 ? h->run_first : 0;
+    const int run_items = h->run_count > 0 ? h->run_count : h->grid;
     // odd <- even, then even <- odd (GPUGrossPitaevskii_BCC.cu:475-481)
     for (int half = 0; half < 2; half++) {
         void *prev = field_buf(h, half == 0 ? 0 : 1);
@@ -378,11 +390,11 @@ gpe_status enqueue_step_real(gpe_handle h)
             l.mode = GPE_REAL_TIME;
             l.potential = h->cfg.potential;
             l.variant = h->tile;
-            l.grid = h->grid;
+            l.grid = run_items;
             l.src = half == 0 ? 0 : 1;
             l.inject_skip_plane = h->inject;
             l.inst = h->idev;
-            l.items = h->items_dev;
+            l.items = h->items_dev + run_first;
             l.maps = h->maps;
             l.vmaps = h->t12_vmaps;
             l.next = next;
@@ -399,9 +411,9 @@ gpe_status enqueue_step_real(gpe_handle h)
             l.potential = h->cfg.potential;
             l.tile = h->tile;
             l.inst = h->idev;
-            l.items = h->items_dev;
-            l.num_items = int(h->items.size());
-            l.grid = h->grid;
+            l.items = h->items_dev + run_first;
+            l.num_items = run_items;
+            l.grid = run_items;
             l.prev = prev;
             l.next = next;
             l.vpot = h->vpot;
@@ -661,7 +673,7 @@ gpe_status run_steps(gpe_handle h, long long steps)
     if (h->cfg.graph_steps < 0 || steps < G) return enqueue_steps(h, steps);
     long long done = 0;
     while (steps - done >= G) {
-        GraphKey key{G, h->parity, h->tol};
+        GraphKey key{G, h->parity, h->tol, h->run_first, h->run_count};
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             const int parity0 = h->parity;
@@ -732,6 +744,7 @@ void free_handle(gpe_handle h)
     cudaFree(h->xfer_segs);
     cudaFree(h->t12_vmaps);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    if (h->down_stream) cudaStreamDestroy(h->down_stream);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -1141,6 +1154,10 @@ static gpe_status gpe_create_impl(const gpe_config *cfg, gpe_handle *out)
             first[oi] = int(h->items.size());
             h->items.insert(h->items.end(), per[oi].begin(), per[oi].end());
         }
+        h->item_order = order;
+        h->item_first = first;
+        h->item_count.resize(cfg->num_instances);
+        for (int i = 0; i < cfg->num_instances; i++) h->item_count[i] = int(per[i].size());
         if (h->persistent) {
             // Each item depends on the items of its instance within one tile and
             // one z-chunk (itself included): the halo it reads, and the reads of
@@ -1660,24 +1677,26 @@ gpe_status gpe_synchronize(gpe_handle h)
     GPE_GUARD(gpe_synchronize_impl(h));
 }
 
-static gpe_status gpe_observables_get_impl(gpe_handle h, int32_t field, gpe_observables *out)
+namespace {
+
+// The observables sums of every instance's field `field` into h->obs_sums: one
+// launch over all instances, then one CTA per instance folds its rows (the same
+// sums as one launch per instance).
+gpe_status enqueue_observables_all(gpe_handle h, int field)
 {
-    gpe_status st = check_handle(h);
-    if (st != GPE_OK) return st;
-    if (!out || (field != 0 && field != 1)) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_observables_get: bad arguments");
-    // every instance in one launch, then one CTA per instance folds its rows
-    // (the same sums as one launch per instance)
     GPE_CUDA_TRY(launch_observables_batch(h->cfg.lattice, h->cfg.precision, h->cfg.potential, h->idev, h->obs_cta_inst,
                                           h->obs_cta_begin, h->obs_total_ctas, field_buf(h, field), h->vpot,
                                           h->obs_batch_partials, h->stream));
     GPE_CUDA_TRY(launch_reduce_partials_batch(h->obs_batch_partials, h->obs_cta_begin, h->cfg.num_instances,
                                               h->obs_sums, h->stream));
     h->launches += 2;
-    std::vector<double> sums(6 * h->cfg.num_instances);
-    GPE_CUDA_TRY(cudaMemcpyAsync(sums.data(), h->obs_sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost,
-                                 h->stream));
-    st = sync_and_check(h);
-    if (st != GPE_OK) return st;
+    return GPE_OK;
+}
+
+// gpe_observables records from the six sums per instance.
+gpe_status observables_from_sums(gpe_handle h, const std::vector<double> &sums, gpe_observables *out,
+                                 const char *where)
+{
     bool all_finite = true;
     for (int i = 0; i < h->cfg.num_instances; i++) {
         const double vol = h->idev_host[i].vol;
@@ -1692,13 +1711,263 @@ static gpe_status gpe_observables_get_impl(gpe_handle h, int32_t field, gpe_obse
         o.pad_ = 0;
         all_finite = all_finite && o.finite;
     }
-    if (!all_finite) return fail(GPE_ERR_NOT_FINITE, "gpe_observables_get: NaN or Inf in the field");
+    if (!all_finite) return fail(GPE_ERR_NOT_FINITE, std::string(where) + ": NaN or Inf in the field");
     return GPE_OK;
+}
+
+}  // namespace
+
+static gpe_status gpe_observables_get_impl(gpe_handle h, int32_t field, gpe_observables *out)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    if (!out || (field != 0 && field != 1)) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_observables_get: bad arguments");
+    if ((st = enqueue_observables_all(h, field)) != GPE_OK) return st;
+    std::vector<double> sums(6 * h->cfg.num_instances);
+    GPE_CUDA_TRY(cudaMemcpyAsync(sums.data(), h->obs_sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost,
+                                 h->stream));
+    st = sync_and_check(h);
+    if (st != GPE_OK) return st;
+    return observables_from_sums(h, sums, out, "gpe_observables_get");
 }
 
 gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out)
 {
     GPE_GUARD(gpe_observables_get_impl(h, field, out));
+}
+
+namespace {
+
+// Instance groups of a round trip: contiguous runs of the work-item order, so
+// that each group's items are one contiguous range.  The first group holds half
+// a share of the values and the others one share each (cuts where the running
+// count passes (g + 1/2) / (G - 1/2) of the total): the steps wait for the first
+// group's upload alone.
+constexpr int kRoundTripGroups = 4;
+
+std::vector<std::vector<int>> round_trip_groups(gpe_handle h, bool split)
+{
+    const int n = h->cfg.num_instances;
+    std::vector<std::vector<int>> groups;
+    if (!split) {
+        groups.emplace_back(n);
+        for (int i = 0; i < n; i++) groups[0][i] = i;
+        return groups;
+    }
+    const int G = std::min(n, kRoundTripGroups);
+    auto values = [&](int i) { return (long long)h->inst[i].nx * h->inst[i].ny * h->inst[i].nz; };
+    long long total = 0;
+    for (int i = 0; i < n; i++) total += values(i);
+    groups.resize(1);
+    long long acc = 0;
+    for (int k = 0; k < n; k++) {
+        const int i = h->item_order[k];
+        const int g = int(groups.size()) - 1;
+        // close the group once it holds its share, if every later group still gets an instance
+        if (!groups[g].empty() && acc * (2 * G - 1) >= total * (2 * g + 1) && n - k >= G - g - 1 &&
+            int(groups.size()) < G)
+            groups.emplace_back();
+        groups.back().push_back(i);
+        acc += values(i);
+    }
+    return groups;
+}
+
+// On every way out of a round trip: the full item range for later step
+// launches again, and no copy still touching the caller's buffers.
+struct RoundTripExit {
+    gpe_handle h;
+    ~RoundTripExit()
+    {
+        h->run_first = h->run_count = 0;
+        if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+        if (h->down_stream) cudaStreamSynchronize(h->down_stream);
+    }
+};
+
+}  // namespace
+
+static gpe_status gpe_round_trip_impl(gpe_handle h, const void *const *even_in, const void *const *odd_in,
+                                      int64_t steps, void *const *even_out, void *const *odd_out,
+                                      gpe_observables *obs)
+{
+    gpe_status st = check_handle(h);
+    if (st != GPE_OK) return st;
+    const int n = h->cfg.num_instances;
+    const bool real = h->cfg.mode == GPE_REAL_TIME;
+    if (steps < 0) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_round_trip: negative step count");
+    if (!even_in || (real && !odd_in)) return fail(GPE_ERR_INVALID_ARGUMENT, "gpe_round_trip: null input array");
+    for (int i = 0; i < n; i++)
+        if (!even_in[i] || (real && !odd_in[i]))
+            return fail(GPE_ERR_INVALID_ARGUMENT,
+                        "gpe_round_trip: input field of instance " + std::to_string(i) + " is null");
+    // Groups step one after another only where a launch can cover a subset of
+    // the instances: the fused half-step kernels in real time, no slabs.
+    const bool split = real && h->fused && !h->two_step && !h->persistent && h->zlinks.empty() && steps > 0 &&
+                       int(h->item_order.size()) == n && n > 1;
+    const std::vector<std::vector<int>> groups = round_trip_groups(h, split);
+    const int G = int(groups.size());
+    // One staging slot per (instance, field), holding the upload and then the download.
+    std::vector<size_t> off(2 * size_t(n));
+    size_t total = 0;
+    for (int i = 0; i < n; i++) {
+        const gpe_instance &in = h->inst[i];
+        const size_t b = size_t(in.nx) * in.ny * in.nz * h->ns * 2 * h->hsize;
+        for (int f = 0; f < 2; f++) {
+            off[2 * i + f] = total;
+            const bool in_used = f == 0 || (odd_in && odd_in[i]);
+            const bool out_used = f == 0 ? (even_out && even_out[i]) : (odd_out && odd_out[i]);
+            if (in_used || out_used) total += slot_bytes(b);
+        }
+    }
+    st = ensure_batch_staging(h, std::max<size_t>(total, 256));
+    if (st == GPE_OK) st = ensure_xfer(h, size_t(2 * G + 1));
+    if (st != GPE_OK) return st;
+    if (!h->down_stream) GPE_CUDA_TRY(cudaStreamCreateWithFlags(&h->down_stream, cudaStreamNonBlocking));
+    RoundTripExit guard{h};
+    char *stage = (char *)h->batch_staging;
+    cudaEvent_t *ev = h->xfer_events.data();  // [0] start, [1..G] group uploaded, [G+1..2G] group converted
+    auto bytes_of = [&](int i) {
+        const gpe_instance &in = h->inst[i];
+        return size_t(in.nx) * in.ny * in.nz * h->ns * 2 * h->hsize;
+    };
+    // Layout conversions between the staging slots and the fields: one launch
+    // per group and direction (the batched transfer kernel, reading or writing
+    // the slots instead of host memory).  Every launch's segment table goes to
+    // the device here, before any work is queued.
+    std::vector<XferSeg> &segs = h->xfer_segs_host;
+    segs.clear();
+    std::vector<int> seg_at(2 * G), seg_n(2 * G), seg_ctas(2 * G);
+    for (int g = 0; g < G; g++)
+        for (int dir = 0; dir < 2; dir++) {
+            const int L = 2 * g + dir;
+            seg_at[L] = int(segs.size());
+            int cta = 0;
+            for (int i : groups[g])
+                for (int f = 0; f < 2; f++) {
+                    const bool used = dir == 0 ? (f == 0 || (odd_in && odd_in[i]))
+                                               : (f == 0 ? even_out && even_out[i] : odd_out && odd_out[i]);
+                    if (!used) continue;
+                    const long long vals = (long long)h->inst[i].nx * h->inst[i].ny * h->inst[i].nz * h->ns;
+                    segs.push_back({stage + off[2 * i + f], i, f, cta, 0});
+                    cta += int((vals + kXferValuesPerCta - 1) / kXferValuesPerCta);
+                }
+            seg_n[L] = int(segs.size()) - seg_at[L];
+            seg_ctas[L] = cta;
+            segs.push_back({nullptr, 0, 0, cta, 0});
+        }
+    if (segs.size() > h->xfer_segs_cap) {
+        cudaFree(h->xfer_segs);
+        h->xfer_segs = nullptr;
+        h->xfer_segs_cap = 0;
+        GPE_CUDA_TRY(cudaMalloc(&h->xfer_segs, sizeof(XferSeg) * segs.size()));
+        h->xfer_segs_cap = segs.size();
+    }
+    GPE_CUDA_TRY(cudaMemcpyAsync(h->xfer_segs, segs.data(), sizeof(XferSeg) * segs.size(), cudaMemcpyHostToDevice,
+                                 h->stream));
+    auto convert = [&](int g, bool up) -> gpe_status {
+        const int L = 2 * g + (up ? 0 : 1);
+        if (seg_n[L] == 0) return GPE_OK;
+        GPE_CUDA_TRY(launch_xfer_batch(h->cfg.precision, h->comp, h->host_fp32, up, h->idev, h->xfer_segs + seg_at[L],
+                                       seg_n[L], seg_ctas[L], field_buf(h, 0), field_buf(h, 1), h->lo[0], h->lo[1],
+                                       h->stream));
+        h->launches++;
+        return GPE_OK;
+    };
+    // Group g's copies up, on the copy stream, then its event ev[1 + g].
+    auto upload = [&](int g) -> gpe_status {
+        for (int i : groups[g]) {
+            const void *src[2] = {even_in[i], odd_in ? odd_in[i] : nullptr};
+            for (int f = 0; f < 2; f++)
+                if (src[f])
+                    GPE_CUDA_TRY(cudaMemcpyAsync(stage + off[2 * i + f], src[f], bytes_of(i), cudaMemcpyHostToDevice,
+                                                 h->copy_stream));
+        }
+        GPE_CUDA_TRY(cudaEventRecord(ev[1 + g], h->copy_stream));
+        return GPE_OK;
+    };
+    // Group g on the handle's stream: wait for its copies, convert, step,
+    // convert back into its slots, then ev[G + 1 + g].
+    std::vector<bool> has_out(G, false);
+    auto compute = [&](int g) -> gpe_status {
+        gpe_status s2;
+        GPE_CUDA_TRY(cudaStreamWaitEvent(h->stream, ev[1 + g], 0));
+        if ((s2 = convert(g, true)) != GPE_OK) return s2;
+        h->imag_ready = false;
+        if (split) {
+            // the group's instances are consecutive in the item order
+            int first = h->grid, count = 0;
+            for (int i : groups[g]) {
+                first = std::min(first, h->item_first[i]);
+                count += h->item_count[i];
+            }
+            h->run_first = first;
+            h->run_count = count;
+            s2 = run_steps(h, steps);
+        } else {
+            s2 = gpe_step_impl(h, steps);
+        }
+        if (s2 != GPE_OK) return s2;
+        has_out[g] = seg_n[2 * g + 1] > 0;
+        if ((s2 = convert(g, false)) != GPE_OK) return s2;
+        if (has_out[g]) GPE_CUDA_TRY(cudaEventRecord(ev[G + 1 + g], h->stream));
+        return GPE_OK;
+    };
+    // Group g's copies down, on the down stream, after its conversions.
+    auto download = [&](int g) -> gpe_status {
+        if (!has_out[g]) return GPE_OK;
+        GPE_CUDA_TRY(cudaStreamWaitEvent(h->down_stream, ev[G + 1 + g], 0));
+        for (int i : groups[g]) {
+            void *dst[2] = {even_out ? even_out[i] : nullptr, odd_out ? odd_out[i] : nullptr};
+            for (int f = 0; f < 2; f++)
+                if (dst[f])
+                    GPE_CUDA_TRY(cudaMemcpyAsync(dst[f], stage + off[2 * i + f], bytes_of(i), cudaMemcpyDeviceToHost,
+                                                 h->down_stream));
+        }
+        return GPE_OK;
+    };
+    // Host order U0, C0, U1, C1, U2, ...: every copy is queued after the
+    // compute it overlaps, so the overlap holds even where the runtime makes a
+    // copy call wait on the host.  Downloads queue once every upload is queued
+    // and wait for the last one, so an output buffer may be any instance's
+    // input buffer; they go in before the observables' read-back, which waits.
+    GPE_CUDA_TRY(cudaEventRecord(ev[0], h->stream));  // earlier work on the handle's stream first
+    GPE_CUDA_TRY(cudaStreamWaitEvent(h->copy_stream, ev[0], 0));
+    GPE_CUDA_TRY(cudaStreamWaitEvent(h->down_stream, ev[0], 0));
+    if ((st = upload(0)) != GPE_OK) return st;
+    if (G == 1) GPE_CUDA_TRY(cudaStreamWaitEvent(h->down_stream, ev[G], 0));
+    int next_down = 0;
+    for (int g = 0; g < G; g++) {
+        if ((st = compute(g)) != GPE_OK) return st;
+        if (g + 1 < G) {
+            if ((st = upload(g + 1)) != GPE_OK) return st;
+            if (g + 1 == G - 1) GPE_CUDA_TRY(cudaStreamWaitEvent(h->down_stream, ev[G], 0));
+        }
+        if (g + 1 >= G - 1)
+            while (next_down < g)
+                if ((st = download(next_down++)) != GPE_OK) return st;
+    }
+    while (next_down < G)
+        if ((st = download(next_down++)) != GPE_OK) return st;
+    // The observables run while the last group's fields travel down.
+    std::vector<double> sums;
+    if (obs) {
+        if ((st = enqueue_observables_all(h, 0)) != GPE_OK) return st;
+        sums.resize(6 * size_t(n));
+        GPE_CUDA_TRY(cudaMemcpyAsync(sums.data(), h->obs_sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost,
+                                     h->stream));
+    }
+    GPE_CUDA_TRY(cudaStreamSynchronize(h->down_stream));
+    GPE_CUDA_TRY(cudaStreamSynchronize(h->copy_stream));
+    st = sync_and_check(h);
+    if (st != GPE_OK) return st;
+    return obs ? observables_from_sums(h, sums, obs, "gpe_round_trip") : GPE_OK;
+}
+
+gpe_status gpe_round_trip(gpe_handle h, const void *const *even_in, const void *const *odd_in, int64_t steps,
+                          void *const *even_out, void *const *odd_out, gpe_observables *obs)
+{
+    GPE_GUARD(gpe_round_trip_impl(h, even_in, odd_in, steps, even_out, odd_out, obs));
 }
 
 static gpe_status gpe_observables_get_impl(gpe_handle h, int32_t field, gpe_observables *out);

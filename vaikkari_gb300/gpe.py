@@ -193,6 +193,8 @@ def load_library(path: str = LIB_PATH):
     lib.gpe_download_many.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), vpp, vpp]
     lib.gpe_step.restype = st
     lib.gpe_step.argtypes = [C.c_void_p, C.c_int64]
+    lib.gpe_round_trip.restype = st
+    lib.gpe_round_trip.argtypes = [C.c_void_p, vpp, vpp, C.c_int64, vpp, vpp, C.POINTER(_Observables)]
     lib.gpe_synchronize.restype = st
     lib.gpe_synchronize.argtypes = [C.c_void_p]
     lib.gpe_observables_get.restype = st
@@ -461,6 +463,44 @@ class Stepper:
 
     def step(self, steps: int):
         _check(self.lib.gpe_step(self.h, int(steps)), "gpe_step")
+
+    def round_trip(self, inputs, steps: int, outs=None, observables: bool = True):
+        """gpe_round_trip: upload every instance, `steps` steps, the observables
+        of field 0, download.  inputs: one (even, odd) pair per instance in the
+        host element type (odd may be None in imaginary time); outs: (even, odd)
+        arrays to fill (None entries are not downloaded; default: new arrays).
+        Returns (outs, observables list or None)."""
+        n = len(self.instances)
+        if len(inputs) != n:
+            raise ValueError(f"round_trip takes one input pair per instance ({n})")
+        keep, pe, po = [], [], []
+        for i, (even, odd) in enumerate(inputs):
+            shp = self.shape(i)
+            e, p_e = self._carray(even, shp)
+            o, p_o = self._carray(odd, shp)
+            keep += [e, o]
+            pe.append(p_e)
+            po.append(p_o)
+        if outs is None:
+            outs = [(np.empty(self.shape(i) + (2,), self.field_dtype), np.empty(self.shape(i) + (2,), self.field_dtype))
+                    for i in range(n)]
+        for i, (e, o) in enumerate(outs):
+            want = self.shape(i) + (2,)
+            for a in (e, o):
+                if a is not None and (a.shape != want or a.dtype != self.field_dtype or not a.flags.c_contiguous):
+                    raise ValueError(f"output array for instance {i} must be C-contiguous {self.field_dtype} {want}")
+        arr = lambda xs: (C.c_void_p * n)(*[x.value if x is not None else None for x in xs])
+        oe = (C.c_void_p * n)(*[e.ctypes.data if e is not None else None for e, _ in outs])
+        oo = (C.c_void_p * n)(*[o.ctypes.data if o is not None else None for _, o in outs])
+        obs = (_Observables * n)() if observables else None
+        st = self.lib.gpe_round_trip(self.h, arr(pe), arr(po) if any(x is not None for x in po) else None,
+                                     int(steps), oe, oo, obs)
+        res = None
+        if observables:
+            res = [{k: getattr(o, k) for k in ("norm", "energy", "mu", "kinetic", "potential", "interaction")}
+                   | {"finite": bool(o.finite)} for o in obs]
+        _check(st, "gpe_round_trip")
+        return outs, res
 
     def synchronize(self):
         _check(self.lib.gpe_synchronize(self.h), "gpe_synchronize")
