@@ -884,6 +884,30 @@ __global__ void scale_field_kernel(const InstDev *__restrict__ insts, int ii, T 
     }
 }
 
+// Host value -> FP32 value hi and the part below it, r = float(x - hi) (x - hi is
+// exact in double).  A float host value is its own hi; its r is hi - hi (zero,
+// or NaN for Inf/NaN as in the double form) with no FP64 arithmetic, which runs
+// at a small fraction of the FP32 rate on this GPU.
+__device__ __forceinline__ void comp_split(double x, float &hi, float &r)
+{
+    hi = __double2float_rn(x);
+    r = __double2float_rn(x - double(hi));
+}
+__device__ __forceinline__ void comp_split(float x, float &hi, float &r)
+{
+    hi = x;
+    r = __fsub_rn(x, x);
+}
+// hi + lo rounded once to the host type.  For float the exact sum (hi and lo
+// span at most 33 significant bits, so double holds it) rounded to float is the
+// correctly rounded float sum, which __fadd_rn gives directly.
+template <typename H> __device__ __forceinline__ H comp_join(float hi, float lo);
+template <> __device__ __forceinline__ double comp_join<double>(float hi, float lo)
+{
+    return double(hi) + double(lo);
+}
+template <> __device__ __forceinline__ float comp_join<float>(float hi, float lo) { return __fadd_rn(hi, lo); }
+
 // GPE_FP32C transfers.  Upload: a double x becomes hi = float(x) and the int8
 // residual of float(x - hi) (x - hi is exact in double) in units of ulp(hi)/256;
 // download: double(hi) + double(residual).  lo holds both components in one
@@ -900,13 +924,12 @@ __global__ void pack_split_kernel(const InstDev *__restrict__ insts, int ii, con
         digits(v, d.slots, d.nx, d.ny, s, x, y, z);
         const long long o = field_index(d, s, x, y, z);
         const typename Cplx<H>::type hv = ((const typename Cplx<H>::type *)src)[v];
-        const double a = double(hv.x), b = double(hv.y);
-        const float ha = __double2float_rn(a), hb = __double2float_rn(b);
+        float ha, hb, ra, rb;
+        comp_split(hv.x, ha, ra);
+        comp_split(hv.y, hb, rb);
         ((float2 *)hi)[o] = make_float2(ha, hb);
         // residual = the part of the value below FP32, in units of ulp(hi) / 256
-        const uint32_t qa = comp_encode(__double2float_rn(a - double(ha)), ha);
-        const uint32_t qb = comp_encode(__double2float_rn(b - double(hb)), hb);
-        lo[o - kLoShift] = uint16_t(qa | (qb << 8));
+        lo[o - kLoShift] = uint16_t(comp_encode(ra, ha) | (comp_encode(rb, hb) << 8));
     }
 }
 
@@ -926,8 +949,8 @@ __global__ void unpack_join_kernel(const InstDev *__restrict__ insts, int ii, co
         const float ha = hv.x, hb = hv.y;
         const float2 lf = make_float2(comp_decode(w, ha), comp_decode(w >> 8, hb));
         typename Cplx<H>::type out;
-        out.x = H(double(ha) + double(lf.x));
-        out.y = H(double(hb) + double(lf.y));
+        out.x = comp_join<H>(ha, lf.x);
+        out.y = comp_join<H>(hb, lf.y);
         ((typename Cplx<H>::type *)dst)[v] = out;
     }
 }
@@ -1040,20 +1063,19 @@ __global__ void __launch_bounds__(256) xfer_batch_kernel(const InstDev *__restri
         const long long o = field_index(d, s, x, y, z);
         if constexpr (UP && COMP) {
             const H2 hv = hin[k];
-            const double va = double(hv.x), vb = double(hv.y);
-            const float ha = __double2float_rn(va), hb = __double2float_rn(vb);
+            float ha, hb, ra, rb;
+            comp_split(hv.x, ha, ra);
+            comp_split(hv.y, hb, rb);
             field[o] = make_float2(ha, hb);
-            const uint32_t qa = comp_encode(__double2float_rn(va - double(ha)), ha);
-            const uint32_t qb = comp_encode(__double2float_rn(vb - double(hb)), hb);
-            lo[o - kLoShift] = uint16_t(qa | (qb << 8));
+            lo[o - kLoShift] = uint16_t(comp_encode(ra, ha) | (comp_encode(rb, hb) << 8));
         } else if constexpr (UP) {
             field[o] = hin[k];
         } else if constexpr (COMP) {
             const uint32_t w = lo[o - kLoShift];
             const float2 hv = field[o];
             H2 out;
-            out.x = H(double(hv.x) + double(comp_decode(w, hv.x)));
-            out.y = H(double(hv.y) + double(comp_decode(w >> 8, hv.y)));
+            out.x = comp_join<H>(hv.x, comp_decode(w, hv.x));
+            out.y = comp_join<H>(hv.y, comp_decode(w >> 8, hv.y));
             ((H2 *)g.host)[v] = out;
         } else {
             ((T2 *)g.host)[v] = field[o];
