@@ -483,10 +483,12 @@ gpe_status gpe_write_bmp(const char *path, const uint8_t *rgb, uint32_t width, u
  * every GPU that loads the library; each row covers GPE_NOALLOC_VALUES_PER_ROW
  * values, so inputs of more than 16,777,216 values return GPE_ERR_TOO_LARGE.
  * All calls share that array: calls that overlap on a GPU race and must be
- * serialised by the caller.  The first call on a device looks the array up and
- * should come before any stream capture; the address is kept per device for the
- * context it was found in, so after cudaDeviceReset (a new context) the next
- * call looks it up again.  It allocates nothing when it succeeds; a failure
+ * serialised by the caller.  No call may be made while its stream (or the
+ * legacy default stream) is being captured into a graph: every call waits for
+ * its stream and reads the sums back to the host, neither of which a capture
+ * allows.  The array's address is looked up on a device's first call and kept
+ * for the context it was found in, so after cudaDeviceReset (a new context) the
+ * next call looks it up again.  It allocates nothing when it succeeds; a failure
  * records its message for gpe_last_error() as every call does.  A field that is
  * zero everywhere has no mu and returns GPE_ERR_NOT_FINITE with its own message.
  * The kinetic term uses the lattice's own weights (a face table's weights are
