@@ -243,9 +243,10 @@ gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out
  * imaginary time; even_out, odd_out, obs and any output entry may be NULL (not
  * downloaded).  An output buffer may be any instance's input buffer.
  * In real time with the fused half-step kernels (no slabs) the instances go in up
- * to four groups of about equal size, contiguous in the work-item order: the
- * copy engines move group g+1 up and group g-1 down while the SMs step group g,
- * and the last group's download runs beside the observables.  Overlap needs
+ * to four groups, contiguous in the work-item order: the copy engines move the
+ * groups up and down while the SMs step the others; a group joins the running
+ * step launches once its copy should have landed and leaves after its steps, and
+ * the last group's download runs beside the observables.  Overlap needs
  * page-locked host buffers; a pageable one makes its copy wait for the host.
  * Replaces the reference's upload (cudaMemcpy3D, GPUGrossPitaevskii_BCC.cu:
  * 370-391), its step loop (475-481) and its download (484), which run one after

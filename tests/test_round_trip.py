@@ -79,15 +79,18 @@ def _compare(got, want):
 
 
 def _step_launches(lattice, kernel, tile, groups, steps):
-    """Step launches one round trip issues; None where not fixed (plain kernels)."""
+    """(fewest, most) step launches of one round trip; None where not fixed
+    (plain kernels).  Groups that step at the same time share launches: at
+    least steps + groups - 1 rounds of two half-step launches, at most one
+    group per round."""
     if kernel != Kernel.FUSED:
         return None
     kind = variants()[tile]["kind"] if lattice == Lattice.BCC2 else 0
     if kind == 2:      # persistent: one launch per call
-        return 1
+        return 1, 1
     if kind == 1:      # two-step: one launch per step
-        return steps
-    return groups * 2 * steps
+        return steps, steps
+    return 2 * (steps + groups - 1), 2 * steps * groups
 
 
 # (lattice, precision, host precision, potential, kernel, tile, groups expected)
@@ -121,10 +124,11 @@ def test_round_trip_equals_calls_in_sequence(lattice, prec, host, potential, ker
         b.upload_many([(i, pairs[i][0], pairs[i][1], V[i]) for i in range(len(insts))])
     n0 = b.launch_count()
     got = b.round_trip(pairs, steps)
-    launches = _step_launches(lattice, kernel, tile, groups, steps)
-    if launches is not None:
+    bounds = _step_launches(lattice, kernel, tile, groups, steps)
+    if bounds is not None:
         # one conversion launch per group each way, 2 observables launches, the step launches
-        assert b.launch_count() - n0 == 2 * groups + 2 + launches
+        stepping = b.launch_count() - n0 - 2 * groups - 2
+        assert bounds[0] <= stepping <= bounds[1], (stepping, bounds)
     _compare(got, want)
     a.close()
     b.close()

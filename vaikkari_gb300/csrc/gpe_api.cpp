@@ -1801,8 +1801,8 @@ static gpe_status gpe_round_trip_impl(gpe_handle h, const void *const *even_in, 
         if (!even_in[i] || (real && !odd_in[i]))
             return fail(GPE_ERR_INVALID_ARGUMENT,
                         "gpe_round_trip: input field of instance " + std::to_string(i) + " is null");
-    // Groups step one after another only where a launch can cover a subset of
-    // the instances: the fused half-step kernels in real time, no slabs.
+    // Instance groups only where a launch can cover a subset of the instances:
+    // the fused half-step kernels in real time, no slabs.
     const bool split = real && h->fused && !h->two_step && !h->persistent && h->zlinks.empty() && steps > 0 &&
                        int(h->item_order.size()) == n && n > 1;
     const std::vector<std::vector<int>> groups = round_trip_groups(h, split);
@@ -1886,30 +1886,19 @@ static gpe_status gpe_round_trip_impl(gpe_handle h, const void *const *even_in, 
         GPE_CUDA_TRY(cudaEventRecord(ev[1 + g], h->copy_stream));
         return GPE_OK;
     };
-    // Group g on the handle's stream: wait for its copies, convert, step,
-    // convert back into its slots, then ev[G + 1 + g].
+    // Group g joins: wait for its copies, convert them into the fields.
     std::vector<bool> has_out(G, false);
-    auto compute = [&](int g) -> gpe_status {
-        gpe_status s2;
+    auto join_group = [&](int g) -> gpe_status {
         GPE_CUDA_TRY(cudaStreamWaitEvent(h->stream, ev[1 + g], 0));
-        if ((s2 = convert(g, true)) != GPE_OK) return s2;
+        gpe_status s2 = convert(g, true);
         h->imag_ready = false;
-        if (split) {
-            // the group's instances are consecutive in the item order
-            int first = h->grid, count = 0;
-            for (int i : groups[g]) {
-                first = std::min(first, h->item_first[i]);
-                count += h->item_count[i];
-            }
-            h->run_first = first;
-            h->run_count = count;
-            s2 = run_steps(h, steps);
-        } else {
-            s2 = gpe_step_impl(h, steps);
-        }
-        if (s2 != GPE_OK) return s2;
+        return s2;
+    };
+    // Group g leaves: convert its fields into its slots, then ev[G + 1 + g].
+    auto leave_group = [&](int g) -> gpe_status {
         has_out[g] = seg_n[2 * g + 1] > 0;
-        if ((s2 = convert(g, false)) != GPE_OK) return s2;
+        gpe_status s2 = convert(g, false);
+        if (s2 != GPE_OK) return s2;
         if (has_out[g]) GPE_CUDA_TRY(cudaEventRecord(ev[G + 1 + g], h->stream));
         return GPE_OK;
     };
@@ -1926,27 +1915,98 @@ static gpe_status gpe_round_trip_impl(gpe_handle h, const void *const *even_in, 
         }
         return GPE_OK;
     };
-    // Host order U0, C0, U1, C1, U2, ...: every copy is queued after the
-    // compute it overlaps, so the overlap holds even where the runtime makes a
-    // copy call wait on the host.  Downloads queue once every upload is queued
-    // and wait for the last one, so an output buffer may be any instance's
-    // input buffer; they go in before the observables' read-back, which waits.
+    // Rolling schedule.  A round advances every group then active by one
+    // leapfrog step, in launches over the active groups' items (consecutive in
+    // the item order).  Group g is active in rounds join[g] .. join[g] + K - 1:
+    // groups join in order as their uploads should have landed and leave in
+    // order after K steps, so most launches cover several groups.  Group g + 1
+    // joins once the rounds since group g joined have stepped about R times its
+    // values, R being how much longer a value takes to come over the host link
+    // (about 200 GB/s; 4 host elements per value) than to take one step in HBM
+    // (about 6 TB/s; B bytes per value-step).  An estimate off either way only
+    // costs overlap: a group's first launch waits for its copies.  Without
+    // groups the one group is active in every round.
+    std::vector<long long> join(G, 0);
+    if (split) {
+        std::vector<double> gv(G, 0.0);
+        for (int g = 0; g < G; g++)
+            for (int i : groups[g]) gv[g] += double(h->inst[i].nx) * h->inst[i].ny * h->inst[i].nz * h->ns;
+        const double B = h->comp ? 56.0 : (h->cfg.precision == GPE_FP64 ? 96.0 : 48.0);
+        const double R = 4.0 * double(h->hsize) / 200.0 * 6000.0 / B;
+        for (int g = 0; g + 1 < G; g++) {
+            double acc = 0.0;
+            long long r = join[g];
+            do {
+                for (int q = 0; q <= g; q++)
+                    if (join[q] <= r && r < join[q] + steps) acc += gv[q];
+                r++;
+            } while (acc < R * gv[g + 1] && r < join[g] + steps);
+            join[g + 1] = r;
+        }
+    }
+    // The schedule in pieces of constant active set, cut where a group joins or leaves.
+    std::vector<long long> cuts = {0};
+    for (int g = 0; g < G; g++) {
+        cuts.push_back(join[g]);
+        cuts.push_back(join[g] + steps);
+    }
+    std::sort(cuts.begin(), cuts.end());
+    cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+    // Host order: U0, then every copy is queued after the compute it overlaps
+    // (U(g+1) after group g's first piece), so the overlap holds even where the
+    // runtime makes a copy call wait on the host.  Downloads queue once every
+    // upload is queued and wait for the last one, so an output buffer may be any
+    // instance's input buffer; they go in before the observables' read-back,
+    // which waits.
     GPE_CUDA_TRY(cudaEventRecord(ev[0], h->stream));  // earlier work on the handle's stream first
     GPE_CUDA_TRY(cudaStreamWaitEvent(h->copy_stream, ev[0], 0));
     GPE_CUDA_TRY(cudaStreamWaitEvent(h->down_stream, ev[0], 0));
     if ((st = upload(0)) != GPE_OK) return st;
+    int uploaded = 1, left = 0, next_down = 0;
     if (G == 1) GPE_CUDA_TRY(cudaStreamWaitEvent(h->down_stream, ev[G], 0));
-    int next_down = 0;
-    for (int g = 0; g < G; g++) {
-        if ((st = compute(g)) != GPE_OK) return st;
-        if (g + 1 < G) {
-            if ((st = upload(g + 1)) != GPE_OK) return st;
-            if (g + 1 == G - 1) GPE_CUDA_TRY(cudaStreamWaitEvent(h->down_stream, ev[G], 0));
+    for (size_t c = 0; c + 1 < cuts.size(); c++) {
+        const long long r0 = cuts[c], r1 = cuts[c + 1];
+        int lo = G, hi = -1;
+        for (int g = 0; g < G; g++) {
+            if (join[g] == r0 && (st = join_group(g)) != GPE_OK) return st;
+            if (join[g] <= r0 && r0 < join[g] + steps) {
+                lo = std::min(lo, g);
+                hi = std::max(hi, g);
+            }
         }
-        if (g + 1 >= G - 1)
-            while (next_down < g)
+        if (lo <= hi) {
+            if (split) {
+                h->run_first = h->item_first[groups[lo][0]];
+                h->run_count = 0;
+                for (int g = lo; g <= hi; g++)
+                    for (int i : groups[g]) {
+                        h->run_first = std::min(h->run_first, h->item_first[i]);
+                        h->run_count += h->item_count[i];
+                    }
+                st = run_steps(h, r1 - r0);
+            } else {
+                st = gpe_step_impl(h, r1 - r0);
+            }
+            if (st != GPE_OK) return st;
+        }
+        for (int g = 0; g < G; g++)
+            if (join[g] + steps == r1 && (st = leave_group(g)) != GPE_OK) return st;
+        while (left < G && join[left] + steps <= r1) left++;
+        while (uploaded < G && join[uploaded - 1] <= r0) {
+            if ((st = upload(uploaded++)) != GPE_OK) return st;
+            if (uploaded == G) GPE_CUDA_TRY(cudaStreamWaitEvent(h->down_stream, ev[G], 0));
+        }
+        if (uploaded == G)
+            while (next_down < left)
                 if ((st = download(next_down++)) != GPE_OK) return st;
     }
+    while (uploaded < G) {
+        if ((st = upload(uploaded++)) != GPE_OK) return st;
+        if (uploaded == G) GPE_CUDA_TRY(cudaStreamWaitEvent(h->down_stream, ev[G], 0));
+    }
+    if (steps == 0)  // no rounds: convert and return the fields as uploaded
+        for (int g = 0; g < G; g++)
+            if ((st = join_group(g)) != GPE_OK || (st = leave_group(g)) != GPE_OK) return st;
     while (next_down < G)
         if ((st = download(next_down++)) != GPE_OK) return st;
     // The observables run while the last group's fields travel down.
