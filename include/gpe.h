@@ -241,7 +241,8 @@ gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out
  * gpe_download_many.  Arrays hold num_instances pointers indexed by instance, in
  * the host element type (gpe_set_host_precision); odd_in may be NULL in
  * imaginary time; even_out, odd_out, obs and any output entry may be NULL (not
- * downloaded).  An output buffer may be any instance's input buffer.
+ * downloaded).  An output buffer may be any instance's input buffer.  A
+ * GPE_POTENTIAL_ARRAY potential is not moved: the one last uploaded stays.
  * In real time with the fused half-step kernels (no slabs) the instances go in up
  * to four groups, contiguous in the work-item order: the copy engines move the
  * groups up and down while the SMs step the others; a group joins the running
