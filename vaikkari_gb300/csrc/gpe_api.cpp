@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "gpe_internal.h"
+#include "gpe_round_trip_plan.h"
 
 namespace gpe {
 
@@ -1738,41 +1739,6 @@ gpe_status gpe_observables_get(gpe_handle h, int32_t field, gpe_observables *out
 
 namespace {
 
-// Instance groups of a round trip: contiguous runs of the work-item order, so
-// that each group's items are one contiguous range.  The first group holds half
-// a share of the values and the others one share each (cuts where the running
-// count passes (g + 1/2) / (G - 1/2) of the total): the steps wait for the first
-// group's upload alone.
-constexpr int kRoundTripGroups = 4;
-
-std::vector<std::vector<int>> round_trip_groups(gpe_handle h, bool split)
-{
-    const int n = h->cfg.num_instances;
-    std::vector<std::vector<int>> groups;
-    if (!split) {
-        groups.emplace_back(n);
-        for (int i = 0; i < n; i++) groups[0][i] = i;
-        return groups;
-    }
-    const int G = std::min(n, kRoundTripGroups);
-    auto values = [&](int i) { return (long long)h->inst[i].nx * h->inst[i].ny * h->inst[i].nz; };
-    long long total = 0;
-    for (int i = 0; i < n; i++) total += values(i);
-    groups.resize(1);
-    long long acc = 0;
-    for (int k = 0; k < n; k++) {
-        const int i = h->item_order[k];
-        const int g = int(groups.size()) - 1;
-        // close the group once it holds its share, if every later group still gets an instance
-        if (!groups[g].empty() && acc * (2 * G - 1) >= total * (2 * g + 1) && n - k >= G - g - 1 &&
-            int(groups.size()) < G)
-            groups.emplace_back();
-        groups.back().push_back(i);
-        acc += values(i);
-    }
-    return groups;
-}
-
 // On every way out of a round trip: the full item range for later step
 // launches again, and no copy still touching the caller's buffers.
 struct RoundTripExit {
@@ -1805,7 +1771,16 @@ static gpe_status gpe_round_trip_impl(gpe_handle h, const void *const *even_in, 
     // the fused half-step kernels in real time, no slabs.
     const bool split = real && h->fused && !h->two_step && !h->persistent && h->zlinks.empty() && steps > 0 &&
                        int(h->item_order.size()) == n && n > 1;
-    const std::vector<std::vector<int>> groups = round_trip_groups(h, split);
+    // Groups and their rolling schedule (gpe_round_trip_plan.h).  R: a value's
+    // upload (four host elements at about 200 GB/s over the host link) against
+    // one step of it in HBM (B bytes per value-step at about 6 TB/s).
+    std::vector<long long> values(n);
+    for (int i = 0; i < n; i++) values[i] = (long long)h->inst[i].nx * h->inst[i].ny * h->inst[i].nz * h->ns;
+    const double B = h->comp ? 56.0 : (h->cfg.precision == GPE_FP64 ? 96.0 : 48.0);
+    const RoundTripPlan plan =
+        plan_round_trip(values, h->item_order, split, steps, 4.0 * double(h->hsize) / 200.0 * 6000.0 / B);
+    const std::vector<std::vector<int>> &groups = plan.groups;
+    const std::vector<long long> &join = plan.join;
     const int G = int(groups.size());
     // One staging slot per (instance, field), holding the upload and then the download.
     std::vector<size_t> off(2 * size_t(n));
@@ -1915,43 +1890,11 @@ static gpe_status gpe_round_trip_impl(gpe_handle h, const void *const *even_in, 
         }
         return GPE_OK;
     };
-    // Rolling schedule.  A round advances every group then active by one
-    // leapfrog step, in launches over the active groups' items (consecutive in
-    // the item order).  Group g is active in rounds join[g] .. join[g] + K - 1:
-    // groups join in order as their uploads should have landed and leave in
-    // order after K steps, so most launches cover several groups.  Group g + 1
-    // joins once the rounds since group g joined have stepped about R times its
-    // values, R being how much longer a value takes to come over the host link
-    // (about 200 GB/s; 4 host elements per value) than to take one step in HBM
-    // (about 6 TB/s; B bytes per value-step).  An estimate off either way only
-    // costs overlap: a group's first launch waits for its copies.  Without
-    // groups the one group is active in every round.
-    std::vector<long long> join(G, 0);
-    if (split) {
-        std::vector<double> gv(G, 0.0);
-        for (int g = 0; g < G; g++)
-            for (int i : groups[g]) gv[g] += double(h->inst[i].nx) * h->inst[i].ny * h->inst[i].nz * h->ns;
-        const double B = h->comp ? 56.0 : (h->cfg.precision == GPE_FP64 ? 96.0 : 48.0);
-        const double R = 4.0 * double(h->hsize) / 200.0 * 6000.0 / B;
-        for (int g = 0; g + 1 < G; g++) {
-            double acc = 0.0;
-            long long r = join[g];
-            do {
-                for (int q = 0; q <= g; q++)
-                    if (join[q] <= r && r < join[q] + steps) acc += gv[q];
-                r++;
-            } while (acc < R * gv[g + 1] && r < join[g] + steps);
-            join[g + 1] = r;
-        }
-    }
-    // The schedule in pieces of constant active set, cut where a group joins or leaves.
-    std::vector<long long> cuts = {0};
-    for (int g = 0; g < G; g++) {
-        cuts.push_back(join[g]);
-        cuts.push_back(join[g] + steps);
-    }
-    std::sort(cuts.begin(), cuts.end());
-    cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+    // The rounds: every active group advances one leapfrog step per round, in
+    // launches over the active groups' items (consecutive in the item order);
+    // groups join as their uploads should have landed and leave after K steps,
+    // so most launches cover several groups.  A group's first launch waits for
+    // its copies, so an estimate off either way only costs overlap.
     // Host order: U0, then every copy is queued after the compute it overlaps
     // (U(g+1) after group g's first piece), so the overlap holds even where the
     // runtime makes a copy call wait on the host.  Downloads queue once every
@@ -1964,16 +1907,11 @@ static gpe_status gpe_round_trip_impl(gpe_handle h, const void *const *even_in, 
     if ((st = upload(0)) != GPE_OK) return st;
     int uploaded = 1, left = 0, next_down = 0;
     if (G == 1) GPE_CUDA_TRY(cudaStreamWaitEvent(h->down_stream, ev[G], 0));
-    for (size_t c = 0; c + 1 < cuts.size(); c++) {
-        const long long r0 = cuts[c], r1 = cuts[c + 1];
-        int lo = G, hi = -1;
-        for (int g = 0; g < G; g++) {
+    for (const RoundTripPiece &piece : plan.pieces) {
+        const long long r0 = piece.r0, r1 = piece.r1;
+        const int lo = piece.lo, hi = piece.hi;
+        for (int g = 0; g < G; g++)
             if (join[g] == r0 && (st = join_group(g)) != GPE_OK) return st;
-            if (join[g] <= r0 && r0 < join[g] + steps) {
-                lo = std::min(lo, g);
-                hi = std::max(hi, g);
-            }
-        }
         if (lo <= hi) {
             if (split) {
                 h->run_first = h->item_first[groups[lo][0]];
