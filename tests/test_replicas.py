@@ -122,3 +122,15 @@ def test_autotune_cache_survives_concurrent_writers(tmp_path):
     mp.start_processes(_tune_writer, args=(path, 20), nprocs=4, join=True, start_method="spawn")
     db = json.load(open(path))
     assert len(db) >= 20 and all(k.startswith("rank") for k in db)
+
+
+def test_autotune_refuses_other_lattices():
+    """The autotuner's variants are the BCC2 fused kernel's: a TETRA12 batch is
+    refused before anything is timed or cached."""
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import pytest
+    from vaikkari_gb300.autotune import autotune
+    from vaikkari_gb300.gpe import Instance, Lattice
+    with pytest.raises(ValueError):
+        autotune([Instance(4, 4, 4, 0.1, 1e-3, 1.0)], lattice=Lattice.TETRA12, cache=False)

@@ -94,7 +94,11 @@ def autotune(instances: List[Instance], fields=None, lattice=Lattice.BCC2, preci
     automatic z-chunk, then the three fastest with each z-chunk in `zchunks`.
     Imaginary time and compensated storage (Precision.FP32C) skip the variants
     that advance whole real-time steps; imaginary time also skips the persistent
-    variants (real time only)."""
+    variants (real time only).  The variants are the BCC2 fused kernel's; other
+    lattices are refused (the fused TETRA12 kernel's six tiles are chosen with
+    gpe_config.tile directly)."""
+    if Lattice(lattice) != Lattice.BCC2:
+        raise ValueError("autotune times the BCC2 fused kernel's variants; pass tile directly for other lattices")
     name = _device_name(device)
     sig = signature(instances, lattice, precision, potential, name, mode)
     db = _load() if cache else {}
